@@ -1,0 +1,172 @@
+/*
+ * subsweep_gpu.h — C ABI of the GB300 sweep library.
+ *
+ * Drop-in for the reference's radiative-transfer sweep + hydrogen-only chemistry
+ * (Tehforsch/subsweep, src/sweep/ and src/chemistry/).  The Rust host keeps its
+ * ECS/plugin framework and calls these entry points through `extern "C"` from a
+ * `GpuSweepPlugin` whose two systems replace the reference's:
+ *
+ *   init_sweep_system  (src/sweep/mod.rs:634-692)  ->  sw_create
+ *   run_sweep_system   (src/sweep/mod.rs:694-739)  ->  sw_step + sw_get_fields
+ *
+ * Plain pointers and sizes only; no CUDA or torch types cross the boundary.  The
+ * library owns all device memory.  One host thread per handle; calls on a handle
+ * are not re-entrant.  All quantities are SI doubles (m, kg, s, K), as the
+ * reference's diman quantities store them.
+ */
+#ifndef SUBSWEEP_GPU_H
+#define SUBSWEEP_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference aborts (panic!/assert!/unwrap) where these return. */
+typedef enum {
+  SW_OK = 0,
+  SW_ERR_INVALID_ARG = 1, /* bad parameters / grid / fields (reference: panic) */
+  SW_ERR_CUDA = 2,        /* CUDA runtime error; sw_last_error has the message */
+  SW_ERR_STALLED = 3,     /* a level sweep could not finish: dependency cycle
+                             (reference: deadlock; check_deadlock analogue) or a
+                             device wait that ran past its time limit */
+  SW_ERR_OOM = 4,         /* device allocation failed */
+  SW_ERR_UNSUPPORTED = 5  /* rotate_directions, > 128 directions, > 64 faces/cell */
+} sw_status;
+
+/* Arithmetic of the transport sweep.  FP64 is the plain drop-in (FP64 end to end).
+ * MIXED runs the sweep in FP32 (scaled photon rates, FP32 face weights, compensated
+ * per-cell rate sums) and keeps FP64 for the chemistry solve, the neutral fraction
+ * (carried as 1 - x_HII) and the timescale-to-level assignment. */
+typedef enum { SW_PRECISION_FP64 = 0, SW_PRECISION_MIXED = 1 } sw_precision;
+
+/* Neighbour kinds of a face, as src/sweep/grid/cell.rs:16-23 on a single rank. */
+enum { SW_FACE_LOCAL = 0, SW_FACE_LOCAL_PERIODIC = 1, SW_FACE_BOUNDARY = 2 };
+
+/* Mirrors SweepParameters (src/sweep/parameters.rs:8-46) plus the scale factor
+ * (Cosmology::scale_factor) and the precision choice.  sw_default_params fills the
+ * reference's serde defaults (parameters.rs:64-78). */
+typedef struct {
+  /* DirectionsSpecification::Num (parameters.rs:48-62): 1, 16, 21, 32, 64 or 84. */
+  int32_t num_directions;
+  /* DirectionsSpecification::Explicit: if non-NULL, num_directions vectors
+   * (xyz interleaved); each is normalised as Directions::from does (direction/mod.rs:97-108). */
+  const double* explicit_directions;
+  int32_t num_timestep_levels; /* >= 1, <= 16 */
+  int32_t periodic;            /* informational; periodicity is carried by face kinds */
+  double max_timestep;         /* s */
+  int32_t rotate_directions;   /* must be 0 */
+  double significant_rate_threshold;       /* photons/s, default 0 */
+  double timestep_safety_factor;           /* default 0.1 */
+  double chemistry_timestep_safety_factor; /* default 0.1 */
+  int32_t check_deadlock;      /* 1: verify the dependency graph is acyclic at sw_create */
+  int32_t prevent_cooling;     /* default 1 */
+  int64_t num_tasks_to_solve_before_send_receive; /* MPI batching knob; accepted, unused */
+  double scale_factor;         /* Cosmology::scale_factor(); 1 when non-cosmological */
+  int32_t precision;           /* sw_precision */
+  int32_t device;              /* CUDA device ordinal; -1 = the calling thread's current device */
+} sw_params;
+
+/* Face-neighbour CSR uploaded once (replaces the Cell component, grid/cell.rs:92-97).
+ * Faces of cell c are row_ptr[c] .. row_ptr[c+1]-1.  Normals must be exactly
+ * antisymmetric between the two sides of a face (true for generator-difference
+ * normals).  The host owns these arrays; sw_create copies them. */
+typedef struct {
+  int64_t num_cells;
+  const int64_t* row_ptr; /* [num_cells + 1] */
+  const int32_t* nbr;     /* [E] neighbour index (ignored for boundary faces) */
+  const uint8_t* kind;    /* [E] SW_FACE_* */
+  const double* area;     /* [E] m^2 */
+  const double* normal;   /* [E * 3] unit normals, xyz interleaved */
+  const double* volume;   /* [num_cells] m^3 */
+  const double* size;     /* [num_cells] m (cbrt(3V / 4pi) for Voronoi cells) */
+} sw_grid_csr;
+
+/* Per-cell initial components read by init_sweep_system (src/sweep/mod.rs:656-671). */
+typedef struct {
+  const double* density;                   /* kg/m^3 */
+  const double* ionized_hydrogen_fraction; /* dimensionless */
+  const double* temperature;               /* K */
+  const double* source;                    /* photons/s */
+} sw_cell_init;
+
+typedef struct sw_handle sw_handle;
+
+/* Cumulative work and timing counters of a handle. */
+typedef struct {
+  int64_t steps;
+  int64_t level_sweeps;
+  int64_t tasks;          /* solved (cell, direction) tasks */
+  int64_t chem_cells;     /* chemistry cell updates */
+  int64_t chem_attempts;  /* try_timestep_update calls */
+  int64_t chem_failures;  /* cells whose chemistry did not converge (reference: log::error) */
+  int64_t rounds;         /* dependency rounds of the persistent sweep kernel */
+  int64_t visits;         /* cell visits of the sweep kernel (tasks / visits = batch size) */
+  double sweep_ms;        /* device time in transport kernels (incl. counting, folding) */
+  double chem_ms;         /* device time in chemistry kernels */
+  double level_ms;        /* device time in level reassignment */
+  double simulation_time; /* s, SimulationTime accumulated by sw_step */
+  double step_ms;         /* device time of whole sw_step calls (CUDA events on the library's stream) */
+  double transport_kernel_ms;  /* device time of the persistent transport kernel alone */
+  int64_t transport_launches;  /* launches of the persistent transport kernel */
+  int64_t kernel_launches;     /* all kernel launches made by sw_step */
+} sw_stats;
+
+/* Fill the reference's defaults (num_directions 84, levels 1, max_timestep 1 Myr). */
+sw_status sw_default_params(sw_params* p);
+
+/* Directions::from_num (src/sweep/direction/mod.rs:58-75): writes num*3 doubles. */
+sw_status sw_directions_from_num(int32_t num, double* out);
+
+/* init_sweep_system (src/sweep/mod.rs:634-692) + Sweep::new (194-232). */
+sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_cell_init* init,
+                    sw_handle** out);
+
+/* Sweep::run_sweeps (src/sweep/mod.rs:258-272): every level sweep of one step, the
+ * chemistry, TimestepState::advance_allowed_levels and update_timestep_levels.  Writes
+ * the elapsed time (TimestepState::current_max_timestep) and adds it to the handle's
+ * simulation time.  (The reference skips the very first run_sweep_system call so the
+ * initial conditions can be written; that is host-plugin logic.) */
+sw_status sw_step(sw_handle* h, double* time_elapsed_out);
+
+/* Write-back of run_sweep_system (src/sweep/mod.rs:718-738): x_HII, T, the species
+ * timestep and PhotonRate = sum over directions of the incoming rate.  Any pointer
+ * may be NULL.  Arrays have num_cells entries. */
+sw_status sw_get_fields(sw_handle* h, double* ionized_hydrogen_fraction, double* temperature,
+                        double* timestep, double* photon_rate);
+
+/* Further per-cell state: change timescale (Site::change_timescale), timestep level,
+ * and IonizationTime (time at which x_HII first exceeded 0.5, +inf before). */
+sw_status sw_get_cell_state(sw_handle* h, double* change_timescale, uint8_t* level,
+                            double* ionization_time);
+
+/* Overwrite x_HII and T (remap / restart); either pointer may be NULL. */
+sw_status sw_set_fields(sw_handle* h, const double* ionized_hydrogen_fraction,
+                        const double* temperature);
+
+/* Number of cells at each level >= l (Sweep::get_cell_counts_per_level,
+ * src/sweep/mod.rs:240-245); per_level has num_timestep_levels entries. */
+sw_status sw_get_level_counts(sw_handle* h, int64_t* per_level);
+
+/* Dependency counts of Sweep::init_counts (src/sweep/mod.rs:346-386) for `level` with
+ * the current cell levels: counts[cell * D + dir], 0 for inactive cells. */
+sw_status sw_get_dependency_counts(sw_handle* h, int32_t level, uint8_t* counts);
+
+/* Per-(cell, direction) transport state in [cell][dir] layout, converted to FP64
+ * photons/s: Site::incoming_total_rate, outgoing_total_rate, periodic_source
+ * (src/sweep/site.rs:12-23).  Any pointer may be NULL. */
+sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double* periodic);
+
+sw_status sw_get_stats(sw_handle* h, sw_stats* out);
+
+/* Message of the last error on this handle ("" if none); with h == NULL, the last
+ * error of sw_create on this thread. */
+const char* sw_last_error(const sw_handle* h);
+
+void sw_destroy(sw_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,698 @@
+// CPU FP64 oracle: restatement of the subsweep sweep + hydrogen-only chemistry.
+//
+// TEST INFRASTRUCTURE ONLY (see oracle.h).  Every function cites the reference
+// file:line it restates (paths within Tehforsch/subsweep).  Compile with
+// -O2 -fno-fast-math -ffp-contract=off so that every expression rounds exactly as
+// the Rust reference's (which never contracts to FMA) does.  The transcendental
+// functions are glibc's, which is what Rust's std uses on Linux.
+#include "oracle.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Units and constants: src/units/mod.rs:14-108.  Every quantity is a plain SI
+// double; a unit constructor multiplies the literal by the unit's SI factor.
+// ---------------------------------------------------------------------------
+const double kMeters = 1.0;
+const double kCentimeters = 0.01 * kMeters;                       // mod.rs:19
+const double kCentimetersSquared = kCentimeters * kCentimeters;   // mod.rs:91
+const double kCubicMeters = 1.0;                                  // mod.rs:75
+const double kCubicCentimeters = 1e-6 * kCubicMeters;             // mod.rs:76
+const double kSeconds = 1.0 * 1.0;                                // mod.rs:44
+const double kCentimetersCubedPerS = kCubicCentimeters / kSeconds;  // mod.rs:93
+const double kJoules = 1.0 * 1.0;                                 // mod.rs:59
+const double kErgs = 1e-7 * kJoules;                              // mod.rs:60
+const double kErgsCentimetersCubedPerS = kErgs * kCentimetersCubedPerS;  // mod.rs:95
+const double kErgsPerS = kErgs / kSeconds;                        // mod.rs:72
+const double kElectronVolts = 1.602176634e-19 * kJoules;          // mod.rs:61
+const double kKelvins = 1.0;
+const double kKilograms = 1.0;
+const double BOLTZMANN_CONSTANT = 1.380649e-23 * kJoules / kKelvins;  // mod.rs:101
+const double PROTON_MASS = 1.67262192369e-27 * kKilograms;             // mod.rs:102
+const double GAMMA = 5.0 / 3.0;                                        // mod.rs:104
+const double SIGMA = 2.9580524545305314e-18 * kCentimetersSquared;     // mod.rs:105
+const double PHOTON_AVERAGE_ENERGY = 18.028356312818811 * kElectronVolts;  // mod.rs:107
+const double RYDBERG_CONSTANT = 13.65693 * kElectronVolts;                 // mod.rs:108
+
+const int MAX_DEPTH = 100;                        // hydrogen_only/mod.rs:34
+const double IONIZED_FRACTION_EPSILON = 1e-10;    // hydrogen_only/mod.rs:38
+const double HYDROGEN_MASS_FRACTION = 1.0;        // hydrogen_only/mod.rs:32
+
+enum Process { PROC_TEMPERATURE = 0, PROC_IONIZATION = 1, PROC_PHOTON_RATE = 2 };
+
+struct Timescale {
+  double time;
+  int process;
+  // chemistry/timescale.rs:114-120 (strict <, NaN picks `other`)
+  Timescale min(const Timescale& other) const { return time < other.time ? *this : other; }
+};
+
+inline double powi2(double x) { return x * x; }
+inline double powi3(double x) { return x * x * x; }
+inline double powi4(double x) { double x2 = x * x; return x2 * x2; }
+
+// glam DVec3::dot: (x*x') + (y*y') + (z*z')
+inline double dot3(const double* a, const double* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+// ---------------------------------------------------------------------------
+// Solver: src/chemistry/hydrogen_only/mod.rs:125-461
+// ---------------------------------------------------------------------------
+struct Solver {
+  double x, temperature, density, volume, length, rate, scale_factor;
+  bool has_floor;
+  double floor_t, floor_x;
+  bool clamp_panicked = false;
+
+  double hydrogen_number_density() const { return density / PROTON_MASS; }            // 139-141
+  double ionized_number_density() const { return hydrogen_number_density() * x; }     // 143-145
+  double neutral_number_density() const { return hydrogen_number_density() * (1.0 - x); }  // 147-149
+  double electron_number_density() const { return ionized_number_density(); }          // 151-154
+  double mu() const { return 1.0 / (x + 1.0); }                                        // 156-159
+
+  double collision_fit_function() const {  // 161-164
+    double t = temperature;
+    return std::sqrt(t) / (1.0 + std::sqrt(t / 1e5)) * std::exp(-157809.1 / t);
+  }
+  double collision_fit_function_derivative() const {  // 166-173
+    double const1 = 1.0 / 1e5;
+    double const2 = 157809.1;
+    double t = temperature;
+    return (std::exp(-const2 / t) *
+            (const1 * const2 * t + 0.5 * std::sqrt(const1 * t) * (2.0 * const2 + t))) /
+           (std::sqrt(powi3(t)) * std::sqrt(const1 * t) * powi2(std::sqrt(const1 * t) + 1.0));
+  }
+  double case_b_recombination_rate() const {  // 175-180
+    double lambda = 315614.0 * kKelvins / temperature;
+    return (2.753e-14 * std::pow(lambda, 1.5) /
+            std::pow(1.0 + std::pow(lambda / 2.74, 0.407), 2.242)) *
+           kCentimetersCubedPerS;
+  }
+  double case_b_recombination_rate_derivative() const {  // 182-194
+    double lambda = 315614.0 * kKelvins / temperature;
+    double dlambda_dt = -(315614.0 * kKelvins) / (temperature * temperature);
+    double c1 = 1.0 / 2.74;
+    double c2 = 0.407;
+    double c3 = 2.242;
+    double d = -std::sqrt(lambda) * std::pow(std::pow(c1 * lambda, c2) + 1.0, -c3 - 1.0) *
+               (c2 * c3 * std::pow(c1 * lambda, c2) - 1.5 * std::pow(c1 * lambda, c2) - 1.5);
+    return ((2.753e-14 * d) * kCentimetersCubedPerS) * dlambda_dt;
+  }
+  double case_b_recombination_cooling_rate() const {  // 196-202
+    double lambda = 315614.0 * kKelvins / temperature;
+    return (3.435e-30 * temperature * std::pow(lambda, 1.97) /
+            std::pow(1.0 + std::pow(lambda / 2.25, 0.376), 3.72)) *
+           kErgsCentimetersCubedPerS;
+  }
+  double case_b_recombination_cooling_rate_derivative() const {  // 204-216
+    double c1 = 315614.0, c2 = 1.97, c3 = 0.376, c4 = 3.72, c5 = 2.25;
+    double t = temperature;
+    double derivative = std::pow(1.0 + std::pow(c1 / (c5 * t), c3), -1.0 - c4) *
+                        (1.0 - 1.0 * c2 + (1.0 - 1.0 * c2 + c3 * c4) * std::pow(c1 / (c5 * t), c3)) *
+                        std::pow(c1 / t, c2);
+    return ((3.435e-30 * derivative) * kErgsCentimetersCubedPerS) / kKelvins;
+  }
+  double collisional_ionization_rate() const {  // 218-220
+    return (5.85e-11 * collision_fit_function()) * kCentimetersCubedPerS;
+  }
+  double collisional_ionization_rate_derivative() const {  // 222-225
+    return ((5.85e-11 * collision_fit_function_derivative()) * kCentimetersCubedPerS) / kKelvins;
+  }
+  double collisional_ionization_cooling_rate() const {  // 227-229
+    return (1.27e-21 * collision_fit_function()) * kErgsCentimetersCubedPerS;
+  }
+  double collisional_ionization_cooling_rate_derivative() const {  // 231-235
+    return ((1.27e-21 * collision_fit_function_derivative()) * kErgsCentimetersCubedPerS) /
+           kKelvins;
+  }
+  double collisional_excitation_cooling_rate() const {  // 237-242
+    double t = temperature;
+    return (7.5e-19 / (1.0 + std::sqrt(t / 1e5)) * std::exp(-118348.0 / t)) *
+           kErgsCentimetersCubedPerS;
+  }
+  double collisional_excitation_cooling_rate_derivative() const {  // 244-253
+    double t = temperature;
+    double c1 = 7.5e-19, c2 = 118348.0, c3 = 1.0 / 1e5;
+    double v = (c1 * std::exp(-c2 / t) *
+                (c2 * c3 * t - 0.5 * c3 * powi2(t) + c2 * std::sqrt(c3 * t))) /
+               (powi2(t) * std::sqrt(c3 * t) * powi2(1.0 + std::sqrt(c3 * t)));
+    return (v * kErgsCentimetersCubedPerS) / kKelvins;
+  }
+  double bremsstrahlung_cooling_rate() const {  // 255-257
+    return (1.42e-27 * std::sqrt(temperature)) * kErgsCentimetersCubedPerS;
+  }
+  double bremsstrahlung_cooling_rate_derivative() const {  // 259-263
+    return ((1.42e-27 / (2.0 * std::sqrt(temperature))) * kErgsCentimetersCubedPerS) / kKelvins;
+  }
+  double compton_cooling_rate() const {  // 265-268
+    double xx = 2.727 / scale_factor;
+    return (1.017e-37 * powi4(xx) * (temperature - xx)) * kErgsPerS;
+  }
+  double compton_cooling_rate_derivative() const {  // 270-273
+    double xx = 2.727 / scale_factor;
+    return ((1.017e-37 * powi4(xx)) * kErgsPerS) / kKelvins;
+  }
+  double cooling_rate() const {  // 275-287
+    double ne = electron_number_density();
+    double nh_neutral = neutral_number_density();
+    double nh_ionized = ionized_number_density();
+    double collisional =
+        (collisional_excitation_cooling_rate() + collisional_ionization_cooling_rate()) * ne *
+        nh_neutral;
+    double recombination = case_b_recombination_cooling_rate() * ne * nh_ionized;
+    double bremsstrahlung = bremsstrahlung_cooling_rate() * ne * nh_ionized;
+    double compton = compton_cooling_rate() * ne;
+    return collisional + recombination + bremsstrahlung + compton;
+  }
+  double cooling_rate_derivative() const {  // 289-302
+    double ne = electron_number_density();
+    double nh_neutral = neutral_number_density();
+    double nh_ionized = ionized_number_density();
+    double collisional = (collisional_excitation_cooling_rate_derivative() +
+                          collisional_ionization_cooling_rate_derivative()) *
+                         ne * nh_neutral;
+    double recombination = case_b_recombination_cooling_rate_derivative() * ne * nh_ionized;
+    double bremsstrahlung = bremsstrahlung_cooling_rate_derivative() * ne * nh_ionized;
+    double compton = compton_cooling_rate_derivative() * ne;
+    return collisional + recombination + bremsstrahlung + compton;
+  }
+  double num_newly_ionized_hydrogen_atoms(double timestep) const {  // 312-319
+    double nhn = neutral_number_density();
+    double absorbed_fraction = 1.0 - std::exp(-nhn * SIGMA * length);
+    double num_photons = timestep * rate;
+    return num_photons * absorbed_fraction;
+  }
+  double photoheating_rate(double timestep) const {  // 321-325
+    double num = num_newly_ionized_hydrogen_atoms(timestep);
+    double ionization_density = num / volume;
+    return ionization_density * (PHOTON_AVERAGE_ENERGY - RYDBERG_CONSTANT) / timestep;
+  }
+  double photoionization_rate(double timestep) const {  // 327-332
+    double num = num_newly_ionized_hydrogen_atoms(timestep);
+    double fraction = num / (neutral_number_density() * volume);
+    return fraction / timestep;
+  }
+  double temperature_change(double timestep) const {  // 304-310
+    double k = (GAMMA - 1.0) * PROTON_MASS / (density * BOLTZMANN_CONSTANT);
+    double lambda = photoheating_rate(timestep) - cooling_rate();
+    double dlambdadt = -cooling_rate_derivative();
+    double m = mu();
+    return k * m * lambda * timestep / (1.0 - k * m * dlambdadt * timestep);
+  }
+  double ionized_fraction_change(double timestep) const {  // 334-354
+    double nh = hydrogen_number_density();
+    double ne = electron_number_density();
+    double alpha = case_b_recombination_rate();
+    double dalpha = case_b_recombination_rate_derivative();
+    double beta = collisional_ionization_rate();
+    double dbeta = collisional_ionization_rate_derivative();
+    double photo = photoionization_rate(timestep);
+    double c = beta * ne + photo;
+    double m = mu();
+    double d = alpha * ne;
+    double xhii = x;
+    double rhsc = ne * temperature * m * HYDROGEN_MASS_FRACTION * dbeta;
+    double dcdx = nh * beta - rhsc;
+    double rhsd = ne * temperature * m * HYDROGEN_MASS_FRACTION * dalpha;
+    double dddx = nh * alpha - rhsd;
+    double j = dcdx - (c + d) - xhii * (dcdx + dddx);
+    return timestep * (c - xhii * (c + d)) / (1.0 - j * timestep);
+  }
+  void clamp() {  // 356-369, with f64::clamp semantics (asserts min <= max)
+    double xf = has_floor ? floor_x : IONIZED_FRACTION_EPSILON;
+    double xmax = 1.0 - IONIZED_FRACTION_EPSILON;
+    if (!(xf <= xmax)) clamp_panicked = true;  // the reference panics here
+    if (x < xf) x = xf;
+    if (x > xmax) x = xmax;
+    if (has_floor && temperature < floor_t) temperature = floor_t;
+  }
+  // update() 444-461. Returns false on TimestepCriterionViolated.
+  static bool update(double& value, double change, double max_allowed, double timestep,
+                     double& recommendation) {
+    double relative_change = std::fmin(std::fabs(change / value), 1.0 / DBL_EPSILON);
+    if (relative_change > max_allowed) return false;
+    value += change;
+    recommendation = timestep * (max_allowed / relative_change);
+    return true;
+  }
+  bool try_timestep_update(double timestep, double safety, Timescale& out) {  // 371-392
+    double tc = temperature_change(timestep);
+    double rec_t;
+    if (!update(temperature, tc, safety, timestep, rec_t)) return false;
+    Timescale ideal_t{rec_t, PROC_TEMPERATURE};
+    double xc = ionized_fraction_change(timestep);
+    double rec_x;
+    if (!update(x, xc, safety, timestep, rec_x)) return false;
+    Timescale ideal_x{rec_x, PROC_IONIZATION};
+    clamp();
+    out = ideal_t.min(ideal_x);
+    return true;
+  }
+  // perform_timestep_internal 394-424; false = TimestepConvergenceFailed.
+  bool perform_internal(double timestep, double safety, int depth, Timescale& out,
+                        int64_t& attempts) {
+    clamp();
+    double init_t = temperature, init_x = x;
+    if (depth > MAX_DEPTH) return false;
+    ++attempts;
+    if (!try_timestep_update(timestep, safety, out)) {
+      temperature = init_t;
+      x = init_x;
+      if (!perform_internal(timestep / 2.0, safety, depth + 1, out, attempts)) return false;
+      return perform_internal(timestep / 2.0, safety, depth + 1, out, attempts);
+    }
+    return true;
+  }
+  // perform_timestep 426-441
+  Timescale perform_timestep(double timestep, double safety, bool* failed, int64_t& attempts) {
+    Timescale out{0.0, PROC_TEMPERATURE};
+    if (!perform_internal(timestep, safety, 0, out, attempts)) {
+      *failed = true;
+      return Timescale{timestep / 10.0, PROC_TEMPERATURE};
+    }
+    *failed = false;
+    return out;
+  }
+};
+
+// TimestepLevel::from_max_timestep_and_desired_timestep, timestep_level.rs:27-36,
+// with Rust's saturating float->usize cast.
+int32_t timestep_level(int32_t max_num_levels, double max_timestep, double desired) {
+  double ratio = max_timestep / desired;
+  double v = std::ceil(std::log2(ratio));
+  int64_t level;
+  if (std::isnan(v) || v <= 0.0)
+    level = 0;
+  else if (v >= 9.2e18)
+    level = INT64_MAX;
+  else
+    level = (int64_t)v;
+  if (level > max_num_levels - 1) level = max_num_levels - 1;
+  return (int32_t)level;
+}
+
+// TimestepState, timestep_state.rs:5-90
+struct TimestepState {
+  double max_timestep;
+  int32_t max_num_levels;
+  int32_t lowest;
+  bool first_done = false;
+  TimestepState(double m, int32_t n) : max_timestep(m), max_num_levels(n), lowest(n - 1) {}
+  std::vector<int32_t> sweep_order() const {  // 22-27, 70-75
+    int32_t num = max_num_levels - lowest;
+    std::vector<int32_t> out;
+    for (uint32_t i = 0; i < (1u << (num - 1)); ++i) {
+      uint32_t first_bit = (uint32_t)(num - 1);
+      for (uint32_t b = 0; b < 32; ++b)
+        if (i & (1u << b)) { first_bit = b; break; }
+      out.push_back(lowest + (int32_t)(num - 1 - first_bit));
+    }
+    return out;
+  }
+  void advance() {  // 37-48
+    if (first_done && lowest > 0) lowest -= 1;
+    if (!first_done) first_done = true;
+  }
+  double timestep_at_level(int32_t level) const {  // timestep_level.rs:42-48
+    return max_timestep * std::pow(0.5, level);
+  }
+  double current_max_timestep() const { return max_timestep * std::pow(0.5, lowest); }  // 77-79
+  int32_t desired_level(double desired) const {  // 54-64
+    int32_t level = timestep_level(max_num_levels, max_timestep, desired);
+    if (level < lowest) level = lowest;
+    return level;
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Sweep<HydrogenOnly>: src/sweep/mod.rs:171-610
+// ---------------------------------------------------------------------------
+struct orc_sim {
+  orc_params p;
+  std::vector<double> dirs;
+  int64_t n;
+  int32_t D;
+  std::vector<int64_t> row_ptr;
+  std::vector<int32_t> nbr;
+  std::vector<uint8_t> kind;
+  std::vector<double> area, normal, volume, size;
+  // Site (site.rs:12-23) in SoA form, per-(cell,dir) arrays [cell*D + dir]
+  std::vector<double> density, source, xhii, temperature, species_timestep, change_timescale,
+      previous_rate;
+  std::vector<double> incoming, outgoing, periodic, periodic_pending;
+  std::vector<uint32_t> missing;
+  std::vector<uint8_t> level;
+  TimestepState ts;
+  int64_t tasks_solved = 0, chem_cells = 0, chem_attempts = 0, chem_failures = 0;
+  bool panicked = false;
+
+  explicit orc_sim(const orc_params* pp) : p(*pp), ts(pp->max_timestep, pp->num_timestep_levels) {}
+
+  double get_rate(int64_t c, int32_t d) const {  // site.rs:53-56
+    double src = source[c] / (double)D;
+    return incoming[c * D + d] + src + periodic[c * D + d];
+  }
+  bool active(int64_t c, int32_t current) const { return level[c] >= current; }
+
+  // Sweep::init_counts, mod.rs:346-386
+  int64_t init_counts(int32_t current, std::vector<uint32_t>& out) const {
+    int64_t n_active = 0;
+    for (int64_t c = 0; c < n; ++c) {
+      if (!active(c, current)) continue;
+      ++n_active;
+      for (int32_t d = 0; d < D; ++d) {
+        uint32_t cnt = 0;
+        for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
+          bool upwind = dot3(&normal[3 * f], &dirs[3 * d]) < 0.0;
+          if (!upwind || kind[f] == ORC_BOUNDARY) continue;
+          if (!active(nbr[f], current)) continue;
+          if (kind[f] == ORC_LOCAL) cnt += 1;
+        }
+        out[c * D + d] = cnt;
+      }
+    }
+    return n_active;
+  }
+
+  // HydrogenOnly::get_outgoing_rate, hydrogen_only/mod.rs:72-88
+  double outgoing_rate(int64_t c, double incoming_rate) const {
+    double nhn = density[c] / PROTON_MASS * (1.0 - xhii[c]);
+    if (incoming_rate < p.significant_rate_threshold) return 0.0;
+    double non_absorbed = std::exp(-nhn * SIGMA * size[c]);
+    return incoming_rate * non_absorbed;
+  }
+
+  // Sweep::solve_task, mod.rs:423-485 (+ get_outgoing_rate 412-421, handle_local_neighbour
+  // 487-503, handle_local_periodic_neighbour 505-513).
+  void solve_task(int64_t c, int32_t d, int32_t current, std::deque<int64_t>& queue) {
+    double& inc = incoming[c * D + d];
+    if (inc < 0.0) inc = 0.0;  // Photons::make_positive, chemistry/mod.rs:61-65
+    double out_new = outgoing_rate(c, get_rate(c, d));
+    double corr = out_new - outgoing[c * D + d];
+    outgoing[c * D + d] = out_new;
+    const double* dir = &dirs[3 * d];
+    double total_effective_area = 0.0;
+    for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
+      double dt = dot3(&normal[3 * f], dir);
+      if (dt > 0.0) total_effective_area += area[f] * dt;
+    }
+    for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
+      double dt = dot3(&normal[3 * f], dir);
+      if (!(dt > 0.0)) continue;
+      double effective_area = area[f] * dt;
+      double w = corr * (effective_area / total_effective_area);
+      int64_t nb = nbr[f];
+      if (kind[f] == ORC_LOCAL) {
+        incoming[nb * D + d] += w;
+        if (active(nb, current)) {
+          uint32_t& m = missing[nb * D + d];
+          m -= 1;
+          if (m == 0) queue.push_back(nb);
+        }
+      } else if (kind[f] == ORC_LOCAL_PERIODIC) {
+        if (p.periodic_mode == ORC_PERIODIC_IMMEDIATE)
+          periodic[nb * D + d] += w;
+        else
+          periodic_pending[nb * D + d] += w;
+      }
+    }
+    ++tasks_solved;
+  }
+
+  // Sweep::update_chemistry, mod.rs:549-574 (+ HydrogenOnly::update_abundances 90-119)
+  void update_chemistry(int32_t current) {
+    for (int64_t c = 0; c < n; ++c) {
+      if (!active(c, current)) continue;
+      double timestep = ts.timestep_at_level(level[c]);
+      double rate = 0.0;
+      for (int32_t d = 0; d < D; ++d) rate += get_rate(c, d);
+      double relative_change;
+      if (std::fabs(rate) < std::fabs(p.significant_rate_threshold)) {  // chemistry/mod.rs:79-81
+        relative_change = 0.0;
+      } else {  // chemistry/mod.rs:73-77
+        relative_change = std::fabs(
+            std::fmin(std::fabs(std::fabs(rate - previous_rate[c]) / rate), 1.0 / DBL_EPSILON));
+      }
+      previous_rate[c] = rate;
+      Timescale rate_ts{timestep / relative_change, PROC_PHOTON_RATE};
+      Solver s;
+      s.x = xhii[c];
+      s.temperature = temperature[c];
+      s.density = density[c];
+      s.volume = volume[c];
+      s.length = size[c];
+      s.rate = rate;
+      s.scale_factor = p.scale_factor;
+      s.has_floor = p.prevent_cooling != 0;
+      s.floor_t = temperature[c];
+      s.floor_x = xhii[c];
+      bool failed = false;
+      Timescale chem_ts = s.perform_timestep(timestep, p.chemistry_timestep_safety_factor, &failed,
+                                             chem_attempts);
+      if (failed) ++chem_failures;
+      if (s.clamp_panicked) panicked = true;
+      temperature[c] = s.temperature;
+      xhii[c] = s.x;
+      species_timestep[c] = chem_ts.time;
+      Timescale change = rate_ts.min(chem_ts);
+      change_timescale[c] = change.time;
+      ++chem_cells;
+    }
+  }
+
+  // Sweep::single_sweep, mod.rs:274-289.  The BinaryHeap keyed by direction only
+  // (task.rs:25-35) pops every task of the highest direction before any lower one,
+  // since new tasks inherit the popped task's direction; within a direction the heap
+  // order is unspecified, and this restatement uses FIFO order.
+  bool single_sweep(int32_t current) {
+    int64_t n_active = init_counts(current, missing);
+    int64_t solved_before = tasks_solved;
+    for (int32_t d = D - 1; d >= 0; --d) {
+      std::deque<int64_t> queue;
+      for (int64_t c = 0; c < n; ++c)  // get_initial_tasks, mod.rs:388-398
+        if (active(c, current) && missing[c * D + d] == 0) queue.push_back(c);
+      while (!queue.empty()) {
+        int64_t c = queue.front();
+        queue.pop_front();
+        solve_task(c, d, current, queue);
+      }
+    }
+    bool complete = (tasks_solved - solved_before) == n_active * (int64_t)D;
+    if (p.periodic_mode == ORC_PERIODIC_SNAPSHOT) {
+      for (size_t i = 0; i < periodic.size(); ++i) {
+        periodic[i] += periodic_pending[i];
+        periodic_pending[i] = 0.0;
+      }
+    }
+    update_chemistry(current);
+    return complete;
+  }
+
+  // Sweep::update_timestep_levels, mod.rs:576-589
+  void update_timestep_levels() {
+    for (int64_t c = 0; c < n; ++c) {
+      double desired = p.timestep_safety_factor * change_timescale[c];
+      level[c] = (uint8_t)ts.desired_level(desired);
+    }
+  }
+
+  void level_counts(int64_t* counts) const {
+    for (int32_t l = 0; l < p.num_timestep_levels; ++l) counts[l] = 0;
+    for (int64_t c = 0; c < n; ++c)
+      for (int32_t l = 0; l <= level[c]; ++l) counts[l] += 1;
+  }
+
+  // Sweep::run_sweeps, mod.rs:258-272
+  int run_sweeps(double* time_elapsed) {
+    std::vector<int64_t> counts(p.num_timestep_levels);
+    level_counts(counts.data());
+    int status = 0;
+    for (int32_t l : ts.sweep_order())
+      if (counts[l] > 0)
+        if (!single_sweep(l)) status = 1;
+    *time_elapsed = ts.current_max_timestep();
+    ts.advance();
+    update_timestep_levels();
+    return status;
+  }
+};
+
+extern "C" {
+
+orc_sim* orc_sim_create(const orc_params* p, const orc_grid* g, const double* density,
+                        const double* xhii, const double* temperature, const double* source) {
+  orc_sim* s = new orc_sim(p);
+  s->D = p->num_directions;
+  s->dirs.assign(p->directions, p->directions + 3 * p->num_directions);
+  s->p.directions = s->dirs.data();
+  s->n = g->num_cells;
+  int64_t E = g->row_ptr[g->num_cells];
+  s->row_ptr.assign(g->row_ptr, g->row_ptr + s->n + 1);
+  s->nbr.assign(g->nbr, g->nbr + E);
+  s->kind.assign(g->kind, g->kind + E);
+  s->area.assign(g->area, g->area + E);
+  s->normal.assign(g->normal, g->normal + 3 * E);
+  s->volume.assign(g->volume, g->volume + s->n);
+  s->size.assign(g->size, g->size + s->n);
+  s->density.assign(density, density + s->n);
+  s->xhii.assign(xhii, xhii + s->n);
+  s->temperature.assign(temperature, temperature + s->n);
+  s->source.assign(source, source + s->n);
+  s->species_timestep.assign(s->n, 0.0);   // HydrogenOnlySpecies::new, hydrogen_only/mod.rs:56-65
+  s->change_timescale.assign(s->n, 0.0);   // Site::new, site.rs:26-43
+  s->previous_rate.assign(s->n, 0.0);
+  size_t nd = (size_t)s->n * (size_t)s->D;
+  s->incoming.assign(nd, 0.0);
+  s->outgoing.assign(nd, 0.0);
+  s->periodic.assign(nd, 0.0);
+  s->periodic_pending.assign(nd, 0.0);
+  s->missing.assign(nd, 0);
+  // Sweep::new: every cell starts at the highest level (mod.rs:206)
+  s->level.assign(s->n, (uint8_t)(p->num_timestep_levels - 1));
+  return s;
+}
+
+void orc_sim_destroy(orc_sim* s) { delete s; }
+
+int orc_sim_step(orc_sim* s, double* time_elapsed) {
+  double te = 0.0;
+  int st = s->run_sweeps(&te);
+  if (time_elapsed) *time_elapsed = te;
+  if (s->panicked) st = 2;
+  return st;
+}
+
+void orc_sim_get_fields(const orc_sim* s, double* xhii, double* temperature, double* timestep,
+                        double* rate, double* change_timescale, uint8_t* level) {
+  for (int64_t c = 0; c < s->n; ++c) {
+    if (xhii) xhii[c] = s->xhii[c];
+    if (temperature) temperature[c] = s->temperature[c];
+    if (timestep) timestep[c] = s->species_timestep[c];
+    if (rate) {  // mod.rs:727-730: sum of incoming over directions
+      double r = 0.0;
+      for (int32_t d = 0; d < s->D; ++d) r += s->incoming[c * s->D + d];
+      rate[c] = r;
+    }
+    if (change_timescale) change_timescale[c] = s->change_timescale[c];
+    if (level) level[c] = s->level[c];
+  }
+}
+
+void orc_sim_get_rates(const orc_sim* s, double* incoming, double* outgoing, double* periodic) {
+  size_t nd = s->incoming.size();
+  if (incoming) std::memcpy(incoming, s->incoming.data(), nd * sizeof(double));
+  if (outgoing) std::memcpy(outgoing, s->outgoing.data(), nd * sizeof(double));
+  if (periodic) std::memcpy(periodic, s->periodic.data(), nd * sizeof(double));
+}
+
+int64_t orc_sim_init_counts(const orc_sim* s, int32_t level, uint8_t* out) {
+  std::vector<uint32_t> tmp((size_t)s->n * s->D, 0);
+  int64_t na = s->init_counts(level, tmp);
+  for (size_t i = 0; i < tmp.size(); ++i) out[i] = (uint8_t)(tmp[i] > 255 ? 255 : tmp[i]);
+  return na;
+}
+
+void orc_sim_level_counts(const orc_sim* s, int64_t* counts) { s->level_counts(counts); }
+
+void orc_sim_work(const orc_sim* s, int64_t* tasks, int64_t* chem_cells) {
+  if (tasks) *tasks = s->tasks_solved;
+  if (chem_cells) *chem_cells = s->chem_cells;
+}
+
+int32_t orc_sim_sweep_order(const orc_sim* s, int32_t* levels_out, int32_t cap) {
+  std::vector<int32_t> o = s->ts.sweep_order();
+  for (int32_t i = 0; i < (int32_t)o.size() && i < cap; ++i) levels_out[i] = o[i];
+  return (int32_t)o.size();
+}
+
+int64_t orc_sim_single_sweep(orc_sim* s, int32_t level) {
+  int64_t before = s->tasks_solved;
+  s->single_sweep(level);
+  return s->tasks_solved - before;
+}
+
+int32_t orc_timestep_level(int32_t max_num_levels, double max_timestep, double desired) {
+  return timestep_level(max_num_levels, max_timestep, desired);
+}
+
+int32_t orc_sweep_order_after(int32_t num_levels, int32_t advances, int32_t* out, int32_t cap) {
+  TimestepState st(1.0, num_levels);
+  for (int32_t i = 0; i < advances; ++i) st.advance();
+  std::vector<int32_t> o = st.sweep_order();
+  for (int32_t i = 0; i < (int32_t)o.size() && i < cap; ++i) out[i] = o[i];
+  return (int32_t)o.size();
+}
+
+int32_t orc_lowest_allowed_after(int32_t num_levels, int32_t advances) {
+  TimestepState st(1.0, num_levels);
+  for (int32_t i = 0; i < advances; ++i) st.advance();
+  return st.lowest;
+}
+
+double orc_rate_fit(int32_t which, double temperature, double scale_factor) {
+  Solver s{};
+  s.temperature = temperature;
+  s.scale_factor = scale_factor;
+  switch (which) {
+    case 0: return s.case_b_recombination_rate();
+    case 1: return s.case_b_recombination_rate_derivative();
+    case 2: return s.collisional_ionization_rate();
+    case 3: return s.collisional_ionization_rate_derivative();
+    case 4: return s.collisional_ionization_cooling_rate();
+    case 5: return s.collisional_ionization_cooling_rate_derivative();
+    case 6: return s.collisional_excitation_cooling_rate();
+    case 7: return s.collisional_excitation_cooling_rate_derivative();
+    case 8: return s.case_b_recombination_cooling_rate();
+    case 9: return s.case_b_recombination_cooling_rate_derivative();
+    case 10: return s.bremsstrahlung_cooling_rate();
+    case 11: return s.bremsstrahlung_cooling_rate_derivative();
+    case 12: return s.compton_cooling_rate();
+    case 13: return s.compton_cooling_rate_derivative();
+    default: return NAN;
+  }
+}
+
+int32_t orc_solver_perform_timestep(double* xhii, double* temperature, double density,
+                                    double volume, double length, double rate,
+                                    double scale_factor, int32_t has_floor, double floor_t,
+                                    double floor_x, double timestep, double safety,
+                                    double* timescale_out, int32_t* process_out) {
+  Solver s{};
+  s.x = *xhii;
+  s.temperature = *temperature;
+  s.density = density;
+  s.volume = volume;
+  s.length = length;
+  s.rate = rate;
+  s.scale_factor = scale_factor;
+  s.has_floor = has_floor != 0;
+  s.floor_t = floor_t;
+  s.floor_x = floor_x;
+  bool failed = false;
+  int64_t attempts = 0;
+  Timescale t = s.perform_timestep(timestep, safety, &failed, attempts);
+  *xhii = s.x;
+  *temperature = s.temperature;
+  if (timescale_out) *timescale_out = t.time;
+  if (process_out) *process_out = t.process;
+  return failed ? 1 : 0;
+}
+
+double orc_outgoing_rate(double density, double xhii, double size, double incoming_rate,
+                         double threshold) {
+  double nhn = density / PROTON_MASS * (1.0 - xhii);
+  if (incoming_rate < threshold) return 0.0;
+  return incoming_rate * std::exp(-nhn * SIGMA * size);
+}
+
+}  // extern "C"

@@ -1,0 +1,285 @@
+// Hydrogen-only chemistry on the device: the semi-implicit x_HII / temperature
+// update of Rosdahl et al. (2015) with recursive timestep halving, as in
+// src/chemistry/hydrogen_only/mod.rs:125-461 of the reference.
+//
+// The reference recurses (perform_timestep_internal, 394-424): a failed attempt
+// over dt is replaced by two attempts over dt/2, depth <= 100.  Here the recursion
+// is an explicit loop.  At any time at most one second half is pending per depth,
+// and pending halves are taken deepest first, so the pending set is a bitmask
+// over depths and the next interval is its highest set bit.  The result (state and
+// the timescale of the last accepted substep) is the same as the recursion's.
+//
+// kCarryNeutral = false restates the reference exactly: the neutral fraction is
+// recomputed as (1 - x) wherever it is used.  kCarryNeutral = true (mixed path)
+// additionally carries y = 1 - x as its own FP64 state, updated by -dx, so the
+// neutral density keeps full relative precision near complete ionisation; the
+// smaller of x and y is the accurate one and the other is re-derived from it.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+namespace swk {
+
+// src/units/mod.rs:14-108, every quantity a plain SI double.
+struct Units {
+  static constexpr double kCentimeters = 0.01;
+  static constexpr double kCentimetersSquared = kCentimeters * kCentimeters;
+  static constexpr double kCubicCentimeters = 1e-6;
+  static constexpr double kSeconds = 1.0;
+  static constexpr double kCentimetersCubedPerS = kCubicCentimeters / kSeconds;
+  static constexpr double kErgs = 1e-7;
+  static constexpr double kErgsCentimetersCubedPerS = kErgs * kCentimetersCubedPerS;
+  static constexpr double kErgsPerS = kErgs / kSeconds;
+  static constexpr double kElectronVolts = 1.602176634e-19;
+  static constexpr double kBoltzmann = 1.380649e-23;
+  static constexpr double kProtonMass = 1.67262192369e-27;
+  static constexpr double kGamma = 5.0 / 3.0;
+  static constexpr double kSigma = 2.9580524545305314e-18 * kCentimetersSquared;
+  static constexpr double kPhotonAverageEnergy = 18.028356312818811 * kElectronVolts;
+  static constexpr double kRydberg = 13.65693 * kElectronVolts;
+};
+
+constexpr int kChemMaxDepth = 100;               // hydrogen_only/mod.rs:34
+constexpr double kIonizedFractionEpsilon = 1e-10;  // hydrogen_only/mod.rs:38
+
+enum ChemProcess : int { kProcTemperature = 0, kProcIonization = 1, kProcPhotonRate = 2 };
+
+struct Timescale {
+  double time;
+  int process;
+};
+
+// chemistry/timescale.rs:114-120: strict <, so NaN selects `b`.
+__device__ __forceinline__ Timescale ts_min(Timescale a, Timescale b) {
+  return a.time < b.time ? a : b;
+}
+
+template <bool kCarryNeutral>
+struct ChemSolver {
+  double x;   // ionized hydrogen fraction
+  double y;   // neutral fraction (only meaningful when kCarryNeutral)
+  double temperature;
+  double density, volume, length, rate, scale_factor;
+  bool has_floor;
+  double floor_t, floor_x;
+  bool clamp_invalid;
+
+  __device__ __forceinline__ double neutral() const { return kCarryNeutral ? y : (1.0 - x); }
+  __device__ __forceinline__ double nh() const { return density / Units::kProtonMass; }
+  __device__ __forceinline__ double n_ionized() const { return nh() * x; }
+  __device__ __forceinline__ double n_neutral() const { return nh() * neutral(); }
+  __device__ __forceinline__ double mu() const { return 1.0 / (x + 1.0); }
+
+  // 161-173
+  __device__ double collision_fit() const {
+    double t = temperature;
+    return sqrt(t) / (1.0 + sqrt(t / 1e5)) * exp(-157809.1 / t);
+  }
+  __device__ double collision_fit_derivative() const {
+    double c1 = 1.0 / 1e5, c2 = 157809.1, t = temperature;
+    double s = sqrt(c1 * t);
+    return (exp(-c2 / t) * (c1 * c2 * t + 0.5 * s * (2.0 * c2 + t))) /
+           (sqrt(t * t * t) * s * ((s + 1.0) * (s + 1.0)));
+  }
+  // 175-194
+  __device__ double case_b_rate() const {
+    double lambda = 315614.0 / temperature;
+    return (2.753e-14 * pow(lambda, 1.5) / pow(1.0 + pow(lambda / 2.74, 0.407), 2.242)) *
+           Units::kCentimetersCubedPerS;
+  }
+  __device__ double case_b_rate_derivative() const {
+    double lambda = 315614.0 / temperature;
+    double dlambda_dt = -315614.0 / (temperature * temperature);
+    double c1 = 1.0 / 2.74, c2 = 0.407, c3 = 2.242;
+    double p = pow(c1 * lambda, c2);
+    double d = -sqrt(lambda) * pow(p + 1.0, -c3 - 1.0) * (c2 * c3 * p - 1.5 * p - 1.5);
+    return ((2.753e-14 * d) * Units::kCentimetersCubedPerS) * dlambda_dt;
+  }
+  // 196-216
+  __device__ double case_b_cooling() const {
+    double lambda = 315614.0 / temperature;
+    return (3.435e-30 * temperature * pow(lambda, 1.97) /
+            pow(1.0 + pow(lambda / 2.25, 0.376), 3.72)) *
+           Units::kErgsCentimetersCubedPerS;
+  }
+  __device__ double case_b_cooling_derivative() const {
+    const double c1 = 315614.0, c2 = 1.97, c3 = 0.376, c4 = 3.72, c5 = 2.25;
+    double t = temperature;
+    double q = pow(c1 / (c5 * t), c3);
+    double derivative = pow(1.0 + q, -1.0 - c4) * (1.0 - 1.0 * c2 + (1.0 - 1.0 * c2 + c3 * c4) * q) *
+                        pow(c1 / t, c2);
+    return (3.435e-30 * derivative) * Units::kErgsCentimetersCubedPerS;
+  }
+  // 237-253
+  __device__ double excitation_cooling() const {
+    double t = temperature;
+    return (7.5e-19 / (1.0 + sqrt(t / 1e5)) * exp(-118348.0 / t)) *
+           Units::kErgsCentimetersCubedPerS;
+  }
+  __device__ double excitation_cooling_derivative() const {
+    double t = temperature;
+    const double c1 = 7.5e-19, c2 = 118348.0, c3 = 1.0 / 1e5;
+    double s = sqrt(c3 * t);
+    double v = (c1 * exp(-c2 / t) * (c2 * c3 * t - 0.5 * c3 * (t * t) + c2 * s)) /
+               ((t * t) * s * ((1.0 + s) * (1.0 + s)));
+    return v * Units::kErgsCentimetersCubedPerS;
+  }
+  // 265-273
+  __device__ double compton_cooling() const {
+    double xx = 2.727 / scale_factor;
+    double x2 = xx * xx;
+    return (1.017e-37 * (x2 * x2) * (temperature - xx)) * Units::kErgsPerS;
+  }
+  __device__ double compton_cooling_derivative() const {
+    double xx = 2.727 / scale_factor;
+    double x2 = xx * xx;
+    return (1.017e-37 * (x2 * x2)) * Units::kErgsPerS;
+  }
+
+  // cooling_rate 275-287 and cooling_rate_derivative 289-302, evaluated together
+  // (the collision fit is shared by the ionization-cooling term of both).
+  __device__ void cooling(double& lambda_c, double& dlambda_c) const {
+    double ne = n_ionized();
+    double nhn = n_neutral();
+    double nhi = n_ionized();
+    double fit = collision_fit();
+    double fitd = collision_fit_derivative();
+    double sq = sqrt(temperature);
+    double coll = (excitation_cooling() + (1.27e-21 * fit) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
+    double recomb = case_b_cooling() * ne * nhi;
+    double brems = ((1.42e-27 * sq) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
+    double compton = compton_cooling() * ne;
+    lambda_c = coll + recomb + brems + compton;
+    double dcoll = (excitation_cooling_derivative() +
+                    (1.27e-21 * fitd) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
+    double drecomb = case_b_cooling_derivative() * ne * nhi;
+    double dbrems = ((1.42e-27 / (2.0 * sq)) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
+    double dcompton = compton_cooling_derivative() * ne;
+    dlambda_c = dcoll + drecomb + dbrems + dcompton;
+  }
+
+  // 312-319
+  __device__ double newly_ionized(double timestep) const {
+    double absorbed = 1.0 - exp(-n_neutral() * Units::kSigma * length);
+    double num_photons = timestep * rate;
+    return num_photons * absorbed;
+  }
+  // 304-310 (+ photoheating_rate 321-325)
+  __device__ double temperature_change(double timestep) const {
+    double k = (Units::kGamma - 1.0) * Units::kProtonMass / (density * Units::kBoltzmann);
+    double heating = (newly_ionized(timestep) / volume) *
+                     (Units::kPhotonAverageEnergy - Units::kRydberg) / timestep;
+    double lc, dlc;
+    cooling(lc, dlc);
+    double lambda = heating - lc;
+    double dlambdadt = -dlc;
+    double m = mu();
+    return k * m * lambda * timestep / (1.0 - k * m * dlambdadt * timestep);
+  }
+  // 334-354 (+ photoionization_rate 327-332)
+  __device__ double ionized_fraction_change(double timestep) const {
+    double n_h = nh();
+    double ne = n_ionized();
+    double alpha = case_b_rate();
+    double dalpha = case_b_rate_derivative();
+    double fit = collision_fit();
+    double beta = (5.85e-11 * fit) * Units::kCentimetersCubedPerS;
+    double dbeta = (5.85e-11 * collision_fit_derivative()) * Units::kCentimetersCubedPerS;
+    double photo = (newly_ionized(timestep) / (n_neutral() * volume)) / timestep;
+    double c = beta * ne + photo;
+    double m = mu();
+    double d = alpha * ne;
+    double xhii = x;
+    double rhsc = ne * temperature * m * 1.0 * dbeta;
+    double dcdx = n_h * beta - rhsc;
+    double rhsd = ne * temperature * m * 1.0 * dalpha;
+    double dddx = n_h * alpha - rhsd;
+    double j = dcdx - (c + d) - xhii * (dcdx + dddx);
+    return timestep * (c - xhii * (c + d)) / (1.0 - j * timestep);
+  }
+
+  // 356-369 with Rust f64::clamp semantics (asserts min <= max: flagged here).
+  __device__ void clamp() {
+    double xf = has_floor ? floor_x : kIonizedFractionEpsilon;
+    const double xmax = 1.0 - kIonizedFractionEpsilon;
+    if (!(xf <= xmax)) clamp_invalid = true;
+    if (kCarryNeutral) {
+      if (x < xf) { x = xf; y = 1.0 - x; }
+      if (x > xmax) { x = xmax; y = kIonizedFractionEpsilon; }
+    } else {
+      if (x < xf) x = xf;
+      if (x > xmax) x = xmax;
+    }
+    if (has_floor && temperature < floor_t) temperature = floor_t;
+  }
+
+  // update() 444-461
+  __device__ __forceinline__ static bool accept(double value, double change, double max_allowed,
+                                                double timestep, double& recommendation) {
+    double relative_change = fmin(fabs(change / value), 1.0 / DBL_EPSILON);
+    if (relative_change > max_allowed) return false;
+    recommendation = timestep * (max_allowed / relative_change);
+    return true;
+  }
+
+  // try_timestep_update 371-392
+  __device__ bool try_update(double timestep, double safety, Timescale& out) {
+    double tc = temperature_change(timestep);
+    double rec_t;
+    if (!accept(temperature, tc, safety, timestep, rec_t)) return false;
+    temperature += tc;
+    double xc = ionized_fraction_change(timestep);
+    double rec_x;
+    if (!accept(x, xc, safety, timestep, rec_x)) return false;
+    x += xc;
+    if (kCarryNeutral) {
+      y -= xc;
+      // keep the smaller fraction exact and derive the other from it
+      if (x < 0.5) y = 1.0 - x; else x = 1.0 - y;
+    }
+    clamp();
+    out = ts_min(Timescale{rec_t, kProcTemperature}, Timescale{rec_x, kProcIonization});
+    return true;
+  }
+
+  // perform_timestep 426-441 with perform_timestep_internal 394-424 unrolled.
+  __device__ Timescale perform_timestep(double timestep, double safety, bool& failed,
+                                        uint32_t& attempts) {
+    uint64_t pend_lo = 0, pend_hi = 0;  // pending second halves at depths 1..127
+    int depth = 0;
+    Timescale last{0.0, kProcTemperature};
+    while (true) {
+      clamp();
+      double t0 = temperature, x0 = x, y0 = y;
+      if (depth > kChemMaxDepth) {
+        failed = true;
+        return Timescale{timestep / 10.0, kProcTemperature};
+      }
+      double sub = ldexp(timestep, -depth);  // == timestep / 2^depth, exact
+      ++attempts;
+      Timescale r;
+      if (!try_update(sub, safety, r)) {
+        temperature = t0;
+        x = x0;
+        y = y0;
+        ++depth;
+        if (depth < 64) pend_lo |= (1ull << depth); else pend_hi |= (1ull << (depth - 64));
+        continue;
+      }
+      last = r;
+      if (pend_hi) {
+        depth = 127 - __clzll((long long)pend_hi);
+        pend_hi &= ~(1ull << (depth - 64));
+      } else if (pend_lo) {
+        depth = 63 - __clzll((long long)pend_lo);
+        pend_lo &= ~(1ull << depth);
+      } else {
+        failed = false;
+        return last;
+      }
+    }
+  }
+};
+
+}  // namespace swk

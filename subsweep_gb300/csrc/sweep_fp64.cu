@@ -1,0 +1,50 @@
+// FP64 drop-in kernels.  Compiled with -fmad=false: the reference (Rust) never fuses
+// multiply-adds, so without contraction every expression rounds as it does there.
+#define SWK_R double
+#define SWK_CARRY false
+#define SWK_OPS kOpsFP64
+#define SWK_NAME "fp64"
+#include "sweep_ops.cuh"
+
+namespace swh {
+
+static int grid_for_cells(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  if (g < 1) g = 1;
+  if (g > 152 * 16) g = 152 * 16;
+  return (int)g;
+}
+
+cudaError_t launch_update_levels(const DevicePtrs& p, int lowest_allowed, cudaStream_t s) {
+  swk::k_update_levels<<<grid_for_cells(p.num_cells), 256, 0, s>>>(
+      (uint32_t)p.num_cells, p.change_timescale, p.level, p.timestep_safety, p.max_timestep,
+      p.num_levels, lowest_allowed, p.ctl);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  swk::k_level_offsets<<<1, 32, 0, s>>>(p.ctl, p.num_levels);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  swk::k_level_scatter<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.level, p.ctl, p.order);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_level_hist(const DevicePtrs& p, cudaStream_t s) {
+  swk::k_level_hist<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.level, p.num_levels, p.ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_level_order(const DevicePtrs& p, cudaStream_t s) {
+  swk::k_level_offsets<<<1, 32, 0, s>>>(p.ctl, p.num_levels);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  swk::k_level_scatter<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.level, p.ctl, p.order);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ionization_time(const DevicePtrs& p, double time, cudaStream_t s) {
+  swk::k_ionization_time<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.xhii,
+                                                                     p.ionization_time, time);
+  return cudaGetLastError();
+}
+
+}  // namespace swh

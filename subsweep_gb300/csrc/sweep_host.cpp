@@ -1,0 +1,762 @@
+// Host runtime of the GB300 sweep library and its C ABI (include/subsweep_gpu.h).
+//
+// Mirrors the reference's Sweep<HydrogenOnly> driver (src/sweep/mod.rs:171-610): the
+// sweep parameters, the hierarchical timestep state and the per-step sequence of
+// level sweeps live here on the host; every per-cell and per-(cell, direction)
+// computation runs in the kernels of sweep_fp64.cu / sweep_mixed.cu.  There is no
+// CPU fallback: every entry point fails with SW_ERR_CUDA when no device is usable.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/subsweep_gpu.h"
+#include "launch.h"
+#include "sweep_types.h"
+
+#include "direction_bins.inc"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// TimestepState, src/sweep/timestep_state.rs:5-90.
+struct TimestepState {
+  double max_timestep = 0.0;
+  int max_num_levels = 1;
+  int lowest = 0;
+  bool first_done = false;
+
+  void init(double m, int n) {
+    max_timestep = m;
+    max_num_levels = n;
+    lowest = n - 1;
+    first_done = false;
+  }
+  // iter_levels_in_sweep_order (22-27) with lowest_active_from_iteration (70-75)
+  std::vector<int> sweep_order() const {
+    int num = max_num_levels - lowest;
+    std::vector<int> out;
+    for (uint32_t i = 0; i < (1u << (num - 1)); ++i) {
+      int first_bit = (i == 0) ? (num - 1) : __builtin_ctz(i);
+      out.push_back(lowest + (num - 1 - first_bit));
+    }
+    return out;
+  }
+  // advance_allowed_levels (37-48)
+  void advance() {
+    if (first_done && lowest > 0) lowest -= 1;
+    if (!first_done) first_done = true;
+  }
+  // current_max_timestep (77-79): max_timestep * 0.5^lowest
+  double current_max_timestep() const { return std::ldexp(max_timestep, -lowest); }
+};
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+}  // namespace
+
+struct sw_handle {
+  sw_params params{};
+  const swh::PrecisionOps* ops = nullptr;
+  std::vector<double> dirs;
+  int D = 0, Dp = 0, words = 0, L = 1;
+  int64_t N = 0, E = 0;
+  TimestepState ts;
+  double sim_time = 0.0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  swh::DevicePtrs p{};
+  std::vector<void*> allocations;
+  std::vector<uint32_t> n_ge_host;  // cells with level >= l at the start of the next step
+  swk::SweepCtl ctl_host{};
+  sw_stats stats{};
+  std::string last_error;
+  double* scratch = nullptr;  // N doubles for field export
+
+  ~sw_handle() {
+    for (void* a : allocations) cudaFree(a);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  bool alloc(T** ptr, size_t count) {
+    cudaError_t e = dalloc(ptr, count);
+    if (e != cudaSuccess) return false;
+    allocations.push_back((void*)*ptr);
+    return true;
+  }
+
+  sw_status fail(sw_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    last_error = buf;
+    return st;
+  }
+  sw_status cuda_fail(cudaError_t e, const char* where) {
+    return fail(e == cudaErrorMemoryAllocation ? SW_ERR_OOM : SW_ERR_CUDA, "%s: %s", where,
+                cudaGetErrorString(e));
+  }
+};
+
+namespace {
+
+#define SW_CUDA(h, call, where)                   \
+  do {                                            \
+    cudaError_t _e = (call);                      \
+    if (_e != cudaSuccess) return (h)->cuda_fail(_e, where); \
+  } while (0)
+
+sw_status create_fail(sw_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_create_error = buf;
+  return st;
+}
+
+bool directions_for(int num, std::vector<double>& out) {
+  const double(*tab)[3] = nullptr;
+  static const double one[1][3] = {{1.0, 0.0, 0.0}};
+  switch (num) {  // Directions::from_num, src/sweep/direction/mod.rs:58-75
+    case 1: tab = one; break;
+    case 16: tab = kDirectionBins16; break;
+    case 21: tab = kDirectionBins21; break;
+    case 32: tab = kDirectionBins32; break;
+    case 64: tab = kDirectionBins64; break;
+    case 84: tab = kDirectionBins84; break;
+    default: return false;
+  }
+  out.assign(&tab[0][0], &tab[0][0] + 3 * num);
+  return true;
+}
+
+// Each LOCAL / LOCAL_PERIODIC face c -> n needs a face n -> c with the bitwise negated
+// normal: the reference counts upwind faces from c's side and delivers fluxes from
+// n's side, so without it a level sweep could never finish.
+bool check_reciprocal_faces(const sw_grid_csr* g, std::string& why) {
+  std::atomic<int64_t> bad{-1};
+  int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&, t]() {
+      for (int64_t c = t; c < g->num_cells; c += nt) {
+        if (bad.load(std::memory_order_relaxed) >= 0) return;
+        for (int64_t f = g->row_ptr[c]; f < g->row_ptr[c + 1]; ++f) {
+          if (g->kind[f] == SW_FACE_BOUNDARY) continue;
+          int64_t n = g->nbr[f];
+          bool found = false;
+          for (int64_t q = g->row_ptr[n]; q < g->row_ptr[n + 1] && !found; ++q)
+            found = g->kind[q] != SW_FACE_BOUNDARY && g->nbr[q] == c &&
+                    g->normal[3 * q] == -g->normal[3 * f] && g->normal[3 * q + 1] == -g->normal[3 * f + 1] &&
+                    g->normal[3 * q + 2] == -g->normal[3 * f + 2];
+          if (!found) {
+            int64_t expected = -1;
+            bad.compare_exchange_strong(expected, f);
+            return;
+          }
+        }
+      }
+    });
+  for (auto& x : th) x.join();
+  if (bad.load() >= 0) {
+    char buf[200];
+    snprintf(buf, sizeof(buf), "face %lld has no reciprocal face with a negated normal",
+             (long long)bad.load());
+    why = buf;
+    return false;
+  }
+  return true;
+}
+
+// check_deadlock analogue (src/sweep/deadlock_detection.rs): with every cell active,
+// each direction's dependency graph must be acyclic (Kahn's algorithm on the host).
+bool check_acyclic(const sw_grid_csr* g, const std::vector<double>& dirs, int D, std::string& why) {
+  int64_t n = g->num_cells;
+  std::vector<uint32_t> cnt(n);
+  std::vector<int64_t> queue(n);
+  for (int d = 0; d < D; ++d) {
+    const double* dv = &dirs[3 * d];
+    auto dotf = [&](int64_t f) {
+      return g->normal[3 * f] * dv[0] + g->normal[3 * f + 1] * dv[1] + g->normal[3 * f + 2] * dv[2];
+    };
+    int64_t qh = 0, qt = 0;
+    for (int64_t c = 0; c < n; ++c) {
+      uint32_t k = 0;
+      for (int64_t f = g->row_ptr[c]; f < g->row_ptr[c + 1]; ++f)
+        if (g->kind[f] == SW_FACE_LOCAL && dotf(f) < 0.0) ++k;
+      cnt[c] = k;
+      if (k == 0) queue[qt++] = c;
+    }
+    while (qh < qt) {
+      int64_t c = queue[qh++];
+      for (int64_t f = g->row_ptr[c]; f < g->row_ptr[c + 1]; ++f)
+        if (g->kind[f] == SW_FACE_LOCAL && dotf(f) > 0.0)
+          if (--cnt[g->nbr[f]] == 0) queue[qt++] = g->nbr[f];
+    }
+    if (qt != n) {
+      char buf[200];
+      snprintf(buf, sizeof(buf), "direction %d: %lld cells lie on dependency cycles", d, (long long)(n - qt));
+      why = buf;
+      return false;
+    }
+  }
+  return true;
+}
+
+sw_status run_level_order(sw_handle* h) {
+  SW_CUDA(h, swh::launch_level_order(h->p, h->stream), "level order");
+  return SW_OK;
+}
+
+sw_status sync_ctl(sw_handle* h) {
+  SW_CUDA(h, cudaMemcpyAsync(&h->ctl_host, h->p.ctl, sizeof(swk::SweepCtl), cudaMemcpyDeviceToHost, h->stream),
+          "read control block");
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
+  h->n_ge_host.assign(h->ctl_host.n_ge, h->ctl_host.n_ge + h->L);
+  return SW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+sw_status sw_default_params(sw_params* p) {
+  if (!p) return SW_ERR_INVALID_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->num_directions = 84;
+  p->explicit_directions = nullptr;
+  p->num_timestep_levels = 1;
+  p->periodic = 0;
+  p->max_timestep = 1e6 * 3.15576e7;  // 1 Myr
+  p->rotate_directions = 0;               // parameters.rs:64-78
+  p->significant_rate_threshold = 0.0;
+  p->timestep_safety_factor = 0.01 * 10.0;  // Dimensionless::percent(10.0)
+  p->chemistry_timestep_safety_factor = 0.01 * 10.0;
+  p->check_deadlock = 0;
+  p->prevent_cooling = 1;
+  p->num_tasks_to_solve_before_send_receive = 10000;
+  p->scale_factor = 1.0;
+  p->precision = SW_PRECISION_FP64;
+  p->device = -1;
+  return SW_OK;
+}
+
+sw_status sw_directions_from_num(int32_t num, double* out) {
+  std::vector<double> d;
+  if (!out || !directions_for(num, d)) return SW_ERR_INVALID_ARG;
+  std::memcpy(out, d.data(), d.size() * sizeof(double));
+  return SW_OK;
+}
+
+sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_cell_init* init,
+                    sw_handle** out) {
+  g_create_error.clear();
+  if (!out) return create_fail(SW_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (!params || !grid || !init) return create_fail(SW_ERR_INVALID_ARG, "NULL argument");
+  const sw_params& P = *params;
+  if (P.rotate_directions)
+    return create_fail(SW_ERR_UNSUPPORTED, "rotate_directions is not supported by the GPU sweep");
+  if (P.num_timestep_levels < 1 || P.num_timestep_levels > 16)
+    return create_fail(SW_ERR_INVALID_ARG, "num_timestep_levels must be in 1..16");
+  if (!(P.max_timestep > 0.0) || !std::isfinite(P.max_timestep))
+    return create_fail(SW_ERR_INVALID_ARG, "max_timestep must be positive");
+  if (P.precision != SW_PRECISION_FP64 && P.precision != SW_PRECISION_MIXED)
+    return create_fail(SW_ERR_INVALID_ARG, "unknown precision");
+  std::vector<double> dirs;
+  int D = P.num_directions;
+  if (P.explicit_directions) {
+    if (D < 1) return create_fail(SW_ERR_INVALID_ARG, "num_directions must be >= 1");
+    dirs.assign(P.explicit_directions, P.explicit_directions + 3 * D);
+    for (int d = 0; d < D; ++d) {  // glam normalize: v * (1 / |v|)
+      double* v = &dirs[3 * d];
+      double inv = 1.0 / std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      if (!std::isfinite(inv)) return create_fail(SW_ERR_INVALID_ARG, "direction %d has zero length", d);
+      v[0] *= inv;
+      v[1] *= inv;
+      v[2] *= inv;
+    }
+  } else if (!directions_for(D, dirs)) {
+    return create_fail(SW_ERR_INVALID_ARG, "num_directions %d has no direction table (1,16,21,32,64,84)", D);
+  }
+  if (D > 32 * swk::kMaxDirWords) return create_fail(SW_ERR_UNSUPPORTED, "at most 128 directions");
+
+  const int64_t N = grid->num_cells;
+  if (N < 1 || N >= (int64_t)1 << 30) return create_fail(SW_ERR_INVALID_ARG, "num_cells must be in 1..2^30-1");
+  if (!grid->row_ptr || !grid->nbr || !grid->kind || !grid->area || !grid->normal || !grid->volume || !grid->size)
+    return create_fail(SW_ERR_INVALID_ARG, "grid array is NULL");
+  if (!init->density || !init->ionized_hydrogen_fraction || !init->temperature || !init->source)
+    return create_fail(SW_ERR_INVALID_ARG, "cell init array is NULL");
+  if (grid->row_ptr[0] != 0) return create_fail(SW_ERR_INVALID_ARG, "row_ptr[0] must be 0");
+  double max_normal = 0.0;
+  for (int64_t c = 0; c < N; ++c) {
+    int64_t nf = grid->row_ptr[c + 1] - grid->row_ptr[c];
+    if (nf < 0) return create_fail(SW_ERR_INVALID_ARG, "row_ptr not monotone at cell %lld", (long long)c);
+    if (nf > swk::kMaxFaces)
+      return create_fail(SW_ERR_UNSUPPORTED, "cell %lld has %lld faces (max %d)", (long long)c, (long long)nf,
+                         swk::kMaxFaces);
+  }
+  const int64_t E = grid->row_ptr[N];
+  for (int64_t f = 0; f < E; ++f) {
+    uint8_t k = grid->kind[f];
+    if (k > SW_FACE_BOUNDARY) return create_fail(SW_ERR_INVALID_ARG, "face %lld has invalid kind", (long long)f);
+    if (k != SW_FACE_BOUNDARY && (grid->nbr[f] < 0 || grid->nbr[f] >= N))
+      return create_fail(SW_ERR_INVALID_ARG, "face %lld neighbour out of range", (long long)f);
+    const double* nv = &grid->normal[3 * f];
+    double l = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+    if (!std::isfinite(l) || !std::isfinite(grid->area[f]))
+      return create_fail(SW_ERR_INVALID_ARG, "face %lld has non-finite geometry", (long long)f);
+    max_normal = std::max(max_normal, l);
+  }
+  std::string why;
+  if (!check_reciprocal_faces(grid, why)) return create_fail(SW_ERR_INVALID_ARG, "%s", why.c_str());
+  if (P.check_deadlock && !check_acyclic(grid, dirs, D, why)) return create_fail(SW_ERR_STALLED, "%s", why.c_str());
+  if (P.prevent_cooling) {
+    // HydrogenOnly clamps x_HII into [x_floor, 1 - 1e-10] and f64::clamp panics when
+    // the floor (the current x_HII) is above that range.
+    for (int64_t c = 0; c < N; ++c)
+      if (init->ionized_hydrogen_fraction[c] > 1.0 - 1e-10)
+        return create_fail(SW_ERR_INVALID_ARG,
+                           "cell %lld: x_HII above 1 - 1e-10 with prevent_cooling (reference panics)",
+                           (long long)c);
+  }
+
+  sw_handle* h = new sw_handle();
+  h->params = P;
+  h->params.explicit_directions = nullptr;
+  h->ops = (P.precision == SW_PRECISION_MIXED) ? &swh::kOpsMixed : &swh::kOpsFP64;
+  h->dirs = dirs;
+  h->D = D;
+  h->Dp = (D + 7) / 8 * 8;
+  h->words = (D + 31) / 32;
+  h->L = P.num_timestep_levels;
+  h->N = N;
+  h->E = E;
+  h->ts.init(P.max_timestep, P.num_timestep_levels);
+
+  auto bail = [&](sw_status st) {
+    g_create_error = h->last_error;
+    delete h;
+    return st;
+  };
+  cudaError_t ce = (P.device >= 0) ? cudaSetDevice(P.device) : cudaGetDevice(&h->device);
+  if (ce == cudaSuccess && P.device >= 0) h->device = P.device;
+  if (ce != cudaSuccess) {
+    h->cuda_fail(ce, "select device");
+    return bail(SW_ERR_CUDA);
+  }
+  int coop = 0, sms = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (!coop) {
+    h->fail(SW_ERR_CUDA, "device does not support cooperative launches");
+    return bail(SW_ERR_CUDA);
+  }
+  int bps = 0;
+  ce = h->ops->occupancy(&bps);
+  if (ce != cudaSuccess || bps < 1) {
+    h->cuda_fail(ce == cudaSuccess ? cudaErrorInvalidConfiguration : ce, "occupancy");
+    return bail(SW_ERR_CUDA);
+  }
+  if ((ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    h->cuda_fail(ce, "stream");
+    return bail(SW_ERR_CUDA);
+  }
+  for (auto& e : h->ev) cudaEventCreate(&e);
+
+  swh::DevicePtrs& p = h->p;
+  p.num_cells = N;
+  p.D = D;
+  p.Dp = h->Dp;
+  p.words = h->words;
+  p.num_levels = h->L;
+  p.threshold = P.significant_rate_threshold;
+  p.max_timestep = P.max_timestep;
+  p.timestep_safety = P.timestep_safety_factor;
+  p.chem_safety = P.chemistry_timestep_safety_factor;
+  p.scale_factor = P.scale_factor;
+  p.prevent_cooling = P.prevent_cooling;
+  p.coop_blocks = bps * sms;
+  p.timeout_ns = 20ull * 1000 * 1000 * 1000;  // 20 s per barrier wait
+  p.max_rounds = (uint32_t)std::min<int64_t>((int64_t)4 * N + 64, 0x7fffffff);
+  double max_dir = 0.0;
+  for (int d = 0; d < D; ++d)
+    max_dir = std::max(max_dir, std::sqrt(dirs[3 * d] * dirs[3 * d] + dirs[3 * d + 1] * dirs[3 * d + 1] +
+                                          dirs[3 * d + 2] * dirs[3 * d + 2]));
+  // FP32 dot of FP32-rounded vectors: |error| <= ~5 * 2^-24 * |n| |d|; 4x margin.
+  p.guard = (float)(20.0 * std::ldexp(1.0, -24) * std::max(1.0, max_normal) * std::max(1.0, max_dir));
+  // Stored rate unit: photons/s in the FP64 drop-in; a power of two in the mixed path,
+  // so that rates up to the total source (times 2^32 headroom) stay finite in FP32 and
+  // the smallest normal float is ~2^-126 of the largest source.
+  double total_source = 0.0;
+  for (int64_t c = 0; c < N; ++c) total_source += std::fabs(init->source[c]);
+  p.rate_scale = 1.0;
+  if (P.precision == SW_PRECISION_MIXED && total_source > 0.0) {
+    int e = 0;
+    std::frexp(total_source, &e);
+    p.rate_scale = std::ldexp(1.0, e - 96);
+  }
+
+  // geometry upload in kernel layout.  FP32 areas carry a power-of-two scale that maps
+  // the largest face area to ~1 (areas of ~1e42 m^2 overflow FP32); the FP32 transport
+  // only uses ratios of areas within a cell, which the scale leaves exact.
+  double max_area = 0.0;
+  for (int64_t f = 0; f < E; ++f) max_area = std::max(max_area, std::fabs(grid->area[f]));
+  int area_exp = 0;
+  if (max_area > 0.0) std::frexp(max_area, &area_exp);
+  {
+    std::vector<double> geo64(4 * (size_t)E);
+    std::vector<float> geo32(4 * (size_t)E);
+    std::vector<uint32_t> nbr(E);
+    std::vector<long long> row(N + 1);
+    for (int64_t i = 0; i <= N; ++i) row[i] = grid->row_ptr[i];
+    for (int64_t f = 0; f < E; ++f) {
+      for (int a = 0; a < 3; ++a) {
+        geo64[4 * f + a] = grid->normal[3 * f + a];
+        geo32[4 * f + a] = (float)grid->normal[3 * f + a];
+      }
+      geo64[4 * f + 3] = grid->area[f];
+      geo32[4 * f + 3] = (float)std::ldexp(grid->area[f], -area_exp);
+      uint32_t kind = grid->kind[f];
+      uint32_t nb = (kind == SW_FACE_BOUNDARY) ? 0u : (uint32_t)grid->nbr[f];
+      nbr[f] = nb | (kind << swk::kKindShift);
+    }
+    long long* d_row;
+    double* d_geo64;
+    float* d_geo32;
+    uint32_t* d_nbr;
+    if (!h->alloc(&d_row, N + 1) || !h->alloc(&d_geo64, 4 * (size_t)E) || !h->alloc(&d_geo32, 4 * (size_t)E) ||
+        !h->alloc(&d_nbr, E)) {
+      h->fail(SW_ERR_OOM, "device allocation of the grid failed");
+      return bail(SW_ERR_OOM);
+    }
+    cudaMemcpy(d_row, row.data(), (N + 1) * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_geo64, geo64.data(), geo64.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_geo32, geo32.data(), geo32.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_nbr, nbr.data(), E * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    p.row_ptr = d_row;
+    p.geo64 = d_geo64;
+    p.geo32 = d_geo32;
+    p.nbr = d_nbr;
+    // cells that receive periodic contributions
+    std::vector<uint32_t> pcells;
+    for (int64_t c = 0; c < N; ++c)
+      for (int64_t f = grid->row_ptr[c]; f < grid->row_ptr[c + 1]; ++f)
+        if (grid->kind[f] == SW_FACE_LOCAL_PERIODIC) {
+          pcells.push_back((uint32_t)c);
+          break;
+        }
+    uint32_t* d_pc;
+    if (!h->alloc(&d_pc, pcells.size())) {
+      h->fail(SW_ERR_OOM, "device allocation failed");
+      return bail(SW_ERR_OOM);
+    }
+    if (!pcells.empty()) cudaMemcpy(d_pc, pcells.data(), pcells.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    p.periodic_cells = d_pc;
+    p.n_periodic_cells = (uint32_t)pcells.size();
+  }
+  // directions
+  {
+    std::vector<float> d32(dirs.begin(), dirs.end());
+    double* d_dir64;
+    float* d_dir32;
+    if (!h->alloc(&d_dir64, dirs.size()) || !h->alloc(&d_dir32, dirs.size())) {
+      h->fail(SW_ERR_OOM, "device allocation failed");
+      return bail(SW_ERR_OOM);
+    }
+    cudaMemcpy(d_dir64, dirs.data(), dirs.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_dir32, d32.data(), d32.size() * sizeof(float), cudaMemcpyHostToDevice);
+    p.dir64 = d_dir64;
+    p.dir32 = d_dir32;
+  }
+  // cells
+  {
+    double *d_size, *d_volume, *d_density, *d_source, *d_x, *d_y, *d_T, *d_att, *d_prev, *d_cts, *d_sdt, *d_ion;
+    uint8_t* d_level;
+    uint32_t* d_order;
+    bool ok = h->alloc(&d_size, N) && h->alloc(&d_volume, N) && h->alloc(&d_density, N) && h->alloc(&d_source, N) &&
+              h->alloc(&d_x, N) && h->alloc(&d_y, N) && h->alloc(&d_T, N) && h->alloc(&d_att, N) &&
+              h->alloc(&d_prev, N) && h->alloc(&d_cts, N) && h->alloc(&d_sdt, N) && h->alloc(&d_ion, N) &&
+              h->alloc(&d_level, N) && h->alloc(&d_order, N) && h->alloc(&h->scratch, N);
+    if (!ok) {
+      h->fail(SW_ERR_OOM, "device allocation of cell state failed");
+      return bail(SW_ERR_OOM);
+    }
+    std::vector<double> y(N), inf(N, INFINITY);
+    for (int64_t c = 0; c < N; ++c) y[c] = 1.0 - init->ionized_hydrogen_fraction[c];
+    cudaMemcpy(d_size, grid->size, N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_volume, grid->volume, N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_density, init->density, N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_source, init->source, N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_x, init->ionized_hydrogen_fraction, N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_y, y.data(), N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_T, init->temperature, N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_ion, inf.data(), N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemset(d_att, 0, N * sizeof(double));
+    cudaMemset(d_prev, 0, N * sizeof(double));  // Site::new: zero previous rate
+    cudaMemset(d_cts, 0, N * sizeof(double));   // change_timescale = 0
+    cudaMemset(d_sdt, 0, N * sizeof(double));   // species timestep = 0
+    cudaMemset(d_level, h->L - 1, N);           // Sweep::new: all cells at level n-1
+    p.size = d_size;
+    p.volume = d_volume;
+    p.density = d_density;
+    p.source = d_source;
+    p.xhii = d_x;
+    p.yneu = d_y;
+    p.temperature = d_T;
+    p.att = d_att;
+    p.previous_rate = d_prev;
+    p.change_timescale = d_cts;
+    p.species_timestep = d_sdt;
+    p.ionization_time = d_ion;
+    p.level = d_level;
+    p.order = d_order;
+  }
+  // per-(cell, direction) state
+  {
+    size_t nd = (size_t)N * h->Dp;
+    size_t rb = (size_t)h->ops->rate_bytes;
+    void *inc, *outg, *per, *pend;
+    uint32_t *cnt, *ready, *queued, *f0, *f1;
+    swk::SweepCtl* ctl;
+    bool ok = h->alloc((char**)&inc, nd * rb) && h->alloc((char**)&outg, nd * rb) &&
+              h->alloc((char**)&per, nd * rb) && h->alloc((char**)&pend, nd * rb) &&
+              h->alloc(&cnt, (size_t)N * (h->Dp / 4)) && h->alloc(&ready, (size_t)N * swk::kMaxDirWords) &&
+              h->alloc(&queued, N) && h->alloc(&f0, N) && h->alloc(&f1, N) && h->alloc(&ctl, 1);
+    if (!ok) {
+      h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed", 4 * nd * rb >> 20);
+      return bail(SW_ERR_OOM);
+    }
+    cudaMemset(inc, 0, nd * rb);
+    cudaMemset(outg, 0, nd * rb);
+    cudaMemset(per, 0, nd * rb);
+    cudaMemset(pend, 0, nd * rb);
+    cudaMemset(cnt, 0, (size_t)N * (h->Dp / 4) * 4);
+    cudaMemset(ready, 0, (size_t)N * swk::kMaxDirWords * 4);
+    cudaMemset(queued, 0, N * 4);
+    cudaMemset(ctl, 0, sizeof(swk::SweepCtl));
+    p.incoming = inc;
+    p.outgoing = outg;
+    p.periodic = per;
+    p.pending = pend;
+    p.counters = cnt;
+    p.ready = ready;
+    p.queued = queued;
+    p.frontier0 = f0;
+    p.frontier1 = f1;
+    p.ctl = ctl;
+  }
+  ce = cudaDeviceSynchronize();
+  if (ce != cudaSuccess) {
+    h->cuda_fail(ce, "upload");
+    return bail(ce == cudaErrorMemoryAllocation ? SW_ERR_OOM : SW_ERR_CUDA);
+  }
+  if (swh::launch_level_hist(p, h->stream) != cudaSuccess || run_level_order(h) != SW_OK || sync_ctl(h) != SW_OK) {
+    if (h->last_error.empty()) h->fail(SW_ERR_CUDA, "level ordering failed");
+    return bail(SW_ERR_CUDA);
+  }
+  *out = h;
+  return SW_OK;
+}
+
+sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
+  if (!h) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  const swh::PrecisionOps& ops = *h->ops;
+  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  uint64_t expected = 0;
+  std::vector<int> order = h->ts.sweep_order();
+  unsigned long long tasks_before = h->ctl_host.tasks;
+  float sweep_ms = 0.f, chem_ms = 0.f, level_ms = 0.f, kernel_ms = 0.f;
+  int64_t launches = 0;
+  SW_CUDA(h, cudaEventRecord(h->ev[5], h->stream), "event");
+  for (int level : order) {
+    // Sweep::run_sweeps skips levels without active cells (mod.rs:262)
+    if (h->n_ge_host[level] == 0) continue;
+    expected += (uint64_t)h->n_ge_host[level] * (uint64_t)h->D;
+    SW_CUDA(h, cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
+    SW_CUDA(h, cudaEventRecord(h->ev[0], h->stream), "event");
+    SW_CUDA(h, ops.attenuation(h->p, level, h->stream), "attenuation kernel");
+    SW_CUDA(h, ops.init_counts(h->p, level, nullptr, h->stream), "init_counts kernel");
+    SW_CUDA(h, cudaEventRecord(h->ev[6], h->stream), "event");
+    SW_CUDA(h, ops.sweep(h->p, level, h->stream), "sweep kernel");
+    SW_CUDA(h, cudaEventRecord(h->ev[7], h->stream), "event");
+    SW_CUDA(h, ops.fold_periodic(h->p, h->stream), "periodic fold kernel");
+    launches += 4 + (h->p.n_periodic_cells > 0 ? 1 : 0);
+    SW_CUDA(h, cudaEventRecord(h->ev[1], h->stream), "event");
+    SW_CUDA(h, ops.chemistry(h->p, level, h->stream), "chemistry kernel");
+    SW_CUDA(h, cudaEventRecord(h->ev[2], h->stream), "event");
+    SW_CUDA(h, cudaStreamSynchronize(h->stream), "level sweep");
+    float a = 0.f, b = 0.f, k = 0.f;
+    cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&k, h->ev[6], h->ev[7]);
+    sweep_ms += a;
+    chem_ms += b;
+    kernel_ms += k;
+    h->stats.transport_launches += 1;
+    uint32_t err = 0, rounds = 0;
+    SW_CUDA(h, cudaMemcpy(&err, &h->p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
+    SW_CUDA(h, cudaMemcpy(&rounds, &h->p.ctl->rounds, sizeof(rounds), cudaMemcpyDeviceToHost), "read rounds");
+    h->stats.rounds += rounds;
+    h->stats.level_sweeps += 1;
+    if (err & (swk::kErrStall | swk::kErrRounds))
+      return h->fail(SW_ERR_STALLED, "level %d sweep stalled (device wait timed out or round limit; flags 0x%x)",
+                     level, err);
+    if (err & swk::kErrClamp)
+      return h->fail(SW_ERR_INVALID_ARG, "x_HII floor above 1 - 1e-10 in the chemistry clamp (reference panics)");
+  }
+  // TimestepState bookkeeping and level reassignment (mod.rs:268-270)
+  double elapsed = h->ts.current_max_timestep();
+  h->ts.advance();
+  SW_CUDA(h, cudaEventRecord(h->ev[3], h->stream), "event");
+  SW_CUDA(h, swh::launch_update_levels(h->p, h->ts.lowest, h->stream), "level kernels");
+  SW_CUDA(h, cudaEventRecord(h->ev[4], h->stream), "event");
+  h->sim_time += elapsed;
+  SW_CUDA(h, swh::launch_ionization_time(h->p, h->sim_time, h->stream), "ionization time kernel");
+  launches += 4;
+  SW_CUDA(h, cudaEventRecord(h->ev[1], h->stream), "event");
+  sw_status st = sync_ctl(h);
+  if (st != SW_OK) return st;
+  cudaEventElapsedTime(&level_ms, h->ev[3], h->ev[4]);
+  float step_ms = 0.f;
+  cudaEventElapsedTime(&step_ms, h->ev[5], h->ev[1]);
+  h->stats.step_ms += step_ms;
+  h->stats.transport_kernel_ms += kernel_ms;
+  h->stats.kernel_launches += launches;
+  uint64_t solved = h->ctl_host.tasks - tasks_before;
+  h->stats.steps += 1;
+  h->stats.tasks = (int64_t)h->ctl_host.tasks;
+  h->stats.visits = (int64_t)h->ctl_host.visits;
+  h->stats.chem_cells = (int64_t)h->ctl_host.chem_cells;
+  h->stats.chem_attempts = (int64_t)h->ctl_host.chem_attempts;
+  h->stats.chem_failures = (int64_t)h->ctl_host.chem_failures;
+  h->stats.sweep_ms += sweep_ms;
+  h->stats.chem_ms += chem_ms;
+  h->stats.level_ms += level_ms;
+  h->stats.simulation_time = h->sim_time;
+  if (time_elapsed_out) *time_elapsed_out = elapsed;
+  if (solved != expected)
+    return h->fail(SW_ERR_STALLED, "sweep solved %llu of %llu tasks: the dependency graph has a cycle",
+                   (unsigned long long)solved, (unsigned long long)expected);
+  return SW_OK;
+}
+
+sw_status sw_get_fields(sw_handle* h, double* x, double* T, double* dt, double* rate) {
+  if (!h) return SW_ERR_INVALID_ARG;
+  size_t nb = (size_t)h->N * sizeof(double);
+  if (x) SW_CUDA(h, cudaMemcpyAsync(x, h->p.xhii, nb, cudaMemcpyDeviceToHost, h->stream), "copy x");
+  if (T) SW_CUDA(h, cudaMemcpyAsync(T, h->p.temperature, nb, cudaMemcpyDeviceToHost, h->stream), "copy T");
+  if (dt) SW_CUDA(h, cudaMemcpyAsync(dt, h->p.species_timestep, nb, cudaMemcpyDeviceToHost, h->stream), "copy dt");
+  if (rate) {
+    SW_CUDA(h, h->ops->photon_rate(h->p, h->scratch, h->stream), "photon rate kernel");
+    SW_CUDA(h, cudaMemcpyAsync(rate, h->scratch, nb, cudaMemcpyDeviceToHost, h->stream), "copy rate");
+  }
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
+  return SW_OK;
+}
+
+sw_status sw_get_cell_state(sw_handle* h, double* change_timescale, uint8_t* level, double* ionization_time) {
+  if (!h) return SW_ERR_INVALID_ARG;
+  size_t nb = (size_t)h->N * sizeof(double);
+  if (change_timescale)
+    SW_CUDA(h, cudaMemcpyAsync(change_timescale, h->p.change_timescale, nb, cudaMemcpyDeviceToHost, h->stream), "copy");
+  if (level) SW_CUDA(h, cudaMemcpyAsync(level, h->p.level, h->N, cudaMemcpyDeviceToHost, h->stream), "copy");
+  if (ionization_time)
+    SW_CUDA(h, cudaMemcpyAsync(ionization_time, h->p.ionization_time, nb, cudaMemcpyDeviceToHost, h->stream), "copy");
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
+  return SW_OK;
+}
+
+sw_status sw_set_fields(sw_handle* h, const double* x, const double* T) {
+  if (!h) return SW_ERR_INVALID_ARG;
+  size_t nb = (size_t)h->N * sizeof(double);
+  if (x) {
+    std::vector<double> y(h->N);
+    for (int64_t c = 0; c < h->N; ++c) y[c] = 1.0 - x[c];
+    SW_CUDA(h, cudaMemcpy(h->p.xhii, x, nb, cudaMemcpyHostToDevice), "copy x");
+    SW_CUDA(h, cudaMemcpy(h->p.yneu, y.data(), nb, cudaMemcpyHostToDevice), "copy y");
+  }
+  if (T) SW_CUDA(h, cudaMemcpy(h->p.temperature, T, nb, cudaMemcpyHostToDevice), "copy T");
+  return SW_OK;
+}
+
+sw_status sw_get_level_counts(sw_handle* h, int64_t* per_level) {
+  if (!h || !per_level) return SW_ERR_INVALID_ARG;
+  for (int l = 0; l < h->L; ++l) per_level[l] = h->n_ge_host[l];
+  return SW_OK;
+}
+
+sw_status sw_get_dependency_counts(sw_handle* h, int32_t level, uint8_t* counts) {
+  if (!h || !counts || level < 0 || level >= h->L) return SW_ERR_INVALID_ARG;
+  uint8_t* d_counts = nullptr;
+  size_t nb = (size_t)h->N * h->D;
+  SW_CUDA(h, cudaMalloc(&d_counts, nb), "alloc");
+  cudaMemsetAsync(d_counts, 0, nb, h->stream);
+  cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream);
+  cudaError_t e = h->ops->init_counts(h->p, level, d_counts, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_counts, nb, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d_counts);
+  if (e != cudaSuccess) return h->cuda_fail(e, "dependency counts");
+  return SW_OK;
+}
+
+sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double* periodic) {
+  if (!h) return SW_ERR_INVALID_ARG;
+  size_t nb = (size_t)h->N * h->D * sizeof(double);
+  double* d_out = nullptr;
+  SW_CUDA(h, cudaMalloc(&d_out, nb), "alloc");
+  const void* srcs[3] = {h->p.incoming, h->p.outgoing, h->p.periodic};
+  double* dsts[3] = {incoming, outgoing, periodic};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+    if (!dsts[i]) continue;
+    e = h->ops->export_rates(h->p, srcs[i], d_out, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dsts[i], d_out, nb, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  }
+  cudaFree(d_out);
+  if (e != cudaSuccess) return h->cuda_fail(e, "export rates");
+  return SW_OK;
+}
+
+sw_status sw_get_stats(sw_handle* h, sw_stats* out) {
+  if (!h || !out) return SW_ERR_INVALID_ARG;
+  *out = h->stats;
+  return SW_OK;
+}
+
+const char* sw_last_error(const sw_handle* h) {
+  if (!h) return g_create_error.c_str();
+  return h->last_error.c_str();
+}
+
+void sw_destroy(sw_handle* h) {
+  if (!h) return;
+  cudaStreamSynchronize(h->stream);
+  delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+"""Seeded synthetic workloads of the sweep benchmark configurations.
+
+All inputs are generated here (no external dataset): a 1 Mpc periodic box per 32^3
+cells (cell size fixed as the grid grows), jittered-lattice or Poisson Voronoi
+generators, hydrogen number densities (uniform, uncorrelated lognormal, or the
+exponential of a Gaussian random field with P(k) ~ k^-2), T = 1e4 K, x_HII = 1e-10
+and point sources placed on their nearest cell.
+
+  C1  32^3, uniform n_H = 1e-3 cm^-3, one 5e48 photons/s source at the centre,
+      84 directions, 1 level, max_timestep 1 Myr, threshold 1e-5 photons/s
+  C2  128^3, lognormal n_H (ln-sigma 1, mean 1e-3), 64 sources log-uniform in
+      1e48..1e50 at random positions, 84 directions, 4 levels, safety 0.1
+  C4  256^3, n_H = exp(GRF), P(k) ~ k^-2, ln-sigma 1.5, mean 2e-4, 1000 sources at
+      the densest cells with rates proportional to density (1e52 total),
+      84 directions, 4 levels
+Any configuration can be scaled down (`n_per_side`) for tests.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import grid as gridmod
+from .sweep import MEGAPARSEC, MEGAYEAR, SweepParameters, mass_density_from_number_density
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    params: SweepParameters
+    grid: gridmod.Grid
+    density: np.ndarray
+    ionized_hydrogen_fraction: np.ndarray
+    temperature: np.ndarray
+    source: np.ndarray
+    steps: int
+
+    def describe(self) -> dict:
+        return {
+            "workload": self.name,
+            "cells": self.grid.num_cells,
+            "faces_per_cell": round(self.grid.num_faces / self.grid.num_cells, 3),
+            "directions": self.params.num_directions(),
+            "timestep_levels": self.params.num_timestep_levels,
+            "periodic": self.params.periodic,
+            "significant_rate_threshold": self.params.significant_rate_threshold,
+        }
+
+
+def _box_for(n_per_side: int) -> float:
+    return MEGAPARSEC * n_per_side / 32.0
+
+
+def c1_small_periodic(n_per_side: int = 32, seed: int = 1, num_directions: int = 84,
+                      nthreads: int = 0) -> Workload:
+    box = _box_for(n_per_side)
+    pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
+    g = gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
+    n = g.num_cells
+    src = gridmod.place_sources(g, np.array([[box / 2, box / 2, box / 2]]), np.array([5e48]))
+    params = SweepParameters(directions=num_directions, num_timestep_levels=1, periodic=True,
+                             max_timestep=1.0 * MEGAYEAR, significant_rate_threshold=1e-5)
+    return Workload(f"C1 periodic jittered-lattice Voronoi {n_per_side}^3, {num_directions} dirs, 1 level",
+                    params, g, np.full(n, float(mass_density_from_number_density(1e-3))), np.full(n, 1e-10),
+                    np.full(n, 1e4), src, steps=10)
+
+
+def c2_lognormal(n_per_side: int = 128, seed: int = 2, num_directions: int = 84, num_levels: int = 4,
+                 nthreads: int = 0) -> Workload:
+    box = _box_for(n_per_side)
+    rng = np.random.default_rng(seed)
+    pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
+    g = gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
+    n = g.num_cells
+    sigma = 1.0
+    n_h = 1e-3 * np.exp(sigma * rng.standard_normal(n) - 0.5 * sigma * sigma)
+    pos = rng.uniform(0.0, box, size=(64, 3))
+    rates = 10.0 ** rng.uniform(48.0, 50.0, size=64)
+    src = gridmod.place_sources(g, pos, rates)
+    params = SweepParameters(directions=num_directions, num_timestep_levels=num_levels, periodic=True,
+                             max_timestep=1.0 * MEGAYEAR, timestep_safety_factor=0.1)
+    return Workload(f"C2 periodic jittered-lattice Voronoi {n_per_side}^3 lognormal, {num_directions} dirs, "
+                    f"{num_levels} levels", params, g, mass_density_from_number_density(n_h), np.full(n, 1e-10),
+                    np.full(n, 1e4), src, steps=4)
+
+
+def gaussian_random_field(m: int, ln_sigma: float, seed: int) -> np.ndarray:
+    """Gaussian random field on an m^3 lattice with P(k) ~ k^-2, unit-normalised to
+    standard deviation ln_sigma (the field whose exponential gives the density)."""
+    rng = np.random.default_rng(seed)
+    white = rng.standard_normal((m, m, m))
+    k = np.fft.fftfreq(m)
+    kz = np.fft.rfftfreq(m)
+    k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
+    amp = np.zeros_like(k2)
+    amp[k2 > 0] = 1.0 / np.sqrt(k2[k2 > 0])  # sqrt(P) with P ~ k^-2
+    field = np.fft.irfftn(np.fft.rfftn(white) * amp, s=(m, m, m))
+    field -= field.mean()
+    return field * (ln_sigma / field.std())
+
+
+def c4_grf(n_per_side: int = 256, seed: int = 4, ln_sigma: float = 1.5, num_sources: int = 1000,
+           num_directions: int = 84, num_levels: int = 4, nthreads: int = 0) -> Workload:
+    box = _box_for(n_per_side)
+    pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
+    g = gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
+    n = g.num_cells
+    field = gaussian_random_field(n_per_side, ln_sigma, seed)
+    ijk = np.minimum((g.position / box * n_per_side).astype(np.int64), n_per_side - 1)
+    ln_n = field[ijk[:, 0], ijk[:, 1], ijk[:, 2]]
+    n_h = np.exp(ln_n)
+    n_h *= 2e-4 / n_h.mean()
+    peaks = np.argsort(n_h)[-num_sources:]
+    src = np.zeros(n)
+    src[peaks] = n_h[peaks] / n_h[peaks].sum() * 1e52
+    params = SweepParameters(directions=num_directions, num_timestep_levels=num_levels, periodic=True,
+                             max_timestep=1.0 * MEGAYEAR)
+    return Workload(f"C4 periodic jittered-lattice Voronoi {n_per_side}^3 GRF, {num_directions} dirs, "
+                    f"{num_levels} levels", params, g, mass_density_from_number_density(n_h), np.full(n, 1e-10),
+                    np.full(n, 1e4), src, steps=4)
+
+
+def cartesian_column(n: int, cell_size: float, n_h: float, source_rate: float, num_levels: int = 1,
+                     max_timestep: float = 1.0 * MEGAYEAR) -> Workload:
+    """1-D column along x (n x 1 x 1 cartesian cells, non-periodic, 1 direction (1,0,0)):
+    the setting of the reference's examples/sweep_1d.rs."""
+    g = gridmod.cartesian(n, 1, 1, cell_size, periodic=False)
+    src = np.zeros(n)
+    src[0] = source_rate
+    params = SweepParameters(directions=1, num_timestep_levels=num_levels, periodic=False,
+                             max_timestep=max_timestep)
+    return Workload(f"cartesian column {n}", params, g,
+                    np.full(n, float(mass_density_from_number_density(n_h))), np.full(n, 1e-10),
+                    np.full(n, 1e4), src, steps=1)
