@@ -283,6 +283,7 @@ def run_ours(args, dist: Dist):
             "tasks": tasks, "chem_cells": chem, "d": d, "clocks": clocks,
         }
     # error of the mixed path against the FP64 drop-in after identical steps
+    sched_levels = int(handles["mixed"].stats()["schedule_levels"])
     fm, ff = handles["mixed"].fields(), handles["fp64"].fields()
     err = {
         "max_abs_dx_HII": float(np.abs(fm["ionized_hydrogen_fraction"] - ff["ionized_hydrogen_fraction"]).max()),
@@ -355,7 +356,8 @@ def run_ours(args, dist: Dist):
         "clocks": mixed["clocks"],
         "clocks_fp64": results["fp64"]["clocks"],
         "cpu_baseline": cpu,
-        "stats": {"rounds": d["rounds"], "visits": d["visits"], "tasks": d["tasks"],
+        "stats": {"tasks": d["tasks"], "levelled_sweeps": d["levelled_sweeps"],
+                  "sweeps": d["level_sweeps"], "schedule_levels": sched_levels,
                   "chem_attempts": d["chem_attempts"], "transport_kernel_ms": d["transport_kernel_ms"],
                   "sweep_ms": d["sweep_ms"], "chem_ms": d["chem_ms"], "level_ms": d["level_ms"],
                   "fp64_transport_kernel_ms": results["fp64"]["d"]["transport_kernel_ms"],

@@ -101,8 +101,6 @@ typedef struct {
   int64_t chem_cells;     /* chemistry cell updates */
   int64_t chem_attempts;  /* try_timestep_update calls */
   int64_t chem_failures;  /* cells whose chemistry did not converge (reference: log::error) */
-  int64_t rounds;         /* dependency rounds of the persistent sweep kernel */
-  int64_t visits;         /* cell visits of the sweep kernel (tasks / visits = batch size) */
   double sweep_ms;        /* device time in transport kernels (incl. counting, folding) */
   double chem_ms;         /* device time in chemistry kernels */
   double level_ms;        /* device time in level reassignment */
@@ -111,6 +109,8 @@ typedef struct {
   double transport_kernel_ms;  /* device time of the persistent transport kernel alone */
   int64_t transport_launches;  /* launches of the persistent transport kernel */
   int64_t kernel_launches;     /* all kernel launches made by sw_step */
+  int64_t levelled_sweeps;     /* level sweeps run on the precomputed levelled schedule */
+  int64_t schedule_levels;     /* Kahn levels of the schedule (0: cyclic grid, no schedule) */
 } sw_stats;
 
 /* Fill the reference's defaults (num_directions 84, levels 1, max_timestep 1 Myr). */

@@ -86,8 +86,6 @@ class SwStats(ctypes.Structure):
         ("chem_cells", c_int64),
         ("chem_attempts", c_int64),
         ("chem_failures", c_int64),
-        ("rounds", c_int64),
-        ("visits", c_int64),
         ("sweep_ms", c_double),
         ("chem_ms", c_double),
         ("level_ms", c_double),
@@ -96,6 +94,8 @@ class SwStats(ctypes.Structure):
         ("transport_kernel_ms", c_double),
         ("transport_launches", c_int64),
         ("kernel_launches", c_int64),
+        ("levelled_sweeps", c_int64),
+        ("schedule_levels", c_int64),
     ]
 
 

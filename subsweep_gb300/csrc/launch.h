@@ -14,19 +14,22 @@ struct SweepCtl;
 
 namespace swh {
 
-// Raw device pointers of one handle.  Rate arrays are double (FP64) or float (mixed).
+// Raw device pointers of one handle.  Rate arrays are double (FP64) or float (mixed);
+// per-task arrays are [dir][cell] with cell stride Np.
 struct DevicePtrs {
   int64_t num_cells;
-  int D, Dp, words, num_levels;
+  int D, num_levels;
+  uint32_t Np;
   float guard;
   double rate_scale;         // photons/s per stored rate unit
   double threshold;          // significant_rate_threshold in photons/s
   double max_timestep, timestep_safety, chem_safety, scale_factor;
   int prevent_cooling;
+  float dir32_host[128 * 3];  // directions for by-value kernel parameters
   // geometry
-  const long long* row_ptr;
+  const uint32_t* off;
   const void* geo64;  // {nx, ny, nz, area} x E doubles, 32-byte aligned
-  const void* geo32;  // float4[E]
+  const void* geo32;  // float4[E], area scaled by a power of two
   const uint32_t* nbr;
   const double* size;
   const double* volume;
@@ -34,9 +37,9 @@ struct DevicePtrs {
   const float* dir32;
   // cells
   uint8_t* level;
-  uint32_t* order;
   const double* density;
   const double* source;
+  const void* src_dir;       // source / D per cell in stored rate units (R)
   double* xhii;
   double* yneu;
   double* temperature;
@@ -51,16 +54,16 @@ struct DevicePtrs {
   void* periodic;
   void* pending;
   uint32_t* counters;
-  uint32_t* ready;
-  uint32_t* queued;
-  uint32_t* frontier0;
-  uint32_t* frontier1;
+  uint32_t* queue;
+  uint32_t* order;           // levelled schedule: task ids grouped by Kahn level
+  const uint32_t* lvl;       // level offsets into order [num_sched_levels + 1]
+  uint32_t num_sched_levels; // 0: no levelled schedule (cyclic graph)
+  int level_blocks;          // resident blocks of the levelled kernel
   const uint32_t* periodic_cells;
   uint32_t n_periodic_cells;
   swk::SweepCtl* ctl;
   int coop_blocks;
   unsigned long long timeout_ns;
-  uint32_t max_rounds;
 };
 
 struct PrecisionOps {
@@ -69,8 +72,12 @@ struct PrecisionOps {
   // blocks of the persistent sweep kernel that are co-resident on this device
   cudaError_t (*occupancy)(int* blocks_per_sm);
   cudaError_t (*attenuation)(const DevicePtrs&, int level, cudaStream_t);
-  cudaError_t (*init_counts)(const DevicePtrs&, int level, uint8_t* debug_counts, cudaStream_t);
+  cudaError_t (*init_counts)(const DevicePtrs&, int level, uint8_t* debug_counts, bool enqueue, cudaStream_t);
   cudaError_t (*sweep)(const DevicePtrs&, int level, cudaStream_t);
+  cudaError_t (*occupancy_levels)(int* blocks_per_sm);
+  cudaError_t (*sweep_levels)(const DevicePtrs&, int level, cudaStream_t);
+  cudaError_t (*kahn_round)(const DevicePtrs&, uint32_t begin, uint32_t end, cudaStream_t);
+  cudaError_t (*schedule_seed)(const DevicePtrs&, cudaStream_t);
   cudaError_t (*fold_periodic)(const DevicePtrs&, cudaStream_t);
   cudaError_t (*chemistry)(const DevicePtrs&, int level, cudaStream_t);
   cudaError_t (*photon_rate)(const DevicePtrs&, double* out, cudaStream_t);
@@ -83,7 +90,6 @@ extern const PrecisionOps kOpsMixed;
 // Precision-independent kernels (compiled in sweep_fp64.cu).
 cudaError_t launch_update_levels(const DevicePtrs&, int lowest_allowed, cudaStream_t);
 cudaError_t launch_level_hist(const DevicePtrs&, cudaStream_t);
-cudaError_t launch_level_order(const DevicePtrs&, cudaStream_t);
 cudaError_t launch_ionization_time(const DevicePtrs&, double time, cudaStream_t);
 
 }  // namespace swh

@@ -21,23 +21,15 @@ cudaError_t launch_update_levels(const DevicePtrs& p, int lowest_allowed, cudaSt
       p.num_levels, lowest_allowed, p.ctl);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  swk::k_level_offsets<<<1, 32, 0, s>>>(p.ctl, p.num_levels);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  swk::k_level_scatter<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.level, p.ctl, p.order);
+  swk::k_level_counts<<<1, 32, 0, s>>>(p.ctl, p.num_levels);
   return cudaGetLastError();
 }
 
 cudaError_t launch_level_hist(const DevicePtrs& p, cudaStream_t s) {
   swk::k_level_hist<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.level, p.num_levels, p.ctl);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_level_order(const DevicePtrs& p, cudaStream_t s) {
-  swk::k_level_offsets<<<1, 32, 0, s>>>(p.ctl, p.num_levels);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  swk::k_level_scatter<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.level, p.ctl, p.order);
+  swk::k_level_counts<<<1, 32, 0, s>>>(p.ctl, p.num_levels);
   return cudaGetLastError();
 }
 

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -72,7 +73,8 @@ struct sw_handle {
   sw_params params{};
   const swh::PrecisionOps* ops = nullptr;
   std::vector<double> dirs;
-  int D = 0, Dp = 0, words = 0, L = 1;
+  int D = 0, L = 1;
+  uint32_t Np = 0;
   int64_t N = 0, E = 0;
   TimestepState ts;
   double sim_time = 0.0;
@@ -86,6 +88,8 @@ struct sw_handle {
   sw_stats stats{};
   std::string last_error;
   double* scratch = nullptr;  // N doubles for field export
+  uint32_t stats_schedule_levels = 0;
+  int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
 
   ~sw_handle() {
     for (void* a : allocations) cudaFree(a);
@@ -224,16 +228,48 @@ bool check_acyclic(const sw_grid_csr* g, const std::vector<double>& dirs, int D,
   return true;
 }
 
-sw_status run_level_order(sw_handle* h) {
-  SW_CUDA(h, swh::launch_level_order(h->p, h->stream), "level order");
-  return SW_OK;
-}
-
 sw_status sync_ctl(sw_handle* h) {
   SW_CUDA(h, cudaMemcpyAsync(&h->ctl_host, h->p.ctl, sizeof(swk::SweepCtl), cudaMemcpyDeviceToHost, h->stream),
           "read control block");
   SW_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
   h->n_ge_host.assign(h->ctl_host.n_ge, h->ctl_host.n_ge + h->L);
+  return SW_OK;
+}
+
+// Levelled schedule (Kahn levels of all N*D tasks with every cell active), built once
+// per grid on the device.  A dependency cycle leaves tasks unscheduled; such a grid
+// keeps only the dependency-driven path, whose sweep then reports the stall as the
+// reference would deadlock.
+sw_status build_schedule(sw_handle* h) {
+  swh::DevicePtrs& p = h->p;
+  const uint64_t total = (uint64_t)h->N * (uint64_t)h->D;
+  SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
+  SW_CUDA(h, h->ops->schedule_seed(p, h->stream), "schedule seed kernel");
+  std::vector<uint32_t> lvl = {0};
+  unsigned long long tail = 0;
+  SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule seed");
+  uint32_t begin = 0;
+  while (tail > begin) {
+    const uint32_t end = (uint32_t)tail;
+    lvl.push_back(end);
+    SW_CUDA(h, h->ops->kahn_round(p, begin, end, h->stream), "schedule round kernel");
+    SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
+    SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule round");
+    begin = end;
+  }
+  uint32_t err = 0;
+  SW_CUDA(h, cudaMemcpy(&err, &p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
+  if (tail != total || err != 0) {
+    p.num_sched_levels = 0;  // cyclic dependency graph
+    return SW_OK;
+  }
+  uint32_t* d_lvl;
+  if (!h->alloc(&d_lvl, lvl.size())) return h->fail(SW_ERR_OOM, "device allocation of the schedule failed");
+  SW_CUDA(h, cudaMemcpy(d_lvl, lvl.data(), lvl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload schedule");
+  p.lvl = d_lvl;
+  p.num_sched_levels = (uint32_t)(lvl.size() - 1);
+  h->stats_schedule_levels = p.num_sched_levels;
   return SW_OK;
 }
 
@@ -300,10 +336,13 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   } else if (!directions_for(D, dirs)) {
     return create_fail(SW_ERR_INVALID_ARG, "num_directions %d has no direction table (1,16,21,32,64,84)", D);
   }
-  if (D > 32 * swk::kMaxDirWords) return create_fail(SW_ERR_UNSUPPORTED, "at most 128 directions");
+  if (D > swk::kMaxDirections) return create_fail(SW_ERR_UNSUPPORTED, "at most 128 directions");
 
   const int64_t N = grid->num_cells;
   if (N < 1 || N >= (int64_t)1 << 30) return create_fail(SW_ERR_INVALID_ARG, "num_cells must be in 1..2^30-1");
+  const uint32_t Np = (uint32_t)((N + 31) / 32 * 32);
+  if ((uint64_t)Np * (uint64_t)D >= 0xffffffffull)
+    return create_fail(SW_ERR_UNSUPPORTED, "num_cells * directions must stay below 2^32 task ids");
   if (!grid->row_ptr || !grid->nbr || !grid->kind || !grid->area || !grid->normal || !grid->volume || !grid->size)
     return create_fail(SW_ERR_INVALID_ARG, "grid array is NULL");
   if (!init->density || !init->ionized_hydrogen_fraction || !init->temperature || !init->source)
@@ -318,6 +357,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
                          swk::kMaxFaces);
   }
   const int64_t E = grid->row_ptr[N];
+  if (E >= 0xffffffffll) return create_fail(SW_ERR_UNSUPPORTED, "at most 2^32-1 faces");
   for (int64_t f = 0; f < E; ++f) {
     uint8_t k = grid->kind[f];
     if (k > SW_FACE_BOUNDARY) return create_fail(SW_ERR_INVALID_ARG, "face %lld has invalid kind", (long long)f);
@@ -348,8 +388,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   h->ops = (P.precision == SW_PRECISION_MIXED) ? &swh::kOpsMixed : &swh::kOpsFP64;
   h->dirs = dirs;
   h->D = D;
-  h->Dp = (D + 7) / 8 * 8;
-  h->words = (D + 31) / 32;
+  h->Np = Np;
   h->L = P.num_timestep_levels;
   h->N = N;
   h->E = E;
@@ -388,18 +427,40 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   swh::DevicePtrs& p = h->p;
   p.num_cells = N;
   p.D = D;
-  p.Dp = h->Dp;
-  p.words = h->words;
+  p.Np = Np;
   p.num_levels = h->L;
+  for (int i = 0; i < 3 * D; ++i) p.dir32_host[i] = (float)dirs[i];
   p.threshold = P.significant_rate_threshold;
   p.max_timestep = P.max_timestep;
   p.timestep_safety = P.timestep_safety_factor;
   p.chem_safety = P.chemistry_timestep_safety_factor;
   p.scale_factor = P.scale_factor;
   p.prevent_cooling = P.prevent_cooling;
+  // Resident blocks of the persistent transport kernel: at most the occupancy limit;
+  // SUBSWEEP_SWEEP_BLOCKS_PER_SM lowers it (launch-shape tuning).
+  // The dependency-driven kernel is bound by contention on its queue counters, not by
+  // occupancy: one resident block per SM measured fastest.
+  int want = 1;
+  if (const char* env = std::getenv("SUBSWEEP_SWEEP_BLOCKS_PER_SM")) want = std::atoi(env);
+  if (want >= 1 && want < bps) bps = want;
   p.coop_blocks = bps * sms;
-  p.timeout_ns = 20ull * 1000 * 1000 * 1000;  // 20 s per barrier wait
-  p.max_rounds = (uint32_t)std::min<int64_t>((int64_t)4 * N + 64, 0x7fffffff);
+  int lbps = 0;
+  ce = h->ops->occupancy_levels(&lbps);
+  if (ce != cudaSuccess || lbps < 1) {
+    h->cuda_fail(ce == cudaSuccess ? cudaErrorInvalidConfiguration : ce, "occupancy");
+    return bail(SW_ERR_CUDA);
+  }
+  if (const char* env = std::getenv("SUBSWEEP_LEVEL_BLOCKS_PER_SM")) {
+    int v = std::atoi(env);
+    if (v >= 1 && v < lbps) lbps = v;
+  }
+  p.level_blocks = lbps * sms;
+  // SUBSWEEP_TRANSPORT=levels|queue pins the transport kernel (tests and tuning).
+  if (const char* env = std::getenv("SUBSWEEP_TRANSPORT")) {
+    if (std::strcmp(env, "levels") == 0) h->force_path = 1;
+    if (std::strcmp(env, "queue") == 0) h->force_path = 2;
+  }
+  p.timeout_ns = 2ull * 1000 * 1000 * 1000;  // a lane waits at most 2 s for its queue slot
   double max_dir = 0.0;
   for (int d = 0; d < D; ++d)
     max_dir = std::max(max_dir, std::sqrt(dirs[3 * d] * dirs[3 * d] + dirs[3 * d + 1] * dirs[3 * d + 1] +
@@ -429,8 +490,8 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     std::vector<double> geo64(4 * (size_t)E);
     std::vector<float> geo32(4 * (size_t)E);
     std::vector<uint32_t> nbr(E);
-    std::vector<long long> row(N + 1);
-    for (int64_t i = 0; i <= N; ++i) row[i] = grid->row_ptr[i];
+    std::vector<uint32_t> row(N + 1);
+    for (int64_t i = 0; i <= N; ++i) row[i] = (uint32_t)grid->row_ptr[i];
     for (int64_t f = 0; f < E; ++f) {
       for (int a = 0; a < 3; ++a) {
         geo64[4 * f + a] = grid->normal[3 * f + a];
@@ -442,7 +503,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
       uint32_t nb = (kind == SW_FACE_BOUNDARY) ? 0u : (uint32_t)grid->nbr[f];
       nbr[f] = nb | (kind << swk::kKindShift);
     }
-    long long* d_row;
+    uint32_t* d_row;
     double* d_geo64;
     float* d_geo32;
     uint32_t* d_nbr;
@@ -451,11 +512,11 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
       h->fail(SW_ERR_OOM, "device allocation of the grid failed");
       return bail(SW_ERR_OOM);
     }
-    cudaMemcpy(d_row, row.data(), (N + 1) * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_row, row.data(), (N + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice);
     cudaMemcpy(d_geo64, geo64.data(), geo64.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(d_geo32, geo32.data(), geo32.size() * sizeof(float), cudaMemcpyHostToDevice);
     cudaMemcpy(d_nbr, nbr.data(), E * sizeof(uint32_t), cudaMemcpyHostToDevice);
-    p.row_ptr = d_row;
+    p.off = d_row;
     p.geo64 = d_geo64;
     p.geo32 = d_geo32;
     p.nbr = d_nbr;
@@ -494,17 +555,28 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   {
     double *d_size, *d_volume, *d_density, *d_source, *d_x, *d_y, *d_T, *d_att, *d_prev, *d_cts, *d_sdt, *d_ion;
     uint8_t* d_level;
-    uint32_t* d_order;
+    char* d_src_dir;
+    const size_t rb = (size_t)h->ops->rate_bytes;
     bool ok = h->alloc(&d_size, N) && h->alloc(&d_volume, N) && h->alloc(&d_density, N) && h->alloc(&d_source, N) &&
               h->alloc(&d_x, N) && h->alloc(&d_y, N) && h->alloc(&d_T, N) && h->alloc(&d_att, N) &&
               h->alloc(&d_prev, N) && h->alloc(&d_cts, N) && h->alloc(&d_sdt, N) && h->alloc(&d_ion, N) &&
-              h->alloc(&d_level, N) && h->alloc(&d_order, N) && h->alloc(&h->scratch, N);
+              h->alloc(&d_level, N) && h->alloc(&d_src_dir, N * rb) && h->alloc(&h->scratch, N);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of cell state failed");
       return bail(SW_ERR_OOM);
     }
     std::vector<double> y(N), inf(N, INFINITY);
     for (int64_t c = 0; c < N; ++c) y[c] = 1.0 - init->ionized_hydrogen_fraction[c];
+    // Site::source_per_direction_bin (site.rs:49-51), in stored rate units
+    if (rb == 8) {
+      std::vector<double> sd(N);
+      for (int64_t c = 0; c < N; ++c) sd[c] = init->source[c] / (double)D;
+      cudaMemcpy(d_src_dir, sd.data(), N * sizeof(double), cudaMemcpyHostToDevice);
+    } else {
+      std::vector<float> sd(N);
+      for (int64_t c = 0; c < N; ++c) sd[c] = (float)(init->source[c] / (double)D / p.rate_scale);
+      cudaMemcpy(d_src_dir, sd.data(), N * sizeof(float), cudaMemcpyHostToDevice);
+    }
     cudaMemcpy(d_size, grid->size, N * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(d_volume, grid->volume, N * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(d_density, init->density, N * sizeof(double), cudaMemcpyHostToDevice);
@@ -531,40 +603,36 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     p.species_timestep = d_sdt;
     p.ionization_time = d_ion;
     p.level = d_level;
-    p.order = d_order;
+    p.src_dir = d_src_dir;
   }
-  // per-(cell, direction) state
+  // per-(cell, direction) state, [dir][cell]
   {
-    size_t nd = (size_t)N * h->Dp;
-    size_t rb = (size_t)h->ops->rate_bytes;
-    void *inc, *outg, *per, *pend;
-    uint32_t *cnt, *ready, *queued, *f0, *f1;
+    const size_t nd = (size_t)Np * D;
+    const size_t rb = (size_t)h->ops->rate_bytes;
+    char *inc, *outg, *per, *pend;
+    uint32_t *cnt, *queue, *order;
     swk::SweepCtl* ctl;
-    bool ok = h->alloc((char**)&inc, nd * rb) && h->alloc((char**)&outg, nd * rb) &&
-              h->alloc((char**)&per, nd * rb) && h->alloc((char**)&pend, nd * rb) &&
-              h->alloc(&cnt, (size_t)N * (h->Dp / 4)) && h->alloc(&ready, (size_t)N * swk::kMaxDirWords) &&
-              h->alloc(&queued, N) && h->alloc(&f0, N) && h->alloc(&f1, N) && h->alloc(&ctl, 1);
+    bool ok = h->alloc(&inc, nd * rb) && h->alloc(&outg, nd * rb) && h->alloc(&per, nd * rb) &&
+              h->alloc(&pend, nd * rb) && h->alloc(&cnt, nd / 4) && h->alloc(&queue, nd) &&
+              h->alloc(&order, nd) && h->alloc(&ctl, 1);
     if (!ok) {
-      h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed", 4 * nd * rb >> 20);
+      h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed", (4 * rb + 5) * nd >> 20);
       return bail(SW_ERR_OOM);
     }
     cudaMemset(inc, 0, nd * rb);
     cudaMemset(outg, 0, nd * rb);
     cudaMemset(per, 0, nd * rb);
     cudaMemset(pend, 0, nd * rb);
-    cudaMemset(cnt, 0, (size_t)N * (h->Dp / 4) * 4);
-    cudaMemset(ready, 0, (size_t)N * swk::kMaxDirWords * 4);
-    cudaMemset(queued, 0, N * 4);
+    cudaMemset(cnt, 0, nd);
+    cudaMemset(queue, 0xff, nd * sizeof(uint32_t));  // every slot empty
     cudaMemset(ctl, 0, sizeof(swk::SweepCtl));
     p.incoming = inc;
     p.outgoing = outg;
     p.periodic = per;
     p.pending = pend;
     p.counters = cnt;
-    p.ready = ready;
-    p.queued = queued;
-    p.frontier0 = f0;
-    p.frontier1 = f1;
+    p.queue = queue;
+    p.order = order;
     p.ctl = ctl;
   }
   ce = cudaDeviceSynchronize();
@@ -572,9 +640,13 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     h->cuda_fail(ce, "upload");
     return bail(ce == cudaErrorMemoryAllocation ? SW_ERR_OOM : SW_ERR_CUDA);
   }
-  if (swh::launch_level_hist(p, h->stream) != cudaSuccess || run_level_order(h) != SW_OK || sync_ctl(h) != SW_OK) {
+  if (swh::launch_level_hist(p, h->stream) != cudaSuccess || sync_ctl(h) != SW_OK) {
     if (h->last_error.empty()) h->fail(SW_ERR_CUDA, "level ordering failed");
     return bail(SW_ERR_CUDA);
+  }
+  {
+    sw_status st = build_schedule(h);
+    if (st != SW_OK) return bail(st);
   }
   *out = h;
   return SW_OK;
@@ -595,15 +667,26 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     // Sweep::run_sweeps skips levels without active cells (mod.rs:262)
     if (h->n_ge_host[level] == 0) continue;
     expected += (uint64_t)h->n_ge_host[level] * (uint64_t)h->D;
-    SW_CUDA(h, cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
+    SW_CUDA(h, cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset queue");
     SW_CUDA(h, cudaEventRecord(h->ev[0], h->stream), "event");
     SW_CUDA(h, ops.attenuation(h->p, level, h->stream), "attenuation kernel");
-    SW_CUDA(h, ops.init_counts(h->p, level, nullptr, h->stream), "init_counts kernel");
+    // Sweeps with at least 1/16 of the cells active walk the precomputed schedule;
+    // sparser ones use the dependency-driven queue, which touches only active tasks.
+    bool levelled = h->p.num_sched_levels > 0 && (uint64_t)h->n_ge_host[level] * 16 >= (uint64_t)h->N;
+    if (h->force_path == 1) levelled = h->p.num_sched_levels > 0;
+    if (h->force_path == 2) levelled = false;
+    SW_CUDA(h, ops.init_counts(h->p, level, nullptr, !levelled, h->stream), "init_counts kernel");
+    launches += 1;
     SW_CUDA(h, cudaEventRecord(h->ev[6], h->stream), "event");
-    SW_CUDA(h, ops.sweep(h->p, level, h->stream), "sweep kernel");
+    if (levelled) {
+      SW_CUDA(h, ops.sweep_levels(h->p, level, h->stream), "levelled sweep kernel");
+      h->stats.levelled_sweeps += 1;
+    } else {
+      SW_CUDA(h, ops.sweep(h->p, level, h->stream), "sweep kernel");
+    }
     SW_CUDA(h, cudaEventRecord(h->ev[7], h->stream), "event");
     SW_CUDA(h, ops.fold_periodic(h->p, h->stream), "periodic fold kernel");
-    launches += 4 + (h->p.n_periodic_cells > 0 ? 1 : 0);
+    launches += 3 + (h->p.n_periodic_cells > 0 ? 1 : 0);
     SW_CUDA(h, cudaEventRecord(h->ev[1], h->stream), "event");
     SW_CUDA(h, ops.chemistry(h->p, level, h->stream), "chemistry kernel");
     SW_CUDA(h, cudaEventRecord(h->ev[2], h->stream), "event");
@@ -616,14 +699,17 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     chem_ms += b;
     kernel_ms += k;
     h->stats.transport_launches += 1;
-    uint32_t err = 0, rounds = 0;
+    uint32_t err = 0;
     SW_CUDA(h, cudaMemcpy(&err, &h->p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
-    SW_CUDA(h, cudaMemcpy(&rounds, &h->p.ctl->rounds, sizeof(rounds), cudaMemcpyDeviceToHost), "read rounds");
-    h->stats.rounds += rounds;
     h->stats.level_sweeps += 1;
-    if (err & (swk::kErrStall | swk::kErrRounds))
-      return h->fail(SW_ERR_STALLED, "level %d sweep stalled (device wait timed out or round limit; flags 0x%x)",
-                     level, err);
+    if (err & (swk::kErrStall | swk::kErrQueue)) {
+      // leave the queue empty so the handle stays usable for inspection
+      cudaMemsetAsync(h->p.queue, 0xff, (size_t)h->Np * h->D * sizeof(uint32_t), h->stream);
+      cudaStreamSynchronize(h->stream);
+      return h->fail(SW_ERR_STALLED,
+                     "level %d sweep stalled: tasks left unsolved after a %.1f s wait (dependency cycle; flags 0x%x)",
+                     level, h->p.timeout_ns * 1e-9, err);
+    }
     if (err & swk::kErrClamp)
       return h->fail(SW_ERR_INVALID_ARG, "x_HII floor above 1 - 1e-10 in the chemistry clamp (reference panics)");
   }
@@ -635,7 +721,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   SW_CUDA(h, cudaEventRecord(h->ev[4], h->stream), "event");
   h->sim_time += elapsed;
   SW_CUDA(h, swh::launch_ionization_time(h->p, h->sim_time, h->stream), "ionization time kernel");
-  launches += 4;
+  launches += 3;
   SW_CUDA(h, cudaEventRecord(h->ev[1], h->stream), "event");
   sw_status st = sync_ctl(h);
   if (st != SW_OK) return st;
@@ -648,7 +734,6 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   uint64_t solved = h->ctl_host.tasks - tasks_before;
   h->stats.steps += 1;
   h->stats.tasks = (int64_t)h->ctl_host.tasks;
-  h->stats.visits = (int64_t)h->ctl_host.visits;
   h->stats.chem_cells = (int64_t)h->ctl_host.chem_cells;
   h->stats.chem_attempts = (int64_t)h->ctl_host.chem_attempts;
   h->stats.chem_failures = (int64_t)h->ctl_host.chem_failures;
@@ -715,7 +800,10 @@ sw_status sw_get_dependency_counts(sw_handle* h, int32_t level, uint8_t* counts)
   SW_CUDA(h, cudaMalloc(&d_counts, nb), "alloc");
   cudaMemsetAsync(d_counts, 0, nb, h->stream);
   cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream);
-  cudaError_t e = h->ops->init_counts(h->p, level, d_counts, h->stream);
+  cudaError_t e = h->ops->init_counts(h->p, level, d_counts, true, h->stream);
+  // the counting kernel enqueued the tasks without dependencies: clear those slots
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->p.queue, 0xff, (size_t)h->Np * h->D * sizeof(uint32_t), h->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_counts, nb, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   cudaFree(d_counts);
@@ -744,6 +832,7 @@ sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double*
 
 sw_status sw_get_stats(sw_handle* h, sw_stats* out) {
   if (!h || !out) return SW_ERR_INVALID_ARG;
+  h->stats.schedule_levels = h->stats_schedule_levels;
   *out = h->stats;
   return SW_OK;
 }

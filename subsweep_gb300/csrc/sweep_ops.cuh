@@ -14,85 +14,113 @@ constexpr bool kCarry = SWK_CARRY;
 
 swk::SweepArgs<R> sweep_args(const DevicePtrs& p, int level) {
   swk::SweepArgs<R> a;
-  a.row_ptr = p.row_ptr;
-  a.geo64 = static_cast<const swk::Geo64*>(p.geo64);
+  a.off = p.off;
   a.geo32 = static_cast<const float4*>(p.geo32);
+  a.geo64 = static_cast<const swk::Geo64*>(p.geo64);
   a.nbr = p.nbr;
-  a.size = p.size;
   a.dir64 = p.dir64;
   a.dir32 = p.dir32;
   a.D = p.D;
-  a.Dp = p.Dp;
-  a.words = p.words;
+  a.Np = p.Np;
+  a.N = (uint32_t)p.num_cells;
   a.guard = p.guard;
   a.level = p.level;
-  a.order = p.order;
-  a.source = p.source;
+  a.src_dir = static_cast<const R*>(p.src_dir);
   a.att = p.att;
-  a.rate_scale = p.rate_scale;
   a.threshold = (R)(p.threshold / p.rate_scale);
   a.incoming = static_cast<R*>(p.incoming);
   a.outgoing = static_cast<R*>(p.outgoing);
   a.periodic = static_cast<R*>(p.periodic);
   a.pending = static_cast<R*>(p.pending);
   a.counters = p.counters;
-  a.ready = p.ready;
-  a.queued = p.queued;
-  a.frontier0 = p.frontier0;
-  a.frontier1 = p.frontier1;
+  a.queue = p.queue;
   a.ctl = p.ctl;
   a.current_level = level;
   a.timeout_ns = p.timeout_ns;
-  a.max_rounds = p.max_rounds;
   return a;
 }
 
 int grid_for(int64_t work, int block) {
   int64_t g = (work + block - 1) / block;
   if (g < 1) g = 1;
-  if (g > 152 * 16) g = 152 * 16;
+  if (g > 152 * 32) g = 152 * 32;
   return (int)g;
 }
 
 cudaError_t occupancy(int* blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep<R>,
-                                                       swk::kWarpsPerBlock * 32, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep<R>, swk::kSweepThreads, 0);
 }
 
 cudaError_t attenuation(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::k_attenuation<kCarry><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
-      p.order, p.ctl, level, p.density, p.xhii, p.yneu, p.size, p.att);
+      (uint32_t)p.num_cells, p.level, level, p.density, p.xhii, p.yneu, p.size, p.att);
   return cudaGetLastError();
 }
 
-cudaError_t init_counts(const DevicePtrs& p, int level, uint8_t* debug_counts, cudaStream_t s) {
+cudaError_t init_counts(const DevicePtrs& p, int level, uint8_t* debug_counts, bool enqueue, cudaStream_t s) {
   swk::SweepArgs<R> a = sweep_args(p, level);
-  int blocks = grid_for(p.num_cells * 32, swk::kWarpsPerBlock * 32);
-  swk::k_init_counts<R><<<blocks, swk::kWarpsPerBlock * 32, 0, s>>>(a, debug_counts);
+  swk::DirParam dirs;
+  for (int i = 0; i < 3 * p.D; ++i) dirs.v[i] = p.dir32_host[i];
+  const unsigned long long capacity = enqueue ? (unsigned long long)p.D * p.Np : 0ull;
+  const int blocks = (int)((p.num_cells + swk::kCountThreads - 1) / swk::kCountThreads);
+  swk::k_init_counts<R><<<blocks, swk::kCountThreads, 0, s>>>(a, dirs, capacity, debug_counts);
   return cudaGetLastError();
 }
 
 cudaError_t sweep(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::SweepArgs<R> a = sweep_args(p, level);
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)swk::k_sweep<R>, dim3(p.coop_blocks),
-                                     dim3(swk::kWarpsPerBlock * 32), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)swk::k_sweep<R>, dim3(p.coop_blocks), dim3(swk::kSweepThreads),
+                                     args, 0, s);
+}
+
+cudaError_t occupancy_levels(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep_sched<R>, swk::kLevelThreads, 0);
+}
+
+cudaError_t sweep_levels(const DevicePtrs& p, int level, cudaStream_t s) {
+  swk::SweepArgs<R> a = sweep_args(p, level);
+  const uint32_t* order = p.order;
+  uint32_t total = (uint32_t)(p.num_cells * p.D);
+  void* args[] = {&a, &order, &total};
+  return cudaLaunchCooperativeKernel((const void*)swk::k_sweep_sched<R>, dim3(p.level_blocks),
+                                     dim3(swk::kLevelThreads), args, 0, s);
+}
+
+// Seed of the schedule: dependency counts with every cell active (the caller has set
+// all levels >= 0), tasks without dependencies appended to `order`.
+cudaError_t schedule_seed(const DevicePtrs& p, cudaStream_t s) {
+  swk::SweepArgs<R> a = sweep_args(p, 0);
+  a.queue = p.order;
+  swk::DirParam dirs;
+  for (int i = 0; i < 3 * p.D; ++i) dirs.v[i] = p.dir32_host[i];
+  const unsigned long long capacity = (unsigned long long)p.D * p.Np;
+  const int blocks = (int)((p.num_cells + swk::kCountThreads - 1) / swk::kCountThreads);
+  swk::k_init_counts<R><<<blocks, swk::kCountThreads, 0, s>>>(a, dirs, capacity, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t kahn_round(const DevicePtrs& p, uint32_t begin, uint32_t end, cudaStream_t s) {
+  swk::SweepArgs<R> a = sweep_args(p, 0);
+  const unsigned long long capacity = (unsigned long long)p.D * p.Np;
+  swk::k_kahn_round<R><<<grid_for((int64_t)(end - begin), 256), 256, 0, s>>>(a, p.order, begin, end, capacity);
+  return cudaGetLastError();
 }
 
 cudaError_t fold_periodic(const DevicePtrs& p, cudaStream_t s) {
   if (p.n_periodic_cells == 0) return cudaSuccess;
-  swk::k_fold_periodic<R><<<grid_for((int64_t)p.n_periodic_cells * p.Dp, 256), 256, 0, s>>>(
-      static_cast<R*>(p.periodic), static_cast<R*>(p.pending), p.periodic_cells, p.n_periodic_cells, p.Dp);
+  swk::k_fold_periodic<R><<<grid_for((int64_t)p.n_periodic_cells * p.D, 256), 256, 0, s>>>(
+      static_cast<R*>(p.periodic), static_cast<R*>(p.pending), p.periodic_cells, p.n_periodic_cells, p.D, p.Np);
   return cudaGetLastError();
 }
 
 cudaError_t chemistry(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::ChemArgs<R> a;
-  a.order = p.order;
+  a.n = (uint32_t)p.num_cells;
   a.ctl = p.ctl;
   a.current_level = level;
   a.D = p.D;
-  a.Dp = p.Dp;
+  a.Np = p.Np;
   a.incoming = static_cast<const R*>(p.incoming);
   a.periodic = static_cast<const R*>(p.periodic);
   a.rate_scale = p.rate_scale;
@@ -118,21 +146,22 @@ cudaError_t chemistry(const DevicePtrs& p, int level, cudaStream_t s) {
 
 cudaError_t photon_rate(const DevicePtrs& p, double* out, cudaStream_t s) {
   swk::k_photon_rate<R><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
-      (uint32_t)p.num_cells, static_cast<const R*>(p.incoming), p.D, p.Dp, p.rate_scale, out);
+      (uint32_t)p.num_cells, static_cast<const R*>(p.incoming), p.D, p.Np, p.rate_scale, out);
   return cudaGetLastError();
 }
 
 cudaError_t export_rates(const DevicePtrs& p, const void* src, double* out, cudaStream_t s) {
   swk::k_export_rates<R><<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(
-      (uint32_t)p.num_cells, static_cast<const R*>(src), p.D, p.Dp, p.rate_scale, out);
+      (uint32_t)p.num_cells, static_cast<const R*>(src), p.D, p.Np, p.rate_scale, out);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 extern const PrecisionOps SWK_OPS = {
-    SWK_NAME,    (int)sizeof(R), occupancy,  attenuation,  init_counts,
-    sweep,       fold_periodic,  chemistry,  photon_rate,  export_rates,
+    SWK_NAME,         (int)sizeof(R), occupancy,  attenuation,   init_counts,   sweep,
+    occupancy_levels, sweep_levels,   kahn_round, schedule_seed, fold_periodic, chemistry,
+    photon_rate,      export_rates,
 };
 
 }  // namespace swh

@@ -75,11 +75,17 @@ def test_c1_small_fp64_parity():
     run_and_compare(w, steps=4)
 
 
-def test_c2_small_lognormal_levels_fp64_parity():
+@pytest.mark.parametrize("transport", ["levels", "queue"])
+def test_c2_small_lognormal_levels_fp64_parity(transport, monkeypatch):
+    """Both transport kernels: the levelled schedule and the dependency-driven queue."""
+    monkeypatch.setenv("SUBSWEEP_TRANSPORT", transport)
     w = workloads.c2_lognormal(n_per_side=12, num_directions=84, num_levels=4, nthreads=2)
     gpu, orc = run_and_compare(w, steps=6)
     # the level hierarchy must actually be exercised
     assert len(np.unique(orc.fields()["level"])) > 1
+    st = gpu.stats()
+    assert (st["levelled_sweeps"] > 0) == (transport == "levels")
+    assert st["schedule_levels"] > 0
 
 
 def test_cartesian_column_analytic():
@@ -128,20 +134,23 @@ def test_poisson_periodic_fp64_parity():
 
 def test_dependency_cycle_reports_stalled_not_hang():
     """A cyclic dependency graph (which deadlocks the reference) ends the GPU sweep with
-    SW_ERR_STALLED: the frontier empties with tasks left."""
+    SW_ERR_STALLED after the bounded wait for the never-filled queue slots."""
     from tests.test_abi import _cyclic_grid
     g = _cyclic_grid()
     n = g.num_cells
     p = SweepParameters(directions=[[0.0, 0.0, 1.0]], num_timestep_levels=1, periodic=False, max_timestep=1.0)
     s = Sweep(p, g, density=np.full(n, 1e-24), ionized_hydrogen_fraction=np.full(n, 1e-10),
               temperature=np.full(n, 1e4), source=np.zeros(n))
+    assert s.stats()["schedule_levels"] == 0  # no levelled schedule for a cyclic graph
     with pytest.raises(SweepError) as e:
         s.run_sweeps()
     assert e.value.status == _native.SW_ERR_STALLED
     s.close()
 
 
-def test_mixed_precision_error_bounds():
+@pytest.mark.parametrize("transport", ["levels", "queue"])
+def test_mixed_precision_error_bounds(transport, monkeypatch):
+    monkeypatch.setenv("SUBSWEEP_TRANSPORT", transport)
     w = workloads.c2_lognormal(n_per_side=12, num_directions=84, num_levels=4, nthreads=2)
     gpu, orc = make_pair(w, precision="mixed")
     for _ in range(6):
