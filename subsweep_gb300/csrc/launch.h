@@ -30,6 +30,7 @@ struct DevicePtrs {
   const uint32_t* off;
   const void* geo64;  // {nx, ny, nz, area} x E doubles, 32-byte aligned
   const void* geo32;  // float4[E], area scaled by a power of two
+  const void* geo16;  // uint4[E] {area*n (scaled) x3, nbr | kind << 30} (pull path)
   const uint32_t* nbr;
   const double* size;
   const double* volume;
@@ -55,6 +56,8 @@ struct DevicePtrs {
   void* pending;
   uint32_t* counters;
   uint32_t* queue;
+  unsigned long long* qe;    // pull path: {q, sweep number} per task
+  uint32_t epoch;            // pull path: number of the current level sweep
   uint32_t* order;           // levelled schedule: task ids grouped by Kahn level
   const uint32_t* lvl;       // level offsets into order [num_sched_levels + 1]
   uint32_t num_sched_levels; // 0: no levelled schedule (cyclic graph)
@@ -69,6 +72,7 @@ struct DevicePtrs {
 struct PrecisionOps {
   const char* name;
   int rate_bytes;
+  bool pull;  // pull-form transport (mixed path): no counters, no queue
   // blocks of the persistent sweep kernel that are co-resident on this device
   cudaError_t (*occupancy)(int* blocks_per_sm);
   cudaError_t (*attenuation)(const DevicePtrs&, int level, cudaStream_t);
@@ -76,12 +80,15 @@ struct PrecisionOps {
   cudaError_t (*sweep)(const DevicePtrs&, int level, cudaStream_t);
   cudaError_t (*occupancy_levels)(int* blocks_per_sm);
   cudaError_t (*sweep_levels)(const DevicePtrs&, int level, cudaStream_t);
-  cudaError_t (*kahn_round)(const DevicePtrs&, uint32_t begin, uint32_t end, cudaStream_t);
+  cudaError_t (*kahn_round)(const DevicePtrs&, uint32_t begin, uint32_t end, uint16_t* task_level, uint32_t round,
+                            cudaStream_t);
   cudaError_t (*schedule_seed)(const DevicePtrs&, cudaStream_t);
   cudaError_t (*fold_periodic)(const DevicePtrs&, cudaStream_t);
   cudaError_t (*chemistry)(const DevicePtrs&, int level, cudaStream_t);
-  cudaError_t (*photon_rate)(const DevicePtrs&, double* out, cudaStream_t);
-  cudaError_t (*export_rates)(const DevicePtrs&, const void* src, double* out, cudaStream_t);
+  // which: 0 incoming, 1 outgoing, 2 periodic; last_epoch: sweep number of the step's
+  // last sweep (pull path)
+  cudaError_t (*photon_rate)(const DevicePtrs&, uint32_t last_epoch, double* out, cudaStream_t);
+  cudaError_t (*export_rates)(const DevicePtrs&, int which, uint32_t last_epoch, double* out, cudaStream_t);
 };
 
 extern const PrecisionOps kOpsFP64;
@@ -91,5 +98,6 @@ extern const PrecisionOps kOpsMixed;
 cudaError_t launch_update_levels(const DevicePtrs&, int lowest_allowed, cudaStream_t);
 cudaError_t launch_level_hist(const DevicePtrs&, cudaStream_t);
 cudaError_t launch_ionization_time(const DevicePtrs&, double time, cudaStream_t);
+cudaError_t launch_schedule_scatter(const DevicePtrs&, const uint16_t* task_level, uint32_t* cursor, cudaStream_t);
 
 }  // namespace swh

@@ -367,10 +367,11 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepArgs<R> a) {
 // ---------------------------------------------------------------------------
 
 // One Kahn round: release the downwind dependents of the tasks order[begin, end)
-// (all cells active), appending the tasks that become free at ctl->tail.
+// (all cells active), appending the tasks that become free at ctl->tail and recording
+// their level (round + 1) in task_level.
 template <typename R>
 __global__ void k_kahn_round(SweepArgs<R> a, uint32_t* order, uint32_t begin, uint32_t end,
-                             unsigned long long capacity) {
+                             unsigned long long capacity, uint16_t* task_level, uint32_t round) {
   const uint32_t nthreads = gridDim.x * blockDim.x;
   const uint32_t span = end - begin;
   const uint32_t iters = (span + nthreads - 1) / nthreads;
@@ -405,11 +406,26 @@ __global__ void k_kahn_round(SweepArgs<R> a, uint32_t* order, uint32_t begin, ui
             const uint32_t shift = 8u * (tn & 3u);
             const uint32_t old = atomicSub(a.counters + (tn >> 2), 1u << shift);
             ready = ((old >> shift) & 0xffu) == 1u;
+            if (ready) task_level[tn] = (uint16_t)(round + 1);
           }
         }
       }
       enqueue(ready, tn, a.ctl, order, capacity);
     }
+  }
+}
+
+// Counting sort of the schedule by level: tasks are visited in increasing task id
+// (direction-major, cells along the space-filling curve) and appended to their level's
+// segment, so each level lists one direction's cells after another in nearly
+// increasing order and consecutive groups touch neighbouring 32-byte sectors.
+static __global__ void k_schedule_scatter(uint32_t n_tasks_padded, uint32_t N, uint32_t Np,
+                                          const uint16_t* task_level, uint32_t* cursor, uint32_t* order) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tasks_padded; t += gridDim.x * blockDim.x) {
+    const uint32_t c = t % Np;
+    if (c >= N) continue;
+    const uint32_t slot = atomicAdd(cursor + task_level[t], 1u);
+    order[slot] = t;
   }
 }
 

@@ -4,6 +4,7 @@
 #define SWK_CARRY false
 #define SWK_OPS kOpsFP64
 #define SWK_NAME "fp64"
+#define SWK_PULL 0
 #include "sweep_ops.cuh"
 
 namespace swh {
@@ -30,6 +31,14 @@ cudaError_t launch_level_hist(const DevicePtrs& p, cudaStream_t s) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   swk::k_level_counts<<<1, 32, 0, s>>>(p.ctl, p.num_levels);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_schedule_scatter(const DevicePtrs& p, const uint16_t* task_level, uint32_t* cursor,
+                                    cudaStream_t s) {
+  const uint32_t total = (uint32_t)((uint64_t)p.Np * p.D);
+  swk::k_schedule_scatter<<<grid_for_cells(total), 256, 0, s>>>(total, (uint32_t)p.num_cells, p.Np, task_level,
+                                                                cursor, p.order);
   return cudaGetLastError();
 }
 

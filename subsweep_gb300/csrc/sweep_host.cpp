@@ -90,6 +90,7 @@ struct sw_handle {
   double* scratch = nullptr;  // N doubles for field export
   uint32_t stats_schedule_levels = 0;
   int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
+  uint32_t last_epoch = 0;  // pull path: sweep number of the last sweep of the last step
 
   ~sw_handle() {
     for (void* a : allocations) cudaFree(a);
@@ -244,16 +245,28 @@ sw_status build_schedule(sw_handle* h) {
   swh::DevicePtrs& p = h->p;
   const uint64_t total = (uint64_t)h->N * (uint64_t)h->D;
   SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
+  struct DeviceScratch {
+    void* ptr = nullptr;
+    ~DeviceScratch() {
+      if (ptr) cudaFree(ptr);
+    }
+  } level_scratch, cursor_scratch;
+  SW_CUDA(h, cudaMalloc(&level_scratch.ptr, (size_t)h->Np * h->D * sizeof(uint16_t)), "schedule scratch");
+  uint16_t* task_level = static_cast<uint16_t*>(level_scratch.ptr);
+  SW_CUDA(h, cudaMemsetAsync(task_level, 0, (size_t)h->Np * h->D * sizeof(uint16_t), h->stream), "schedule scratch");
   SW_CUDA(h, h->ops->schedule_seed(p, h->stream), "schedule seed kernel");
   std::vector<uint32_t> lvl = {0};
   unsigned long long tail = 0;
   SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
   SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule seed");
   uint32_t begin = 0;
+  uint32_t round = 0;
   while (tail > begin) {
     const uint32_t end = (uint32_t)tail;
     lvl.push_back(end);
-    SW_CUDA(h, h->ops->kahn_round(p, begin, end, h->stream), "schedule round kernel");
+    if (round + 1 >= 0xffffu) return h->fail(SW_ERR_UNSUPPORTED, "dependency graph deeper than 65534 levels");
+    SW_CUDA(h, h->ops->kahn_round(p, begin, end, task_level, round, h->stream), "schedule round kernel");
+    ++round;
     SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
     SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule round");
     begin = end;
@@ -261,12 +274,29 @@ sw_status build_schedule(sw_handle* h) {
   uint32_t err = 0;
   SW_CUDA(h, cudaMemcpy(&err, &p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
   if (tail != total || err != 0) {
-    p.num_sched_levels = 0;  // cyclic dependency graph
+    // cyclic dependency graph: no schedule.  The push path falls back to the
+    // dependency-driven queue; the pull path visits tasks in id order and its waits run
+    // out, so either reports the stall at the first sweep, where the reference deadlocks.
+    p.num_sched_levels = 0;
+    if (h->ops->pull) {
+      std::vector<uint32_t> ids;
+      ids.reserve(total);
+      for (uint32_t d = 0; d < (uint32_t)h->D; ++d)
+        for (uint32_t c = 0; c < (uint32_t)h->N; ++c) ids.push_back(d * h->Np + c);
+      SW_CUDA(h, cudaMemcpy(p.order, ids.data(), ids.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "order");
+    }
+    SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
     return SW_OK;
   }
   uint32_t* d_lvl;
   if (!h->alloc(&d_lvl, lvl.size())) return h->fail(SW_ERR_OOM, "device allocation of the schedule failed");
   SW_CUDA(h, cudaMemcpy(d_lvl, lvl.data(), lvl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload schedule");
+  // rewrite each level's segment in task-id order (counting sort by level)
+  SW_CUDA(h, cudaMalloc(&cursor_scratch.ptr, lvl.size() * sizeof(uint32_t)), "schedule scratch");
+  uint32_t* cursor = static_cast<uint32_t*>(cursor_scratch.ptr);
+  SW_CUDA(h, cudaMemcpy(cursor, lvl.data(), lvl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "schedule");
+  SW_CUDA(h, swh::launch_schedule_scatter(p, task_level, cursor, h->stream), "schedule scatter kernel");
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule scatter");
   p.lvl = d_lvl;
   p.num_sched_levels = (uint32_t)(lvl.size() - 1);
   h->stats_schedule_levels = p.num_sched_levels;
@@ -489,6 +519,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   {
     std::vector<double> geo64(4 * (size_t)E);
     std::vector<float> geo32(4 * (size_t)E);
+    std::vector<uint32_t> geo16(h->ops->pull ? 4 * (size_t)E : 0);
     std::vector<uint32_t> nbr(E);
     std::vector<uint32_t> row(N + 1);
     for (int64_t i = 0; i <= N; ++i) row[i] = (uint32_t)grid->row_ptr[i];
@@ -502,6 +533,14 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
       uint32_t kind = grid->kind[f];
       uint32_t nb = (kind == SW_FACE_BOUNDARY) ? 0u : (uint32_t)grid->nbr[f];
       nbr[f] = nb | (kind << swk::kKindShift);
+      if (h->ops->pull) {  // {area * n in the scaled FP32 area unit, neighbour | kind}
+        const double a = std::ldexp(grid->area[f], -area_exp);
+        for (int c3 = 0; c3 < 3; ++c3) {
+          const float v = (float)(a * grid->normal[3 * f + c3]);
+          std::memcpy(&geo16[4 * f + c3], &v, sizeof(float));
+        }
+        geo16[4 * f + 3] = nbr[f];
+      }
     }
     uint32_t* d_row;
     double* d_geo64;
@@ -516,6 +555,15 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     cudaMemcpy(d_geo64, geo64.data(), geo64.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(d_geo32, geo32.data(), geo32.size() * sizeof(float), cudaMemcpyHostToDevice);
     cudaMemcpy(d_nbr, nbr.data(), E * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (h->ops->pull) {
+      uint32_t* d_geo16;
+      if (!h->alloc(&d_geo16, geo16.size())) {
+        h->fail(SW_ERR_OOM, "device allocation of the grid failed");
+        return bail(SW_ERR_OOM);
+      }
+      cudaMemcpy(d_geo16, geo16.data(), geo16.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+      p.geo16 = d_geo16;
+    }
     p.off = d_row;
     p.geo64 = d_geo64;
     p.geo32 = d_geo32;
@@ -609,23 +657,34 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   {
     const size_t nd = (size_t)Np * D;
     const size_t rb = (size_t)h->ops->rate_bytes;
-    char *inc, *outg, *per, *pend;
-    uint32_t *cnt, *queue, *order;
-    swk::SweepCtl* ctl;
-    bool ok = h->alloc(&inc, nd * rb) && h->alloc(&outg, nd * rb) && h->alloc(&per, nd * rb) &&
-              h->alloc(&pend, nd * rb) && h->alloc(&cnt, nd / 4) && h->alloc(&queue, nd) &&
+    // push path (FP64): incoming, outgoing, periodic, pending rates and the ready queue;
+    // pull path (mixed): incoming and periodic rates and the {q, sweep} words.
+    const bool pull = h->ops->pull;
+    char *inc = nullptr, *outg = nullptr, *per = nullptr, *pend = nullptr;
+    uint32_t *cnt = nullptr, *queue = nullptr, *order = nullptr;
+    unsigned long long* qe = nullptr;
+    swk::SweepCtl* ctl = nullptr;
+    bool ok = h->alloc(&inc, nd * rb) && h->alloc(&per, nd * rb) && h->alloc(&cnt, nd / 4) &&
               h->alloc(&order, nd) && h->alloc(&ctl, 1);
+    if (ok && pull) ok = h->alloc(&qe, nd);
+    if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
-      h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed", (4 * rb + 5) * nd >> 20);
+      h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
+              (pull ? 2 * rb + 13 : 4 * rb + 9) * nd >> 20);
       return bail(SW_ERR_OOM);
     }
     cudaMemset(inc, 0, nd * rb);
-    cudaMemset(outg, 0, nd * rb);
     cudaMemset(per, 0, nd * rb);
-    cudaMemset(pend, 0, nd * rb);
     cudaMemset(cnt, 0, nd);
-    cudaMemset(queue, 0xff, nd * sizeof(uint32_t));  // every slot empty
+    if (pull) {
+      cudaMemset(qe, 0, nd * sizeof(unsigned long long));
+    } else {
+      cudaMemset(outg, 0, nd * rb);
+      cudaMemset(pend, 0, nd * rb);
+      cudaMemset(queue, 0xff, nd * sizeof(uint32_t));  // every slot empty
+    }
     cudaMemset(ctl, 0, sizeof(swk::SweepCtl));
+    p.qe = qe;
     p.incoming = inc;
     p.outgoing = outg;
     p.periodic = per;
@@ -675,8 +734,14 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     bool levelled = h->p.num_sched_levels > 0 && (uint64_t)h->n_ge_host[level] * 16 >= (uint64_t)h->N;
     if (h->force_path == 1) levelled = h->p.num_sched_levels > 0;
     if (h->force_path == 2) levelled = false;
-    SW_CUDA(h, ops.init_counts(h->p, level, nullptr, !levelled, h->stream), "init_counts kernel");
-    launches += 1;
+    if (ops.pull) {
+      levelled = true;  // the pull path always walks the schedule (or the id order)
+      h->p.epoch += 1;
+      h->last_epoch = h->p.epoch;
+    } else {
+      SW_CUDA(h, ops.init_counts(h->p, level, nullptr, !levelled, h->stream), "init_counts kernel");
+      launches += 1;
+    }
     SW_CUDA(h, cudaEventRecord(h->ev[6], h->stream), "event");
     if (levelled) {
       SW_CUDA(h, ops.sweep_levels(h->p, level, h->stream), "levelled sweep kernel");
@@ -704,7 +769,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     h->stats.level_sweeps += 1;
     if (err & (swk::kErrStall | swk::kErrQueue)) {
       // leave the queue empty so the handle stays usable for inspection
-      cudaMemsetAsync(h->p.queue, 0xff, (size_t)h->Np * h->D * sizeof(uint32_t), h->stream);
+      if (h->p.queue) cudaMemsetAsync(h->p.queue, 0xff, (size_t)h->Np * h->D * sizeof(uint32_t), h->stream);
       cudaStreamSynchronize(h->stream);
       return h->fail(SW_ERR_STALLED,
                      "level %d sweep stalled: tasks left unsolved after a %.1f s wait (dependency cycle; flags 0x%x)",
@@ -755,7 +820,7 @@ sw_status sw_get_fields(sw_handle* h, double* x, double* T, double* dt, double* 
   if (T) SW_CUDA(h, cudaMemcpyAsync(T, h->p.temperature, nb, cudaMemcpyDeviceToHost, h->stream), "copy T");
   if (dt) SW_CUDA(h, cudaMemcpyAsync(dt, h->p.species_timestep, nb, cudaMemcpyDeviceToHost, h->stream), "copy dt");
   if (rate) {
-    SW_CUDA(h, h->ops->photon_rate(h->p, h->scratch, h->stream), "photon rate kernel");
+    SW_CUDA(h, h->ops->photon_rate(h->p, h->last_epoch, h->scratch, h->stream), "photon rate kernel");
     SW_CUDA(h, cudaMemcpyAsync(rate, h->scratch, nb, cudaMemcpyDeviceToHost, h->stream), "copy rate");
   }
   SW_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
@@ -800,10 +865,7 @@ sw_status sw_get_dependency_counts(sw_handle* h, int32_t level, uint8_t* counts)
   SW_CUDA(h, cudaMalloc(&d_counts, nb), "alloc");
   cudaMemsetAsync(d_counts, 0, nb, h->stream);
   cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream);
-  cudaError_t e = h->ops->init_counts(h->p, level, d_counts, true, h->stream);
-  // the counting kernel enqueued the tasks without dependencies: clear those slots
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(h->p.queue, 0xff, (size_t)h->Np * h->D * sizeof(uint32_t), h->stream);
+  cudaError_t e = h->ops->init_counts(h->p, level, d_counts, false, h->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_counts, nb, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   cudaFree(d_counts);
@@ -816,12 +878,11 @@ sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double*
   size_t nb = (size_t)h->N * h->D * sizeof(double);
   double* d_out = nullptr;
   SW_CUDA(h, cudaMalloc(&d_out, nb), "alloc");
-  const void* srcs[3] = {h->p.incoming, h->p.outgoing, h->p.periodic};
   double* dsts[3] = {incoming, outgoing, periodic};
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
     if (!dsts[i]) continue;
-    e = h->ops->export_rates(h->p, srcs[i], d_out, h->stream);
+    e = h->ops->export_rates(h->p, i, h->last_epoch, d_out, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dsts[i], d_out, nb, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   }

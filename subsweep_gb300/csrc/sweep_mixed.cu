@@ -5,4 +5,5 @@
 #define SWK_CARRY true
 #define SWK_OPS kOpsMixed
 #define SWK_NAME "mixed"
+#define SWK_PULL 1
 #include "sweep_ops.cuh"

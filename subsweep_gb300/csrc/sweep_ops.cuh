@@ -5,6 +5,9 @@
 
 #include "launch.h"
 #include "sweep_device.cuh"
+#if SWK_PULL
+#include "sweep_pull.cuh"
+#endif
 
 namespace swh {
 namespace {
@@ -100,10 +103,12 @@ cudaError_t schedule_seed(const DevicePtrs& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t kahn_round(const DevicePtrs& p, uint32_t begin, uint32_t end, cudaStream_t s) {
+cudaError_t kahn_round(const DevicePtrs& p, uint32_t begin, uint32_t end, uint16_t* task_level, uint32_t round,
+                       cudaStream_t s) {
   swk::SweepArgs<R> a = sweep_args(p, 0);
   const unsigned long long capacity = (unsigned long long)p.D * p.Np;
-  swk::k_kahn_round<R><<<grid_for((int64_t)(end - begin), 256), 256, 0, s>>>(a, p.order, begin, end, capacity);
+  swk::k_kahn_round<R><<<grid_for((int64_t)(end - begin), 256), 256, 0, s>>>(a, p.order, begin, end, capacity,
+                                                                              task_level, round);
   return cudaGetLastError();
 }
 
@@ -144,24 +149,92 @@ cudaError_t chemistry(const DevicePtrs& p, int level, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t photon_rate(const DevicePtrs& p, double* out, cudaStream_t s) {
+#if SWK_PULL
+swk::PullArgs pull_args(const DevicePtrs& p, int level) {
+  swk::PullArgs a;
+  a.off = p.off;
+  a.geo16 = static_cast<const uint4*>(p.geo16);
+  a.geo64 = static_cast<const swk::Geo64*>(p.geo64);
+  a.dir64 = p.dir64;
+  a.dir32 = p.dir32;
+  a.D = p.D;
+  a.Np = p.Np;
+  a.N = (uint32_t)p.num_cells;
+  a.level = p.level;
+  a.src_dir = static_cast<const float*>(p.src_dir);
+  a.att = p.att;
+  a.threshold = (float)(p.threshold / p.rate_scale);
+  a.incoming = static_cast<float*>(p.incoming);
+  a.periodic = static_cast<const float*>(p.periodic);
+  a.qe = p.qe;
+  a.ctl = p.ctl;
+  a.current_level = level;
+  a.epoch = p.epoch;
+  a.timeout_ns = p.timeout_ns;
+  return a;
+}
+
+cudaError_t occupancy_pull(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep_pull, swk::kPullThreads, 0);
+}
+
+cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
+  swk::PullArgs a = pull_args(p, level);
+  const uint32_t* order = p.order;
+  uint32_t total = (uint32_t)(p.num_cells * p.D);
+  void* args[] = {&a, &order, &total};
+  return cudaLaunchCooperativeKernel((const void*)swk::k_sweep_pull, dim3(p.level_blocks), dim3(swk::kPullThreads),
+                                     args, 0, s);
+}
+
+cudaError_t fold_pull(const DevicePtrs& p, cudaStream_t s) {
+  if (p.n_periodic_cells == 0) return cudaSuccess;
+  swk::PullArgs a = pull_args(p, 0);
+  swk::k_fold_pull<<<grid_for((int64_t)p.n_periodic_cells * p.D, 256), 256, 0, s>>>(
+      a, static_cast<float*>(p.periodic), p.periodic_cells, p.n_periodic_cells);
+  return cudaGetLastError();
+}
+
+cudaError_t photon_rate(const DevicePtrs& p, uint32_t last_epoch, double* out, cudaStream_t s) {
+  swk::PullArgs a = pull_args(p, 0);
+  swk::k_photon_rate_pull<<<grid_for(p.num_cells, 128), 128, 0, s>>>(a, last_epoch, p.rate_scale, out);
+  return cudaGetLastError();
+}
+
+cudaError_t export_rates(const DevicePtrs& p, int which, uint32_t last_epoch, double* out, cudaStream_t s) {
+  swk::PullArgs a = pull_args(p, 0);
+  swk::k_export_pull<<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(a, last_epoch, which, p.rate_scale, out);
+  return cudaGetLastError();
+}
+#else
+cudaError_t photon_rate(const DevicePtrs& p, uint32_t, double* out, cudaStream_t s) {
   swk::k_photon_rate<R><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
       (uint32_t)p.num_cells, static_cast<const R*>(p.incoming), p.D, p.Np, p.rate_scale, out);
   return cudaGetLastError();
 }
 
-cudaError_t export_rates(const DevicePtrs& p, const void* src, double* out, cudaStream_t s) {
+cudaError_t export_rates(const DevicePtrs& p, int which, uint32_t, double* out, cudaStream_t s) {
+  const void* src = which == 0 ? p.incoming : (which == 1 ? p.outgoing : p.periodic);
   swk::k_export_rates<R><<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(
       (uint32_t)p.num_cells, static_cast<const R*>(src), p.D, p.Np, p.rate_scale, out);
   return cudaGetLastError();
 }
+#endif
 
 }  // namespace
 
+#if SWK_PULL
 extern const PrecisionOps SWK_OPS = {
-    SWK_NAME,         (int)sizeof(R), occupancy,  attenuation,   init_counts,   sweep,
-    occupancy_levels, sweep_levels,   kahn_round, schedule_seed, fold_periodic, chemistry,
-    photon_rate,      export_rates,
+    SWK_NAME,       (int)sizeof(R), true,       occupancy,     attenuation, init_counts, sweep,
+    occupancy_pull, sweep_pull,     kahn_round, schedule_seed, fold_pull,   chemistry,   photon_rate,
+    export_rates,
 };
+#else
+extern const PrecisionOps SWK_OPS = {
+    SWK_NAME,         (int)sizeof(R), false,      occupancy,     attenuation,   init_counts, sweep,
+    occupancy_levels, sweep_levels,   kahn_round, schedule_seed, fold_periodic, chemistry,   photon_rate,
+    export_rates,
+};
+#endif
 
 }  // namespace swh

@@ -148,9 +148,8 @@ def test_dependency_cycle_reports_stalled_not_hang():
     s.close()
 
 
-@pytest.mark.parametrize("transport", ["levels", "queue"])
-def test_mixed_precision_error_bounds(transport, monkeypatch):
-    monkeypatch.setenv("SUBSWEEP_TRANSPORT", transport)
+def test_mixed_precision_error_bounds():
+    """Pull-form FP32 transport + FP64 chemistry against the FP64 oracle."""
     w = workloads.c2_lognormal(n_per_side=12, num_directions=84, num_levels=4, nthreads=2)
     gpu, orc = make_pair(w, precision="mixed")
     for _ in range(6):
@@ -160,3 +159,35 @@ def test_mixed_precision_error_bounds(transport, monkeypatch):
     dt = (np.abs(fg["temperature"] - fo["temperature"]) / fo["temperature"]).max()
     assert dx <= 1e-4, dx
     assert dt <= 1e-4, dt
+
+
+def test_mixed_precision_c1_rates_and_periodic():
+    """Pull-form rates (incoming, outgoing, periodic, PhotonRate) against the oracle's
+    push-form ones on a periodic box with an ionization front, within FP32 accuracy."""
+    w = workloads.c1_small_periodic(n_per_side=10, num_directions=84, nthreads=2)
+    gpu, orc = make_pair(w, precision="mixed")
+    for _ in range(3):
+        assert gpu.run_sweeps() == orc.run_sweeps()
+    fg, fo = gpu.fields(), orc.fields()
+    assert np.abs(fg["ionized_hydrogen_fraction"] - fo["ionized_hydrogen_fraction"]).max() <= 1e-4
+    assert (np.abs(fg["temperature"] - fo["temperature"]) / fo["temperature"]).max() <= 1e-4
+    # FP32 rates are stored in units of 2^-96 of the total source, so exponential-tail
+    # rates below ~1e-20 of the total luminosity are not represented (flushed to zero)
+    floor = 1e-20 * w.source.sum()
+    np.testing.assert_allclose(fg["photon_rate"], fo["photon_rate"], rtol=1e-4, atol=floor)
+    rg, ro = gpu.rates(), orc.rates()
+    for k in ("incoming", "outgoing", "periodic"):
+        np.testing.assert_allclose(rg[k], ro[k], rtol=1e-4, atol=floor, err_msg=k)
+
+
+def test_mixed_precision_cycle_reports_stalled():
+    from tests.test_abi import _cyclic_grid
+    g = _cyclic_grid()
+    n = g.num_cells
+    p = SweepParameters(directions=[[0.0, 0.0, 1.0]], num_timestep_levels=1, periodic=False, max_timestep=1.0)
+    s = Sweep(p, g, density=np.full(n, 1e-24), ionized_hydrogen_fraction=np.full(n, 1e-10),
+              temperature=np.full(n, 1e4), source=np.zeros(n), precision="mixed")
+    with pytest.raises(SweepError) as e:
+        s.run_sweeps()
+    assert e.value.status == _native.SW_ERR_STALLED
+    s.close()
