@@ -160,6 +160,16 @@ sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double*
 
 sw_status sw_get_stats(sw_handle* h, sw_stats* out);
 
+/* Same result as sw_get_dependency_counts, for callers that cannot allocate device
+ * memory (a host engine whose GPU memory is owned by its own pool, code that must not
+ * trigger the synchronisation cudaMalloc/cudaFree can cause): it stages the counts in
+ * a fixed 16 MiB __device__ array of the library instead of a cudaMalloc'd buffer and
+ * allocates nothing.  num_cells * directions must not exceed 16 MiB (SW_ERR_INVALID_ARG
+ * otherwise).  The first call on a device looks up the array's device address; make it
+ * before any stream capture.  Calls share the array, so calls that overlap on the GPU
+ * race.  This entry point has no counterpart in the reference. */
+sw_status sw_get_dependency_counts_noalloc(sw_handle* h, int32_t level, uint8_t* counts);
+
 /* Message of the last error on this handle ("" if none); with h == NULL, the last
  * error of sw_create on this thread. */
 const char* sw_last_error(const sw_handle* h);

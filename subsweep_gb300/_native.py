@@ -32,7 +32,7 @@ SW_FACE_BOUNDARY = 2
 ABI_SYMBOLS = (
     "sw_default_params", "sw_directions_from_num", "sw_create", "sw_step", "sw_get_fields",
     "sw_get_cell_state", "sw_set_fields", "sw_get_level_counts", "sw_get_dependency_counts",
-    "sw_get_rates", "sw_get_stats", "sw_last_error", "sw_destroy",
+    "sw_get_rates", "sw_get_stats", "sw_last_error", "sw_destroy", "sw_get_dependency_counts_noalloc",
 )
 
 
@@ -128,6 +128,7 @@ def load_gpu() -> ctypes.CDLL:
     lib.sw_get_level_counts.argtypes = [c_void_p, c_void_p]
     lib.sw_get_dependency_counts.argtypes = [c_void_p, c_int32, c_void_p]
     lib.sw_get_rates.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
+    lib.sw_get_dependency_counts_noalloc.argtypes = [c_void_p, c_int32, c_void_p]
     lib.sw_get_stats.argtypes = [c_void_p, ctypes.POINTER(SwStats)]
     lib.sw_last_error.argtypes = [c_void_p]
     lib.sw_last_error.restype = ctypes.c_char_p

@@ -66,6 +66,7 @@ def build(verbose: bool = False) -> dict:
         (CSRC / "sweep_fp64.cu", False),
         (CSRC / "sweep_mixed.cu", True),
         (CSRC / "sweep_host.cpp", True),
+        (CSRC / "sweep_noalloc.cu", True),
     ]
     with cf.ThreadPoolExecutor(max_workers=4) as ex:
         futs = [ex.submit(_nvcc_obj, src, fmad, verbose) for src, fmad in jobs]

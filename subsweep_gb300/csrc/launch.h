@@ -8,6 +8,8 @@
 
 #include <cstdint>
 
+#include "../../include/subsweep_gpu.h"
+
 namespace swk {
 struct SweepCtl;
 }
@@ -93,6 +95,21 @@ struct PrecisionOps {
 
 extern const PrecisionOps kOpsFP64;
 extern const PrecisionOps kOpsMixed;
+
+// Read access to a handle's device state for entry points defined outside the host
+// runtime's translation unit.
+struct HandleView {
+  DevicePtrs* p;
+  const PrecisionOps* ops;
+  cudaStream_t stream;
+  int device;
+  int64_t num_cells;
+  int num_directions;
+  int num_levels;
+};
+bool handle_view(sw_handle* h, HandleView* out);
+// Record an error message on the handle (returned by sw_last_error) and return `st`.
+sw_status handle_fail(sw_handle* h, sw_status st, const char* message);
 
 // Precision-independent kernels (compiled in sweep_fp64.cu).
 cudaError_t launch_update_levels(const DevicePtrs&, int lowest_allowed, cudaStream_t);

@@ -305,6 +305,28 @@ sw_status build_schedule(sw_handle* h) {
 
 }  // namespace
 
+
+namespace swh {
+
+bool handle_view(sw_handle* h, HandleView* out) {
+  if (!h || !out) return false;
+  out->p = &h->p;
+  out->ops = h->ops;
+  out->stream = h->stream;
+  out->device = h->device;
+  out->num_cells = h->N;
+  out->num_directions = h->D;
+  out->num_levels = h->L;
+  return true;
+}
+
+sw_status handle_fail(sw_handle* h, sw_status st, const char* message) {
+  if (h) h->last_error = message;
+  return st;
+}
+
+}  // namespace swh
+
 extern "C" {
 
 sw_status sw_default_params(sw_params* p) {
