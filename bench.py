@@ -269,7 +269,8 @@ def run_ours(args, dist: Dist):
 
     results = {}
     handles = {}
-    for precision in ("fp64", "mixed"):
+    precisions = ("fp64", "mixed") if args.precision == "both" else (args.precision,)
+    for precision in precisions:
         s, d, clocks = time_precision(w, precision, device, args.warmup, args.steps, dist)
         handles[precision] = s
         step_s = d["step_ms"] / 1e3
@@ -283,18 +284,21 @@ def run_ours(args, dist: Dist):
             "tasks": tasks, "chem_cells": chem, "d": d, "clocks": clocks,
         }
     # error of the mixed path against the FP64 drop-in after identical steps
-    sched_levels = int(handles["mixed"].stats()["schedule_levels"])
-    fm, ff = handles["mixed"].fields(), handles["fp64"].fields()
-    err = {
-        "max_abs_dx_HII": float(np.abs(fm["ionized_hydrogen_fraction"] - ff["ionized_hydrogen_fraction"]).max()),
-        "max_rel_dT": float((np.abs(fm["temperature"] - ff["temperature"]) / ff["temperature"]).max()),
-        "levels_equal_fraction": float((handles["mixed"].cell_state()["level"] ==
-                                        handles["fp64"].cell_state()["level"]).mean()),
-    }
-    handles["fp64"].close()
+    head = "mixed" if "mixed" in results else "fp64"
+    sched_levels = int(handles[head].stats()["schedule_levels"])
+    err = None
+    if len(results) == 2:
+        fm, ff = handles["mixed"].fields(), handles["fp64"].fields()
+        err = {
+            "max_abs_dx_HII": float(np.abs(fm["ionized_hydrogen_fraction"] - ff["ionized_hydrogen_fraction"]).max()),
+            "max_rel_dT": float((np.abs(fm["temperature"] - ff["temperature"]) / ff["temperature"]).max()),
+            "levels_equal_fraction": float((handles["mixed"].cell_state()["level"] ==
+                                            handles["fp64"].cell_state()["level"]).mean()),
+        }
+        handles["fp64"].close()
 
     # end to end through the C ABI: each step = sw_step + field write-back to host memory
-    s = handles["mixed"]
+    s = handles[head]
     n = w.grid.num_cells
     out = {k: np.empty(n) for k in ("ionized_hydrogen_fraction", "temperature", "timestep", "photon_rate")}
     st0 = s.stats()
@@ -309,10 +313,10 @@ def run_ours(args, dist: Dist):
     e2e_tasks = dist.allreduce(float(st1["tasks"] - st0["tasks"]), "sum")
     s.close()
 
-    mixed = results["mixed"]
+    mixed = results[head]
     d = mixed["d"]
     peaks = measured_peaks()
-    b_task = bytes_per_task(f_dn, 4)
+    b_task = bytes_per_task(f_dn, 4 if head == "mixed" else 8)
     achieved_gbs = d["tasks"] * b_task / (d["transport_kernel_ms"] / 1e3) / 1e9 if d["transport_kernel_ms"] else None
     launches = d["transport_launches"]
     cpu = None
@@ -335,33 +339,37 @@ def run_ours(args, dist: Dist):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 transport + f64 chemistry",
+        "dtype": "f32 transport + f64 chemistry" if head == "mixed" else "f64",
         "data": "synthetic",
-        "config": dict(w.describe(), precision="mixed", replicas=args.gpus,
+        "config": dict(w.describe(), precision=head, replicas=args.gpus,
                        l2="per-(cell,dir) state of %.1f GB per array > 129 MB L2; no flush needed" %
                           (n * ((w.params.num_directions() + 7) // 8 * 8) * 4 / 1e9),
                        grid_build_s=round(grid_s, 1)),
         "chem_cells_per_s": mixed["chem_cells_per_s"],
-        "fp64": {k: results["fp64"][k] for k in ("cell_dir_updates_per_s", "chem_cells_per_s", "ms_per_step")},
-        "speedup_mixed_vs_fp64": results["fp64"]["ms_per_step"] / mixed["ms_per_step"],
+        "fp64": ({k: results["fp64"][k] for k in ("cell_dir_updates_per_s", "chem_cells_per_s", "ms_per_step")}
+                 if "fp64" in results else None),
+        "speedup_mixed_vs_fp64": (results["fp64"]["ms_per_step"] / mixed["ms_per_step"]
+                                  if len(results) == 2 else None),
         "error_mixed_vs_fp64": err,
         "e2e": {"value": e2e_tasks / e2e_max, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 4 * 8 * n},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": (achieved_gbs / peaks["hbm_gbs"]) if achieved_gbs else None,
-                     "traffic": None, "kernel": "k_sweep<float>",
+                     "traffic": None, "kernel": "k_sweep_pull" if head == "mixed" else "k_sweep_sched<double>",
                      "bytes_per_task": b_task, "f_dn": f_dn, "launches": launches,
                      "peak_source": peaks["source"]},
         "gpu_launches": int(d["kernel_launches"]),
         "clocks": mixed["clocks"],
-        "clocks_fp64": results["fp64"]["clocks"],
+        "clocks_fp64": results["fp64"]["clocks"] if "fp64" in results else None,
         "cpu_baseline": cpu,
         "stats": {"tasks": d["tasks"], "levelled_sweeps": d["levelled_sweeps"],
+                  "transport_attempts": d["transport_attempts"],
                   "sweeps": d["level_sweeps"], "schedule_levels": sched_levels,
                   "chem_attempts": d["chem_attempts"], "transport_kernel_ms": d["transport_kernel_ms"],
                   "sweep_ms": d["sweep_ms"], "chem_ms": d["chem_ms"], "level_ms": d["level_ms"],
-                  "fp64_transport_kernel_ms": results["fp64"]["d"]["transport_kernel_ms"],
-                  "fp64_chem_ms": results["fp64"]["d"]["chem_ms"]},
+                  "fp64_transport_kernel_ms": (results["fp64"]["d"]["transport_kernel_ms"]
+                                               if "fp64" in results else None),
+                  "fp64_chem_ms": results["fp64"]["d"]["chem_ms"] if "fp64" in results else None},
     }
     print(json.dumps(line), flush=True)
 
@@ -376,6 +384,8 @@ def main():
     ap.add_argument("--n-per-side", type=int, default=None)
     ap.add_argument("--cpu-sample-side", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["both", "fp64", "mixed"], default="both",
+                    help="GPU arithmetic(s) to time; value reports the mixed path when it runs")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -111,6 +111,8 @@ typedef struct {
   int64_t kernel_launches;     /* all kernel launches made by sw_step */
   int64_t levelled_sweeps;     /* level sweeps run on the precomputed levelled schedule */
   int64_t schedule_levels;     /* Kahn levels of the schedule (0: cyclic grid, no schedule) */
+  int64_t transport_attempts;  /* pull-path task attempts, retries included (tasks = success) */
+  int64_t upwind_slots;        /* pull path: upwind LOCAL (face, direction) pairs of the grid */
 } sw_stats;
 
 /* Fill the reference's defaults (num_directions 84, levels 1, max_timestep 1 Myr). */

@@ -96,6 +96,8 @@ class SwStats(ctypes.Structure):
         ("kernel_launches", c_int64),
         ("levelled_sweeps", c_int64),
         ("schedule_levels", c_int64),
+        ("transport_attempts", c_int64),
+        ("upwind_slots", c_int64),
     ]
 
 

@@ -63,6 +63,10 @@ struct DevicePtrs {
   uint32_t* order;           // levelled schedule: task ids grouped by Kahn level
   const uint32_t* lvl;       // level offsets into order [num_sched_levels + 1]
   uint32_t num_sched_levels; // 0: no levelled schedule (cyclic graph)
+  void* pull_rec;            // pull path: uint4 task record per schedule position
+  void* pull_slots;          // pull path: uint2 upwind slots of all positions
+  uint32_t* act;             // pull path: compacted active positions of the current sweep
+  uint32_t* chunk;           // pull path: compaction chunk offsets, count at [num_chunks]
   int level_blocks;          // resident blocks of the levelled kernel
   const uint32_t* periodic_cells;
   uint32_t n_periodic_cells;
@@ -91,6 +95,11 @@ struct PrecisionOps {
   // last sweep (pull path)
   cudaError_t (*photon_rate)(const DevicePtrs&, uint32_t last_epoch, double* out, cudaStream_t);
   cudaError_t (*export_rates)(const DevicePtrs&, int which, uint32_t last_epoch, double* out, cudaStream_t);
+  // pull path, once per grid: phase 0 writes the per-position task records and the
+  // 64-bit exclusive scan of the upwind counts per chunk into chunk_off (total at
+  // chunk_off[num_chunks]); phase 1, with pull_slots allocated, writes the slots.
+  // nullptr on the push path.
+  cudaError_t (*records)(const DevicePtrs&, int phase, unsigned long long* chunk_off, cudaStream_t);
 };
 
 extern const PrecisionOps kOpsFP64;

@@ -107,8 +107,10 @@ __device__ __forceinline__ uint32_t atom_sub_release(uint32_t* p, uint32_t v) {
   return old;
 }
 
+// (n.x*d.x + n.y*d.y) + n.z*d.z with every product and sum rounded separately, as the
+// reference evaluates it, in translation units compiled with and without contraction
 __device__ __forceinline__ double dot64(const Geo64& g, double dx, double dy, double dz) {
-  return g.x * dx + g.y * dy + g.z * dz;
+  return __dadd_rn(__dadd_rn(__dmul_rn(g.x, dx), __dmul_rn(g.y, dy)), __dmul_rn(g.z, dz));
 }
 
 // Exact classification of a face against a direction: the sign of the FP64 dot

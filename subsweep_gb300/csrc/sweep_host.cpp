@@ -89,7 +89,9 @@ struct sw_handle {
   std::string last_error;
   double* scratch = nullptr;  // N doubles for field export
   uint32_t stats_schedule_levels = 0;
+  int64_t stats_upwind_slots = 0;
   int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
+  bool trace = false;  // SUBSWEEP_TRACE: one stderr line per level sweep
   uint32_t last_epoch = 0;  // pull path: sweep number of the last sweep of the last step
 
   ~sw_handle() {
@@ -303,6 +305,38 @@ sw_status build_schedule(sw_handle* h) {
   return SW_OK;
 }
 
+// Pull path: task records and upwind slots of every schedule position (after the
+// schedule, or the id order of a cyclic grid, is in place).
+sw_status build_records(sw_handle* h) {
+  if (!h->ops->records) return SW_OK;
+  swh::DevicePtrs& p = h->p;
+  const size_t nc = (size_t)((h->N * (int64_t)h->D + swk::kCompactChunk - 1) / swk::kCompactChunk);
+  struct DeviceScratch {
+    void* ptr = nullptr;
+    ~DeviceScratch() {
+      if (ptr) cudaFree(ptr);
+    }
+  } off_scratch;
+  SW_CUDA(h, cudaMalloc(&off_scratch.ptr, (nc + 1) * sizeof(unsigned long long)), "record scratch");
+  auto* chunk_off = static_cast<unsigned long long*>(off_scratch.ptr);
+  SW_CUDA(h, h->ops->records(p, 0, chunk_off, h->stream), "task record kernels");
+  unsigned long long total = 0;
+  SW_CUDA(h, cudaMemcpyAsync(&total, chunk_off + nc, sizeof(total), cudaMemcpyDeviceToHost, h->stream),
+          "read slot total");
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "task records");
+  uint2* slots = nullptr;
+  if (!h->alloc(&slots, std::max<unsigned long long>(total, 1)))
+    return h->fail(SW_ERR_OOM, "device allocation of the upwind slots (%llu MB) failed", (total * 8) >> 20);
+  p.pull_slots = slots;
+  SW_CUDA(h, h->ops->records(p, 1, chunk_off, h->stream), "upwind slot kernel");
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "upwind slots");
+  uint32_t err = 0;
+  SW_CUDA(h, cudaMemcpy(&err, &p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
+  if (err & swk::kErrRecords) return h->fail(SW_ERR_CUDA, "upwind slot classification disagrees with its count");
+  h->stats_upwind_slots = (int64_t)total;
+  return SW_OK;
+}
+
 }  // namespace
 
 
@@ -512,6 +546,9 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (std::strcmp(env, "levels") == 0) h->force_path = 1;
     if (std::strcmp(env, "queue") == 0) h->force_path = 2;
   }
+  // SUBSWEEP_TRACE=1 prints one line per level sweep to stderr (level, active tasks,
+  // transport kernel / transport / chemistry milliseconds, transport attempts).
+  if (const char* env = std::getenv("SUBSWEEP_TRACE")) h->trace = env[0] != '\0' && env[0] != '0';
   p.timeout_ns = 2ull * 1000 * 1000 * 1000;  // a lane waits at most 2 s for its queue slot
   double max_dir = 0.0;
   for (int d = 0; d < D; ++d)
@@ -688,11 +725,14 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     swk::SweepCtl* ctl = nullptr;
     bool ok = h->alloc(&inc, nd * rb) && h->alloc(&per, nd * rb) && h->alloc(&cnt, nd / 4) &&
               h->alloc(&order, nd) && h->alloc(&ctl, 1);
-    if (ok && pull) ok = h->alloc(&qe, nd);
+    uint4* rec = nullptr;
+    uint32_t *act = nullptr, *chunk = nullptr;
+    const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
+    if (ok && pull) ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act, nd) && h->alloc(&chunk, chunks);
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
-              (pull ? 2 * rb + 13 : 4 * rb + 9) * nd >> 20);
+              (pull ? 2 * rb + 33 : 4 * rb + 9) * nd >> 20);
       return bail(SW_ERR_OOM);
     }
     cudaMemset(inc, 0, nd * rb);
@@ -707,6 +747,9 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     }
     cudaMemset(ctl, 0, sizeof(swk::SweepCtl));
     p.qe = qe;
+    p.pull_rec = rec;
+    p.act = act;
+    p.chunk = chunk;
     p.incoming = inc;
     p.outgoing = outg;
     p.periodic = per;
@@ -727,6 +770,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   }
   {
     sw_status st = build_schedule(h);
+    if (st == SW_OK) st = build_records(h);
     if (st != SW_OK) return bail(st);
   }
   *out = h;
@@ -760,6 +804,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
       levelled = true;  // the pull path always walks the schedule (or the id order)
       h->p.epoch += 1;
       h->last_epoch = h->p.epoch;
+      if (level > 0) launches += 3;  // compaction of the active positions
     } else {
       SW_CUDA(h, ops.init_counts(h->p, level, nullptr, !levelled, h->stream), "init_counts kernel");
       launches += 1;
@@ -786,6 +831,13 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     chem_ms += b;
     kernel_ms += k;
     h->stats.transport_launches += 1;
+    if (h->trace) {
+      swk::SweepCtl c{};
+      cudaMemcpy(&c, h->p.ctl, sizeof(c), cudaMemcpyDeviceToHost);
+      std::fprintf(stderr, "subsweep sweep level=%d active_tasks=%llu kernel_ms=%.3f transport_ms=%.3f chem_ms=%.3f attempts=%llu\n",
+                   level, (unsigned long long)h->n_ge_host[level] * (unsigned long long)h->D, k, a, b,
+                   (unsigned long long)c.attempts);
+    }
     uint32_t err = 0;
     SW_CUDA(h, cudaMemcpy(&err, &h->p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
     h->stats.level_sweeps += 1;
@@ -824,6 +876,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   h->stats.chem_cells = (int64_t)h->ctl_host.chem_cells;
   h->stats.chem_attempts = (int64_t)h->ctl_host.chem_attempts;
   h->stats.chem_failures = (int64_t)h->ctl_host.chem_failures;
+  h->stats.transport_attempts = (int64_t)h->ctl_host.attempts;
   h->stats.sweep_ms += sweep_ms;
   h->stats.chem_ms += chem_ms;
   h->stats.level_ms += level_ms;
@@ -916,6 +969,7 @@ sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double*
 sw_status sw_get_stats(sw_handle* h, sw_stats* out) {
   if (!h || !out) return SW_ERR_INVALID_ARG;
   h->stats.schedule_levels = h->stats_schedule_levels;
+  h->stats.upwind_slots = h->stats_upwind_slots;
   *out = h->stats;
   return SW_OK;
 }

@@ -3,6 +3,8 @@
 // (R = float, carried neutral fraction); each defines SWK_R, SWK_CARRY and SWK_OPS.
 #pragma once
 
+#include <cstdlib>
+
 #include "launch.h"
 #include "sweep_device.cuh"
 #if SWK_PULL
@@ -171,19 +173,77 @@ swk::PullArgs pull_args(const DevicePtrs& p, int level) {
   a.current_level = level;
   a.epoch = p.epoch;
   a.timeout_ns = p.timeout_ns;
+  a.rec = static_cast<const uint4*>(p.pull_rec);
+  a.slots = static_cast<const uint2*>(p.pull_slots);
+  a.act = nullptr;
+  a.act_count = nullptr;
+  a.count = (uint32_t)(p.num_cells * p.D);
   return a;
 }
 
-cudaError_t occupancy_pull(int* blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep_pull, swk::kPullThreads, 0);
+uint32_t num_chunks(const DevicePtrs& p) {
+  return (uint32_t)((p.num_cells * p.D + swk::kCompactChunk - 1) / swk::kCompactChunk);
 }
 
+cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_off, cudaStream_t s) {
+  swk::PullArgs a = pull_args(p, 0);
+  uint4* rec = static_cast<uint4*>(p.pull_rec);
+  const uint32_t nc = num_chunks(p);
+  if (phase == 0) {
+    swk::k_pull_rec_count<<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(a, p.order, a.count, rec);
+    swk::k_pull_slot_chunks<<<nc, swk::kCompactThreads, 0, s>>>(rec, a.count, p.chunk);
+    swk::k_scan_chunks64<<<1, swk::kScanThreads, 0, s>>>(p.chunk, nc, chunk_off);
+  } else {
+    swk::k_pull_slots<<<nc, swk::kCompactThreads, 0, s>>>(a, rec, a.count, chunk_off,
+                                                          static_cast<uint2*>(p.pull_slots));
+  }
+  return cudaGetLastError();
+}
+
+// Variants of the pull kernel: cursors per group (K) and the resident blocks per SM
+// targeted by the compiler.  SUBSWEEP_PULL_VARIANT = 10 * K + blocks picks one.
+constexpr int kDefaultPullVariant = 14;
+
+const void* pull_kernel(int variant) {
+  switch (variant) {
+    case 13: return (const void*)swk::k_sweep_pull<1, 3>;
+    case 15: return (const void*)swk::k_sweep_pull<1, 5>;
+    case 22: return (const void*)swk::k_sweep_pull<2, 2>;
+    case 24: return (const void*)swk::k_sweep_pull<2, 4>;
+    case 32: return (const void*)swk::k_sweep_pull<3, 2>;
+    case 23: return (const void*)swk::k_sweep_pull<2, 3>;
+    default: return (const void*)swk::k_sweep_pull<1, 4>;
+  }
+}
+
+int pull_variant() {
+  const char* env = std::getenv("SUBSWEEP_PULL_VARIANT");
+  return env ? std::atoi(env) : kDefaultPullVariant;
+}
+
+cudaError_t occupancy_pull(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pull_kernel(pull_variant()),
+                                                       swk::kPullThreads, 0);
+}
+
+// Sweeps above level 0 visit only the positions of active cells: a stable compaction of
+// the schedule (three launches) precedes the sweep kernel, which reads the count from
+// the device.
 cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, level);
-  const uint32_t* order = p.order;
-  uint32_t total = (uint32_t)(p.num_cells * p.D);
-  void* args[] = {&a, &order, &total};
-  return cudaLaunchCooperativeKernel((const void*)swk::k_sweep_pull, dim3(p.level_blocks), dim3(swk::kPullThreads),
+  if (level > 0) {
+    const uint32_t nc = num_chunks(p);
+    swk::k_compact_count<<<nc, swk::kCompactThreads, 0, s>>>(p.order, a.count, p.level, level, p.Np, p.chunk);
+    swk::k_compact_scan<<<1, swk::kScanThreads, 0, s>>>(p.chunk, nc, p.chunk + nc);
+    swk::k_compact_scatter<<<nc, swk::kCompactThreads, 0, s>>>(p.order, a.count, p.level, level, p.Np, p.chunk,
+                                                               p.act, p.qe, p.epoch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    a.act = p.act;
+    a.act_count = p.chunk + nc;
+  }
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel(pull_kernel(pull_variant()), dim3(p.level_blocks), dim3(swk::kPullThreads),
                                      args, 0, s);
 }
 
@@ -227,13 +287,13 @@ cudaError_t export_rates(const DevicePtrs& p, int which, uint32_t, double* out, 
 extern const PrecisionOps SWK_OPS = {
     SWK_NAME,       (int)sizeof(R), true,       occupancy,     attenuation, init_counts, sweep,
     occupancy_pull, sweep_pull,     kahn_round, schedule_seed, fold_pull,   chemistry,   photon_rate,
-    export_rates,
+    export_rates,   records,
 };
 #else
 extern const PrecisionOps SWK_OPS = {
     SWK_NAME,         (int)sizeof(R), false,      occupancy,     attenuation,   init_counts, sweep,
     occupancy_levels, sweep_levels,   kahn_round, schedule_seed, fold_periodic, chemistry,   photon_rate,
-    export_rates,
+    export_rates,     nullptr,
 };
 #endif
 

@@ -6,18 +6,20 @@
 // of  area_f |n_f . d| * out(n, d) / A(n, d),  where A(n, d) is n's total effective
 // downwind area.  This path evaluates that sum directly: every task publishes
 //   q(c, d) = out(c, d) / A(c, d)
-// together with the number of the sweep that produced it, as one 64-bit word, and a
-// task gathers q from its upwind neighbours.  A neighbour that is active in the
-// current sweep is ready once its word carries the current sweep number; an inactive
-// one keeps the q of its last solve (its flux persists, as in the reference).  The
-// 64-bit word is written and read in single accesses, so there are no atomics, no
-// counters and no fences on this path.  Tasks are visited in the levelled schedule
-// order, every upwind task lies at an earlier schedule position, and a task whose
-// inputs are not all published yet is retried.
+// together with the number of the sweep that produced it, as one 64-bit word
+// {q bits, sweep << 1 | stamped}, and a task gathers q from its upwind neighbours once
+// all their words carry the current sweep number.  Before a sweep above level 0, the
+// tasks of inactive cells are stamped with the sweep number (stamped bit set) and keep
+// their q: an inactive neighbour's flux persists, as in the reference.  The word is
+// written and read in single 64-bit accesses, so there are no atomics, no counters and
+// no fences on this path.  Tasks are visited in the levelled schedule order, every
+// upwind task lies at an earlier schedule position, and a task whose inputs are not
+// all published yet is retried.
 //
 // Geometry is one 16-byte load per face: {area * n (FP32, area scaled by 2^-k),
 // neighbour | kind << 30}.  The sign of n . d decides up/downwind exactly: the FP32 dot
-// decides when it exceeds its rounding bound, else the FP64 normal does.
+// decides when it exceeds its rounding bound, else the FP64 normal does.  The sweep
+// itself reads precomputed per-position records and upwind slots (below).
 #pragma once
 
 #include "sweep_device.cuh"
@@ -44,29 +46,53 @@ struct PullArgs {
   int current_level;
   uint32_t epoch;
   unsigned long long timeout_ns;
+  // sweep kernel
+  const uint4* rec;           // per schedule position: {task, 1/A_down, slot offset lo, count | offset hi << 8}
+  const uint2* slots;         // upwind LOCAL faces of every position: {cell, |area n . d| (FP32)}
+  const uint32_t* act;        // compacted active positions, or nullptr: every position
+  const uint32_t* act_count;  // device count of act (written by the compaction)
+  uint32_t count;             // number of positions when act is nullptr
 };
 
+// The words are only ever read and written whole and nothing else is ordered against
+// them inside a sweep, so the accesses need no memory clobber.
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
   unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+
+// predicated form: returns 0 without touching memory when pred is false
+__device__ __forceinline__ unsigned long long ld_relaxed_u64_if(bool pred, const unsigned long long* p) {
+  unsigned long long v = 0;
+  asm volatile(
+      "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.relaxed.gpu.global.u64 %0, [%1];\n\t}"
+      : "+l"(v)
+      : "l"(p), "r"((uint32_t)pred));
   return v;
 }
 
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v));
 }
 
-__device__ __forceinline__ unsigned long long pack_qe(float q, uint32_t epoch) {
-  return ((unsigned long long)epoch << 32) | (unsigned long long)__float_as_uint(q);
+// {q, sweep << 1}: solved in `sweep`; {q, sweep << 1 | 1}: stamped (inactive in `sweep`)
+__device__ __forceinline__ unsigned long long pack_qe(float q, uint32_t sweep) {
+  return ((unsigned long long)(sweep << 1) << 32) | (unsigned long long)__float_as_uint(q);
+}
+__device__ __forceinline__ bool word_current(unsigned long long w, uint32_t sweep) {
+  return (uint32_t)(w >> 33) == sweep;
 }
 
 // Signed effective area s = (area n) . d of one face, with the exact sign of n . d:
 // returns +|s| downwind, -|s| upwind, 0 when n . d == 0.
 __device__ __forceinline__ float face_eff(const uint4& g, float fx, float fy, float fz, const Geo64* g64,
                                           double dx, double dy, double dz) {
+  // explicit roundings: every kernel that classifies a face gets the same answer
   const float ax = __uint_as_float(g.x), ay = __uint_as_float(g.y), az = __uint_as_float(g.z);
-  const float s = ax * fx + ay * fy + az * fz;
-  const float bound = 8.0e-7f * (fabsf(ax * fx) + fabsf(ay * fy) + fabsf(az * fz));
+  const float s = __fmaf_rn(az, fz, __fmaf_rn(ay, fy, __fmul_rn(ax, fx)));
+  const float bound =
+      __fmul_rn(8.0e-7f, __fadd_rn(__fadd_rn(fabsf(__fmul_rn(ax, fx)), fabsf(__fmul_rn(ay, fy))), fabsf(__fmul_rn(az, fz))));
   if (s > bound) return s;
   if (s < -bound) return s;
   const double e = dot64(*g64, dx, dy, dz);
@@ -76,121 +102,421 @@ __device__ __forceinline__ float face_eff(const uint4& g, float fx, float fy, fl
 }
 
 constexpr int kPullThreads = 256;
+constexpr int kPullGroup = 8;   // lanes per task
+constexpr int kPullRounds = 2;  // slots per lane held in registers (tasks with <= 16 upwind faces)
 
-// One attempt at the tasks of the warp's groups (kGroup lanes each).  Returns, per
-// group, whether the task was committed (all active upwind inputs published).
-__device__ __forceinline__ bool try_solve_pull(const PullArgs& a, bool have, uint32_t t) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t gl = lane & (kGroup - 1);
-  uint32_t c = 0, d = 0, beg = 0, nf = 0;
-  float per = 0.f, src = 0.f;
-  double att = 0.0;
-  if (have) {
-    d = t / a.Np;
-    c = t - d * a.Np;
-    if (gl == 0) {
-      beg = a.off[c];
-      nf = a.off[c + 1] - beg;
-      per = __ldcg(a.periodic + t);
-      src = a.src_dir[c];
-      att = a.att[c];
-    }
-  }
-  beg = __shfl_sync(0xffffffffu, beg, 0, kGroup);
-  nf = __shfl_sync(0xffffffffu, nf, 0, kGroup);
-  float fx = 0.f, fy = 0.f, fz = 0.f;
-  double dx = 0.0, dy = 0.0, dz = 0.0;
-  if (have) {
-    fx = a.dir32[3 * d]; fy = a.dir32[3 * d + 1]; fz = a.dir32[3 * d + 2];
-    dx = a.dir64[3 * d]; dy = a.dir64[3 * d + 1]; dz = a.dir64[3 * d + 2];
-  }
-  uint32_t rounds = (nf + kGroup - 1) / kGroup;
-  for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
-  float area_down = 0.f, in = 0.f;
-  bool ok = true;
-  for (uint32_t k = 0; k < rounds; ++k) {
-    const uint32_t fl = gl + k * kGroup;
-    if (fl >= nf) continue;
-    const uint32_t f = beg + fl;
-    const uint4 g = a.geo16[f];
-    const float s = face_eff(g, fx, fy, fz, a.geo64 + f, dx, dy, dz);
-    if (s > 0.f) {
-      area_down += s;
-    } else if (s < 0.f && (g.w >> kKindShift) == kKindLocal) {
-      const uint32_t n = g.w & kNbrMask;
-      const unsigned long long w = ld_relaxed_u64(a.qe + (size_t)d * a.Np + n);
-      if ((uint32_t)(w >> 32) != a.epoch && a.level[n] >= a.current_level) {
-        ok = false;  // active upwind neighbour not solved yet in this sweep
-      } else {
-        in += -s * __uint_as_float((uint32_t)w);
-      }
-    }
-  }
-  // group reductions
-  for (int o = 1; o < kGroup; o <<= 1) {
-    area_down += __shfl_xor_sync(0xffffffffu, area_down, o, kGroup);
-    in += __shfl_xor_sync(0xffffffffu, in, o, kGroup);
-    ok = (__shfl_xor_sync(0xffffffffu, ok ? 1 : 0, o, kGroup) != 0) && ok;
-  }
-  const bool commit = have && ok;
-  if (commit && gl == 0) {
-    const float r = (in + src) + per;  // Site::get_rate, site.rs:53-56
-    const float out = (r < a.threshold) ? 0.f : r * (float)att;  // get_outgoing_rate
-    const float q = area_down > 0.f ? out / area_down : 0.f;
-    a.incoming[t] = in;
-    st_relaxed_u64(a.qe + t, pack_qe(q, a.epoch));
-  }
-  return commit;
+// t = d * Np + c  ->  (c, d) without a runtime integer division: FP32 estimate of the
+// quotient (t / Np <= 128, so it is off by at most one), then an exact correction.
+__device__ __forceinline__ void split_task(uint32_t t, uint32_t Np, float inv_np, uint32_t& c, uint32_t& d) {
+  int q = (int)(__uint2float_rn(t) * inv_np);
+  long long r = (long long)t - (long long)q * Np;
+  if (r < 0) { --q; r += Np; }
+  if (r >= (long long)Np) { ++q; r -= Np; }
+  d = (uint32_t)q;
+  c = (uint32_t)r;
 }
 
-// Scheduled pull sweep (cooperative launch; every block resident).  Group g visits
-// schedule positions g, g + G, ...; inactive cells' tasks are skipped.
-__global__ void __launch_bounds__(kPullThreads) k_sweep_pull(PullArgs a, const uint32_t* order, uint32_t total_sched) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t gl = lane & (kGroup - 1);
-  const uint32_t groups = gridDim.x * (kPullThreads / kGroup);
-  uint32_t i = blockIdx.x * (kPullThreads / kGroup) + (threadIdx.x / kGroup);
-  unsigned long long solved = 0;
-  bool stop = false;
-  while (!stop && __any_sync(0xffffffffu, i < total_sched)) {
-    bool pending = false;
-    uint32_t t = 0;
-    if (i < total_sched) {
-      t = order[i];
-      const uint32_t c = t - (t / a.Np) * a.Np;
-      pending = a.level[c] >= a.current_level;
+// record word w: upwind count (7 bits) | direction << 7 (7 bits) | slot offset >> 32 << 14
+__device__ __forceinline__ unsigned long long rec_offset(const uint4& r) {
+  return (unsigned long long)r.z | ((unsigned long long)(r.w >> 14) << 32);
+}
+__device__ __forceinline__ uint32_t rec_count(const uint4& r) { return r.w & 0x7fu; }
+__device__ __forceinline__ uint32_t rec_dir(const uint4& r) { return (r.w >> 7) & 0x7fu; }
+
+// ---------------------------------------------------------------------------------------
+// Task records and upwind slots, built once per grid from the schedule (geometry only).
+// Position p of the schedule (task t = order[p] = d * Np + c) gets
+//   rec[p]   = {c, bits of 1 / A_down (FP32; 0 when no face is downwind),
+//               slot offset (low 32 bits), upwind count | d << 7 | offset >> 32 << 14}
+//   slots[offset + k] = {upwind task d * Np + n, |area n . d| in FP32}, k < count,
+// for the upwind LOCAL faces of c in face order (exact sign of n . d).  A_down is
+// summed in face order.  Counts, a chunked 64-bit exclusive scan, then the writes.
+
+__device__ __forceinline__ void classify_task(const PullArgs& a, uint32_t t, float inv_np, uint32_t& c,
+                                              uint32_t& d, uint32_t& beg, uint32_t& nf) {
+  split_task(t, a.Np, inv_np, c, d);
+  beg = a.off[c];
+  nf = a.off[c + 1] - beg;
+}
+
+__global__ void k_pull_rec_count(PullArgs a, const uint32_t* order, uint32_t total, uint4* rec) {
+  const float inv_np = 1.0f / (float)a.Np;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+    const uint32_t t = order[p];
+    uint32_t c, d, beg, nf;
+    classify_task(a, t, inv_np, c, d, beg, nf);
+    const float fx = a.dir32[3 * d], fy = a.dir32[3 * d + 1], fz = a.dir32[3 * d + 2];
+    const double dx = a.dir64[3 * d], dy = a.dir64[3 * d + 1], dz = a.dir64[3 * d + 2];
+    float area_down = 0.f;
+    uint32_t n_up = 0;
+    for (uint32_t j = 0; j < nf; ++j) {
+      const uint4 g = a.geo16[beg + j];
+      const float sj = face_eff(g, fx, fy, fz, a.geo64 + beg + j, dx, dy, dz);
+      if (sj > 0.f) area_down += sj;
+      else if (sj < 0.f && (g.w >> kKindShift) == kKindLocal) ++n_up;
     }
-    unsigned long long w0 = 0;
-    uint32_t wait_ns = 32;
-    while (__any_sync(0xffffffffu, pending)) {
-      const bool done = try_solve_pull(a, pending, t);
-      if (__any_sync(0xffffffffu, done)) {
-        if (done) {
-          pending = false;
-          if (gl == 0) ++solved;
-        }
-        w0 = 0;
-        wait_ns = 32;
-      } else {
-        int expired = 0;
-        if (lane == 0) {
-          const unsigned long long now = globaltimer_ns();
-          if (w0 == 0) w0 = now;
-          expired = (now - w0 > a.timeout_ns) || (*(volatile uint32_t*)&a.ctl->error != 0);
-        }
-        if (__shfl_sync(0xffffffffu, expired, 0)) {
-          if (lane == 0) atomicOr(&a.ctl->error, kErrStall);
-          stop = true;
-          break;
-        }
-        __nanosleep(wait_ns);
-        wait_ns = min(wait_ns * 2, 512u);
+    const float inv = area_down > 0.f ? 1.0f / area_down : 0.f;
+    rec[p] = make_uint4(c, __float_as_uint(inv), 0u, n_up | (d << 7));
+  }
+}
+
+// per chunk of kCompactChunk positions: total upwind count
+__global__ void __launch_bounds__(kCompactThreads) k_pull_slot_chunks(const uint4* rec, uint32_t total,
+                                                                      uint32_t* chunk) {
+  const uint32_t first = blockIdx.x * kCompactChunk + threadIdx.x * kCompactPer;
+  uint32_t n = 0;
+  for (int k = 0; k < kCompactPer; ++k)
+    if (first + k < total) n += rec_count(rec[first + k]);
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  __shared__ uint32_t ws[kCompactThreads / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t s = 0;
+    for (int w = 0; w < kCompactThreads / 32; ++w) s += ws[w];
+    chunk[blockIdx.x] = s;
+  }
+}
+
+// exclusive 64-bit scan of the chunk totals (one block); the grand total at out[n]
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) k_scan_chunks64(const uint32_t* chunk, uint32_t n,
+                                                                unsigned long long* out) {
+  __shared__ unsigned long long warp_sum[kScanThreads / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long carry = 0;
+  for (uint32_t base = 0; base < n; base += kScanThreads) {
+    const uint32_t i = base + threadIdx.x;
+    const unsigned long long v = i < n ? chunk[i] : 0ull;
+    unsigned long long x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    unsigned long long wbase = 0, tot = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+      const unsigned long long s = warp_sum[w];
+      if ((uint32_t)w < warp) wbase += s;
+      tot += s;
+    }
+    if (i < n) out[i] = carry + wbase + x - v;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+// Writes at most the counted number of slots per position; a classification that
+// disagrees with the count flags kErrRecords.
+__global__ void __launch_bounds__(kCompactThreads) k_pull_slots(PullArgs a, uint4* rec, uint32_t total,
+                                                                const unsigned long long* chunk_off,
+                                                                uint2* slots) {
+  const uint32_t first = blockIdx.x * kCompactChunk + threadIdx.x * kCompactPer;
+  uint32_t mine = 0;
+  for (int k = 0; k < kCompactPer; ++k)
+    if (first + k < total) mine += rec_count(rec[first + k]);
+  // block-exclusive prefix of the per-thread totals
+  __shared__ uint32_t ws[kCompactThreads / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = mine;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  uint32_t wbase = 0;
+  for (uint32_t w = 0; w < warp; ++w) wbase += ws[w];
+  unsigned long long o = chunk_off[blockIdx.x] + wbase + x - mine;
+  for (int k = 0; k < kCompactPer; ++k) {
+    const uint32_t p = first + k;
+    if (p >= total) break;
+    uint4 r = rec[p];
+    const uint32_t n_up = rec_count(r);
+    const uint32_t c = r.x, d = rec_dir(r);
+    r.z = (uint32_t)o;
+    r.w = n_up | (d << 7) | ((uint32_t)(o >> 32) << 14);
+    rec[p] = r;
+    const uint32_t beg = a.off[c], nf = a.off[c + 1] - beg;
+    const uint32_t dnp = d * a.Np;
+    const float fx = a.dir32[3 * d], fy = a.dir32[3 * d + 1], fz = a.dir32[3 * d + 2];
+    const double dx = a.dir64[3 * d], dy = a.dir64[3 * d + 1], dz = a.dir64[3 * d + 2];
+    uint32_t written = 0;
+    for (uint32_t j = 0; j < nf; ++j) {
+      const uint4 g = a.geo16[beg + j];
+      if ((g.w >> kKindShift) != kKindLocal) continue;
+      const float sj = face_eff(g, fx, fy, fz, a.geo64 + beg + j, dx, dy, dz);
+      if (sj < 0.f) {
+        if (written < n_up) slots[o + written] = make_uint2(dnp + (g.w & kNbrMask), __float_as_uint(-sj));
+        ++written;
       }
     }
-    i += groups;
+    if (written != n_up) atomicOr(&a.ctl->error, kErrRecords);
+    o += n_up;
   }
-  for (int o = 16; o > 0; o >>= 1) solved += __shfl_xor_sync(0xffffffffu, solved, o);
+}
+
+// ---------------------------------------------------------------------------------------
+// Stable compaction of the schedule positions whose cell is active in a sweep of
+// `level` (level[c] >= level): counts per chunk, an exclusive scan of the counts, and
+// the scatter.  Each thread owns kCompactPer consecutive positions.
+
+__device__ __forceinline__ uint32_t active_bits(const uint32_t* order, uint32_t total, const uint8_t* level,
+                                                int cur, uint32_t Np, float inv_np, uint32_t first) {
+  uint32_t bits = 0;
+#pragma unroll
+  for (int k = 0; k < kCompactPer; ++k) {
+    const uint32_t p = first + k;
+    if (p < total) {
+      uint32_t c, d;
+      split_task(order[p], Np, inv_np, c, d);
+      if (level[c] >= cur) bits |= 1u << k;
+    }
+  }
+  return bits;
+}
+
+// exclusive block-wide prefix sum of v (kCompactThreads threads); returns the block total
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& excl) {
+  __shared__ uint32_t warp_sum[kCompactThreads / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) warp_sum[warp] = x;
+  __syncthreads();
+  uint32_t base = 0, total = 0;
+  for (int w = 0; w < kCompactThreads / 32; ++w) {
+    const uint32_t ws = warp_sum[w];
+    if ((uint32_t)w < warp) base += ws;
+    total += ws;
+  }
+  __syncthreads();
+  excl = base + x - v;
+  return total;
+}
+
+__global__ void __launch_bounds__(kCompactThreads) k_compact_count(const uint32_t* order, uint32_t total,
+                                                                   const uint8_t* level, int cur, uint32_t Np,
+                                                                   uint32_t* chunk) {
+  const float inv_np = 1.0f / (float)Np;
+  const uint32_t first = blockIdx.x * kCompactChunk + threadIdx.x * kCompactPer;
+  const uint32_t n = __popc(active_bits(order, total, level, cur, Np, inv_np, first));
+  uint32_t excl;
+  const uint32_t sum = block_exclusive_scan(n, excl);
+  if (threadIdx.x == 0) chunk[blockIdx.x] = sum;
+}
+
+// exclusive scan of the chunk counts in place (one block); the total goes to *count
+__global__ void __launch_bounds__(kScanThreads) k_compact_scan(uint32_t* chunk, uint32_t n, uint32_t* count) {
+  __shared__ uint32_t warp_sum[kScanThreads / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < n; base += kScanThreads) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < n ? chunk[i] : 0u;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    uint32_t wbase = 0, total = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+      const uint32_t ws = warp_sum[w];
+      if ((uint32_t)w < warp) wbase += ws;
+      total += ws;
+    }
+    if (i < n) chunk[i] = carry + wbase + x - v;
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = carry;
+}
+
+// Also stamps the words of the inactive tasks with the sweep number (stamped bit set),
+// so the sweep's readiness test is the sweep number alone.  Nothing else touches the
+// words between the previous kernel and the sweep.
+__global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(const uint32_t* order, uint32_t total,
+                                                                     const uint8_t* level, int cur, uint32_t Np,
+                                                                     const uint32_t* chunk, uint32_t* act,
+                                                                     unsigned long long* qe, uint32_t sweep) {
+  const float inv_np = 1.0f / (float)Np;
+  const uint32_t first = blockIdx.x * kCompactChunk + threadIdx.x * kCompactPer;
+  uint32_t bits = active_bits(order, total, level, cur, Np, inv_np, first);
+  uint32_t excl;
+  block_exclusive_scan(__popc(bits), excl);
+  for (int k = 0; k < kCompactPer; ++k)
+    if (first + k < total && !((bits >> k) & 1u))
+      reinterpret_cast<uint32_t*>(qe + order[first + k])[1] = (sweep << 1) | 1u;
+  uint32_t o = chunk[blockIdx.x] + excl;
+  while (bits) {
+    const int k = __ffs(bits) - 1;
+    act[o++] = first + k;
+    bits &= bits - 1;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Scheduled pull sweep (cooperative launch; every block resident).
+//
+// A group of kPullGroup lanes runs K cursors; cursor v (of V = groups * K) visits the
+// active positions v, v + V, v + 2V, ... in schedule order.  For its current task a
+// cursor gathers the upwind tasks' words through the task's slots (lane l: slots l,
+// l + 8, ...) and commits
+//   in = sum_slots |area n . d| q(n, d),   out = (in + source/D + periodic) * attenuation
+// (zero below the threshold), q = out / A_down, once every word carries the current
+// sweep number; otherwise it retries.  Each cursor keeps a pipeline of its next
+// positions (position index, record, slots), every stage loaded one task before it is
+// used, so a task waits only for its neighbours' words.  The warp sleeps with
+// exponential backoff only when none of its cursors committed.  Every dependency lies
+// at an earlier position and every cursor walks its positions in order, so the
+// earliest unsolved task can always commit.
+template <int K>
+struct PullCursor {
+  uint32_t i[K];                       // current position index
+  uint4 cur[K], n1[K], n2[K];          // records of positions i, i + V, i + 2V
+  uint32_t p3[K];                      // schedule position of i + 3V
+  uint2 s[K][kPullRounds], ns[K][kPullRounds];  // slots of i and i + V
+  bool have[K];
+};
+
+__device__ __forceinline__ uint32_t pull_pos(const PullArgs& a, uint32_t j) { return a.act ? a.act[j] : j; }
+
+__device__ __forceinline__ void load_slots(const PullArgs& a, const uint4& r, uint32_t gl, uint2 (&s)[kPullRounds]) {
+  const uint32_t n = rec_count(r);
+  const uint2* base = a.slots + rec_offset(r);
+#pragma unroll
+  for (int k = 0; k < kPullRounds; ++k)
+    if (gl + k * kPullGroup < n) s[k] = __ldg(base + gl + k * kPullGroup);
+}
+
+template <int K, int kMinBlocks>
+__global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArgs a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = lane & (kPullGroup - 1);
+  const uint32_t gfirst = lane & ~(uint32_t)(kPullGroup - 1);
+  const uint32_t V = gridDim.x * (kPullThreads / kPullGroup) * K;
+  const uint32_t v0 = (blockIdx.x * (kPullThreads / kPullGroup) + (threadIdx.x / kPullGroup)) * K;
+  const uint32_t count = a.act ? *a.act_count : a.count;
+  const uint32_t sweep = a.epoch;
+  PullCursor<K> q;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const uint32_t i = v0 + k;
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    q.i[k] = i;
+    q.cur[k] = q.n1[k] = q.n2[k] = z;
+    q.p3[k] = 0;
+    if (i < count) q.cur[k] = a.rec[pull_pos(a, i)];
+    if (i + V < count) q.n1[k] = a.rec[pull_pos(a, i + V)];
+    if (i + 2 * V < count) q.n2[k] = a.rec[pull_pos(a, i + 2 * V)];
+    if (i + 3 * V < count) q.p3[k] = pull_pos(a, i + 3 * V);
+    q.have[k] = i < count;
+    load_slots(a, q.cur[k], gl, q.s[k]);
+    if (i + V < count) load_slots(a, q.n1[k], gl, q.ns[k]);
+  }
+  unsigned long long solved = 0, attempts = 0, w0 = 0;
+  uint32_t wait_ns = 32;
+  while (true) {
+    bool any_have = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) any_have = any_have || q.have[k];
+    if (!__any_sync(0xffffffffu, any_have)) break;
+    // the upwind words of the current tasks, and the leaders' cell data
+    unsigned long long w[K][kPullRounds];
+    float src[K], per[K], att[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t n_up = q.have[k] ? rec_count(q.cur[k]) : 0u;
+#pragma unroll
+      for (int r = 0; r < kPullRounds; ++r)
+        w[k][r] = ld_relaxed_u64_if(gl + r * kPullGroup < n_up, a.qe + q.s[k][r].x);
+      src[k] = per[k] = att[k] = 0.f;
+      if (q.have[k] && gl == 0) {
+        const uint32_t c = q.cur[k].x;
+        src[k] = a.src_dir[c];
+        per[k] = __ldcg(a.periodic + rec_dir(q.cur[k]) * a.Np + c);
+        att[k] = (float)a.att[c];
+      }
+    }
+    bool progress = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t n_up = q.have[k] ? rec_count(q.cur[k]) : 0u;
+      float in = 0.f;
+      bool bad = false;
+#pragma unroll
+      for (int r = 0; r < kPullRounds; ++r) {
+        if (gl + r * kPullGroup < n_up) {
+          bad = bad || !word_current(w[k][r], sweep);
+          in = fmaf(__uint_as_float(q.s[k][r].y), __uint_as_float((uint32_t)w[k][r]), in);
+        }
+      }
+      // tasks with more than kPullGroup * kPullRounds upwind faces: the rest from memory
+      for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
+        const uint2 sl = a.slots[rec_offset(q.cur[k]) + j];
+        const unsigned long long wn = ld_relaxed_u64(a.qe + sl.x);
+        bad = bad || !word_current(wn, sweep);
+        in = fmaf(__uint_as_float(sl.y), __uint_as_float((uint32_t)wn), in);
+      }
+      const bool ok = ((__ballot_sync(0xffffffffu, bad) >> gfirst) & ((1u << kPullGroup) - 1u)) == 0u;
+#pragma unroll
+      for (int o = 1; o < kPullGroup; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, kPullGroup);
+      const bool commit = q.have[k] && ok;
+      if (q.have[k] && gl == 0) ++attempts;
+      if (commit && gl == 0) {
+        const uint32_t t = rec_dir(q.cur[k]) * a.Np + q.cur[k].x;
+        const float rt = (in + src[k]) + per[k];                   // Site::get_rate, site.rs:53-56
+        const float out = (rt < a.threshold) ? 0.f : rt * att[k];  // get_outgoing_rate
+        const float qv = out * __uint_as_float(q.cur[k].y);
+        a.incoming[t] = in;
+        st_relaxed_u64(a.qe + t, pack_qe(qv, sweep));
+        ++solved;
+      }
+      if (commit) {  // advance the cursor and its pipeline by one position
+        const uint32_t i = q.i[k] + V;
+        q.i[k] = i;
+        q.cur[k] = q.n1[k];
+#pragma unroll
+        for (int r = 0; r < kPullRounds; ++r) q.s[k][r] = q.ns[k][r];
+        q.have[k] = i < count;
+        q.n1[k] = q.n2[k];
+        if (i + V < count) load_slots(a, q.n1[k], gl, q.ns[k]);
+        if (i + 2 * V < count) q.n2[k] = a.rec[q.p3[k]];
+        if (i + 3 * V < count) q.p3[k] = pull_pos(a, i + 3 * V);
+        progress = true;
+      }
+    }
+    if (__any_sync(0xffffffffu, progress)) {
+      w0 = 0;
+      wait_ns = 32;
+    } else {
+      int expired = 0;
+      if (lane == 0) {
+        const unsigned long long now = globaltimer_ns();
+        if (w0 == 0) w0 = now;
+        expired = (now - w0 > a.timeout_ns) || (*(volatile uint32_t*)&a.ctl->error != 0);
+      }
+      if (__shfl_sync(0xffffffffu, expired, 0)) {
+        if (lane == 0) atomicOr(&a.ctl->error, kErrStall);
+        break;
+      }
+      __nanosleep(wait_ns);
+      wait_ns = min(wait_ns * 2, 256u);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    solved += __shfl_xor_sync(0xffffffffu, solved, o);
+    attempts += __shfl_xor_sync(0xffffffffu, attempts, o);
+  }
   if (lane == 0 && solved) atomicAdd(&a.ctl->tasks, solved);
+  if (lane == 0 && attempts) atomicAdd(&a.ctl->attempts, attempts);
 }
 
 // Gathered incoming rate of (c, d): sum over upwind LOCAL faces of |s| q(n, d), or
@@ -225,7 +551,7 @@ __global__ void k_fold_pull(PullArgs a, float* periodic, const uint32_t* cells, 
 // neighbours' current q (the reference keeps adding corrections to inactive cells).
 __device__ __forceinline__ float current_incoming(const PullArgs& a, uint32_t c, uint32_t d, uint32_t last_epoch) {
   const size_t t = (size_t)d * a.Np + c;
-  if ((uint32_t)(a.qe[t] >> 32) == last_epoch) return a.incoming[t];
+  if ((uint32_t)(a.qe[t] >> 32) == (last_epoch << 1)) return a.incoming[t];  // solved, not stamped
   return gather_in(a, c, d, false);
 }
 

@@ -16,8 +16,13 @@ constexpr uint32_t kKindShift = 30;
 constexpr uint32_t kNbrMask = (1u << kKindShift) - 1;
 constexpr uint32_t kKindLocal = 0, kKindPeriodic = 1, kKindBoundary = 2;
 constexpr uint32_t kEmptySlot = 0xffffffffu;
+// stable compaction of schedule positions (pull path): threads per block, positions per
+// thread, positions per chunk
+constexpr int kCompactThreads = 256;
+constexpr int kCompactPer = 8;
+constexpr uint32_t kCompactChunk = kCompactThreads * kCompactPer;
 
-enum : uint32_t { kErrStall = 1u, kErrQueue = 2u, kErrClamp = 8u };
+enum : uint32_t { kErrStall = 1u, kErrQueue = 2u, kErrClamp = 8u, kErrRecords = 16u };
 
 // Control block of one handle (device memory).
 struct SweepCtl {
@@ -29,6 +34,7 @@ struct SweepCtl {
   unsigned long long chem_cells;
   unsigned long long chem_attempts;
   unsigned long long chem_failures;
+  unsigned long long attempts;  // task attempts of the pull transport (retries included)
   uint32_t n_ge[32];       // number of cells with level >= l (current level assignment)
   uint32_t hist[32];       // scratch level histogram
 };
