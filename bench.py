@@ -144,6 +144,14 @@ def mean_downwind_faces(grid, directions: np.ndarray, sample: int = 60000, seed:
     return float((dots > 0).sum() / (len(cells) * directions.shape[0])) if counts.sum() else 0.0
 
 
+# DRAM bytes per task of the pull transport kernel, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on a level-0 launch of the C2 grid at
+# 64^3 (22,020,096 tasks): 2.254 GB per launch.  The per-launch traffic at other sizes
+# is scaled by the tasks of a launch.
+MEASURED_DRAM_BYTES_PER_TASK = {"mixed": 102.4}
+TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 launch on C2 64^3, per task"
+
+
 def bytes_per_task(f_dn: float, rate_bytes: int, counter_bytes: int = 1) -> float:
     """Algorithmic bytes of one cell-direction update: read incoming, periodic and the
     old outgoing rate, write the new one, and read-modify-write the incoming rate and
@@ -319,6 +327,8 @@ def run_ours(args, dist: Dist):
     b_task = bytes_per_task(f_dn, 4 if head == "mixed" else 8)
     achieved_gbs = d["tasks"] * b_task / (d["transport_kernel_ms"] / 1e3) / 1e9 if d["transport_kernel_ms"] else None
     launches = d["transport_launches"]
+    traffic = (MEASURED_DRAM_BYTES_PER_TASK[head] * d["tasks"] / launches
+               if head in MEASURED_DRAM_BYTES_PER_TASK and launches else None)
     cpu = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         c_tasks, c_chem, c_wall = cpu_sample(args.workload, args.cpu_sample_side, 1, 1, 1)
@@ -355,7 +365,9 @@ def run_ours(args, dist: Dist):
                 "d2h_bytes_per_step": 4 * 8 * n},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": (achieved_gbs / peaks["hbm_gbs"]) if achieved_gbs else None,
-                     "traffic": None, "kernel": "k_sweep_pull" if head == "mixed" else "k_sweep_sched<double>",
+                     "traffic": traffic, "traffic_unit": "bytes per launch",
+                     "traffic_source": TRAFFIC_SOURCE if traffic else None,
+                     "kernel": "k_sweep_pull" if head == "mixed" else "k_sweep_sched<double>",
                      "bytes_per_task": b_task, "f_dn": f_dn, "launches": launches,
                      "peak_source": peaks["source"]},
         "gpu_launches": int(d["kernel_launches"]),
