@@ -200,9 +200,10 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
   return cudaGetLastError();
 }
 
-// Variants of the pull kernel: cursors per group (K) and the resident blocks per SM
-// targeted by the compiler.  SUBSWEEP_PULL_VARIANT = 10 * K + blocks picks one.
-constexpr int kDefaultPullVariant = 14;
+// Variants of the pull kernel: independent cursors (10 * cursors per group + target
+// blocks per SM) or warp-lockstep blocks of four positions (90 + blocks per SM).
+// SUBSWEEP_PULL_VARIANT picks one.
+constexpr int kDefaultPullVariant = 94;
 
 const void* pull_kernel(int variant) {
   switch (variant) {
@@ -212,6 +213,9 @@ const void* pull_kernel(int variant) {
     case 24: return (const void*)swk::k_sweep_pull<2, 4>;
     case 32: return (const void*)swk::k_sweep_pull<3, 2>;
     case 23: return (const void*)swk::k_sweep_pull<2, 3>;
+    case 94: return (const void*)swk::k_sweep_pull_lock<4>;
+    case 95: return (const void*)swk::k_sweep_pull_lock<5>;
+    case 96: return (const void*)swk::k_sweep_pull_lock<6>;
     default: return (const void*)swk::k_sweep_pull<1, 4>;
   }
 }

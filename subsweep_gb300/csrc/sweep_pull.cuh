@@ -519,6 +519,115 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArg
   if (lane == 0 && attempts) atomicAdd(&a.ctl->attempts, attempts);
 }
 
+// Warp-lockstep variant of the pull sweep: warp w owns the blocks of four consecutive
+// positions b = w, w + W, ... (group g of the warp takes position 4b + g) and advances
+// all four together once every one has committed, so the pipeline shift is a
+// warp-uniform branch and the four groups' records and slots are contiguous.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(PullArgs a) {
+  constexpr uint32_t kGroups = 32 / kPullGroup;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = lane & (kPullGroup - 1);
+  const uint32_t g = lane / kPullGroup;
+  const uint32_t gfirst = g * kPullGroup;
+  const uint32_t gmask = ((1u << kPullGroup) - 1u) << gfirst;
+  const uint32_t W = gridDim.x * (kPullThreads / 32);
+  const uint32_t count = a.act ? *a.act_count : a.count;
+  const uint32_t sweep = a.epoch;
+  uint32_t b = blockIdx.x * (kPullThreads / 32) + threadIdx.x / 32;
+  // this group's position index in block bb
+  auto idx = [&](uint32_t bb) { return bb * kGroups + g; };
+  const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+  uint4 cur = z, n1 = z, n2 = z;
+  uint2 s[kPullRounds], ns[kPullRounds];
+  uint32_t p3 = 0;
+  if (idx(b) < count) cur = a.rec[pull_pos(a, idx(b))];
+  if (idx(b + W) < count) n1 = a.rec[pull_pos(a, idx(b + W))];
+  if (idx(b + 2 * W) < count) n2 = a.rec[pull_pos(a, idx(b + 2 * W))];
+  if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
+  load_slots(a, cur, gl, s);
+  if (idx(b + W) < count) load_slots(a, n1, gl, ns);
+  bool have = idx(b) < count;
+  unsigned long long solved = 0, attempts = 0, w0 = 0;
+  uint32_t wait_ns = 32;
+  while (b * kGroups < count) {
+    const uint32_t n_up = have ? rec_count(cur) : 0u;
+    unsigned long long w[kPullRounds];
+#pragma unroll
+    for (int r = 0; r < kPullRounds; ++r) w[r] = ld_relaxed_u64_if(gl + r * kPullGroup < n_up, a.qe + s[r].x);
+    float src = 0.f, per = 0.f, att = 0.f;
+    if (have && gl == 0) {
+      src = a.src_dir[cur.x];
+      per = __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x);
+      att = (float)a.att[cur.x];
+    }
+    float in = 0.f;
+    bool bad = false;
+#pragma unroll
+    for (int r = 0; r < kPullRounds; ++r) {
+      if (gl + r * kPullGroup < n_up) {
+        bad = bad || !word_current(w[r], sweep);
+        in = fmaf(__uint_as_float(s[r].y), __uint_as_float((uint32_t)w[r]), in);
+      }
+    }
+    for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
+      const uint2 sj = a.slots[rec_offset(cur) + j];
+      const unsigned long long wn = ld_relaxed_u64(a.qe + sj.x);
+      bad = bad || !word_current(wn, sweep);
+      in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
+    }
+    const uint32_t badmask = __ballot_sync(0xffffffffu, bad);
+#pragma unroll
+    for (int o = 1; o < kPullGroup; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, kPullGroup);
+    const bool commit = have && (badmask & gmask) == 0u;
+    if (have && gl == 0) ++attempts;
+    if (commit && gl == 0) {
+      const uint32_t t = rec_dir(cur) * a.Np + cur.x;
+      const float rt = (in + src) + per;                   // Site::get_rate, site.rs:53-56
+      const float out = (rt < a.threshold) ? 0.f : rt * att;  // get_outgoing_rate
+      a.incoming[t] = in;
+      st_relaxed_u64(a.qe + t, pack_qe(out * __uint_as_float(cur.y), sweep));
+      ++solved;
+    }
+    have = have && !commit;
+    const bool any_commit = __any_sync(0xffffffffu, commit);
+    if (!__any_sync(0xffffffffu, have)) {  // every group of the block done: advance the warp
+      b += W;
+      cur = n1;
+#pragma unroll
+      for (int r = 0; r < kPullRounds; ++r) s[r] = ns[r];
+      n1 = n2;
+      have = idx(b) < count;
+      if (idx(b + W) < count) load_slots(a, n1, gl, ns);
+      if (idx(b + 2 * W) < count) n2 = a.rec[p3];
+      if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
+    }
+    if (any_commit) {
+      w0 = 0;
+      wait_ns = 32;
+    } else {
+      int expired = 0;
+      if (lane == 0) {
+        const unsigned long long now = globaltimer_ns();
+        if (w0 == 0) w0 = now;
+        expired = (now - w0 > a.timeout_ns) || (*(volatile uint32_t*)&a.ctl->error != 0);
+      }
+      if (__shfl_sync(0xffffffffu, expired, 0)) {
+        if (lane == 0) atomicOr(&a.ctl->error, kErrStall);
+        break;
+      }
+      __nanosleep(wait_ns);
+      wait_ns = min(wait_ns * 2, 256u);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    solved += __shfl_xor_sync(0xffffffffu, solved, o);
+    attempts += __shfl_xor_sync(0xffffffffu, attempts, o);
+  }
+  if (lane == 0 && solved) atomicAdd(&a.ctl->tasks, solved);
+  if (lane == 0 && attempts) atomicAdd(&a.ctl->attempts, attempts);
+}
+
 // Gathered incoming rate of (c, d): sum over upwind LOCAL faces of |s| q(n, d), or
 // over LOCAL_PERIODIC faces when `periodic_faces`.
 __device__ __forceinline__ float gather_in(const PullArgs& a, uint32_t c, uint32_t d, bool periodic_faces) {
