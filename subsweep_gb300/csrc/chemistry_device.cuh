@@ -71,104 +71,73 @@ struct ChemSolver {
   __device__ __forceinline__ double n_neutral() const { return nh() * neutral(); }
   __device__ __forceinline__ double mu() const { return 1.0 / (x + 1.0); }
 
-  // 161-173
-  __device__ double collision_fit() const {
-    double t = temperature;
-    return sqrt(t) / (1.0 + sqrt(t / 1e5)) * exp(-157809.1 / t);
-  }
-  __device__ double collision_fit_derivative() const {
-    double c1 = 1.0 / 1e5, c2 = 157809.1, t = temperature;
-    double s = sqrt(c1 * t);
-    return (exp(-c2 / t) * (c1 * c2 * t + 0.5 * s * (2.0 * c2 + t))) /
-           (sqrt(t * t * t) * s * ((s + 1.0) * (s + 1.0)));
-  }
-  // 175-194
-  __device__ double case_b_rate() const {
-    double lambda = 315614.0 / temperature;
-    return (2.753e-14 * pow(lambda, 1.5) / pow(1.0 + pow(lambda / 2.74, 0.407), 2.242)) *
-           Units::kCentimetersCubedPerS;
-  }
-  __device__ double case_b_rate_derivative() const {
-    double lambda = 315614.0 / temperature;
-    double dlambda_dt = -315614.0 / (temperature * temperature);
-    double c1 = 1.0 / 2.74, c2 = 0.407, c3 = 2.242;
-    double p = pow(c1 * lambda, c2);
-    double d = -sqrt(lambda) * pow(p + 1.0, -c3 - 1.0) * (c2 * c3 * p - 1.5 * p - 1.5);
-    return ((2.753e-14 * d) * Units::kCentimetersCubedPerS) * dlambda_dt;
-  }
-  // 196-216
-  __device__ double case_b_cooling() const {
-    double lambda = 315614.0 / temperature;
-    return (3.435e-30 * temperature * pow(lambda, 1.97) /
-            pow(1.0 + pow(lambda / 2.25, 0.376), 3.72)) *
-           Units::kErgsCentimetersCubedPerS;
-  }
-  __device__ double case_b_cooling_derivative() const {
-    const double c1 = 315614.0, c2 = 1.97, c3 = 0.376, c4 = 3.72, c5 = 2.25;
-    double t = temperature;
-    double q = pow(c1 / (c5 * t), c3);
-    double derivative = pow(1.0 + q, -1.0 - c4) * (1.0 - 1.0 * c2 + (1.0 - 1.0 * c2 + c3 * c4) * q) *
-                        pow(c1 / t, c2);
-    return (3.435e-30 * derivative) * Units::kErgsCentimetersCubedPerS;
-  }
-  // 237-253
-  __device__ double excitation_cooling() const {
-    double t = temperature;
-    return (7.5e-19 / (1.0 + sqrt(t / 1e5)) * exp(-118348.0 / t)) *
-           Units::kErgsCentimetersCubedPerS;
-  }
-  __device__ double excitation_cooling_derivative() const {
-    double t = temperature;
-    const double c1 = 7.5e-19, c2 = 118348.0, c3 = 1.0 / 1e5;
-    double s = sqrt(c3 * t);
-    double v = (c1 * exp(-c2 / t) * (c2 * c3 * t - 0.5 * c3 * (t * t) + c2 * s)) /
-               ((t * t) * s * ((1.0 + s) * (1.0 + s)));
-    return v * Units::kErgsCentimetersCubedPerS;
-  }
-  // 265-273
-  __device__ double compton_cooling() const {
-    double xx = 2.727 / scale_factor;
-    double x2 = xx * xx;
-    return (1.017e-37 * (x2 * x2) * (temperature - xx)) * Units::kErgsPerS;
-  }
-  __device__ double compton_cooling_derivative() const {
-    double xx = 2.727 / scale_factor;
-    double x2 = xx * xx;
-    return (1.017e-37 * (x2 * x2)) * Units::kErgsPerS;
+  // The rate fits and their temperature derivatives (161-302) share their powers and
+  // exponentials: each derivative below is the reference's formula with the common
+  // factor taken from the fit evaluated at the same temperature
+  // ((1 + p)^(-c - 1) = 1 / ((1 + p)^c (1 + p)), lambda^1.5 = lambda sqrt(lambda)).
+  // The values agree with separate evaluation to rounding.
+
+  // collision_fit 161-166 and collision_fit_derivative 167-173
+  __device__ static void collision_fits(double t, double sqrt_t, double s5, double& fit, double& fitd) {
+    const double c1 = 1.0 / 1e5, c2 = 157809.1;
+    const double e = exp(-c2 / t);
+    fit = sqrt_t / (1.0 + s5) * e;
+    fitd = (e * (c1 * c2 * t + 0.5 * s5 * (2.0 * c2 + t))) / ((t * sqrt_t) * s5 * ((s5 + 1.0) * (s5 + 1.0)));
   }
 
-  // cooling_rate 275-287 and cooling_rate_derivative 289-302, evaluated together
-  // (the collision fit is shared by the ionization-cooling term of both).
+  // cooling_rate 275-287 and cooling_rate_derivative 289-302 at the current temperature:
+  // collisional ionization / excitation cooling (237-253), case B recombination cooling
+  // (196-216), bremsstrahlung and Compton cooling (265-273).
   __device__ void cooling(double& lambda_c, double& dlambda_c) const {
-    double ne = n_ionized();
-    double nhn = n_neutral();
-    double nhi = n_ionized();
-    double fit = collision_fit();
-    double fitd = collision_fit_derivative();
-    double sq = sqrt(temperature);
-    double coll = (excitation_cooling() + (1.27e-21 * fit) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
-    double recomb = case_b_cooling() * ne * nhi;
-    double brems = ((1.42e-27 * sq) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
-    double compton = compton_cooling() * ne;
-    lambda_c = coll + recomb + brems + compton;
-    double dcoll = (excitation_cooling_derivative() +
-                    (1.27e-21 * fitd) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
-    double drecomb = case_b_cooling_derivative() * ne * nhi;
-    double dbrems = ((1.42e-27 / (2.0 * sq)) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
-    double dcompton = compton_cooling_derivative() * ne;
-    dlambda_c = dcoll + drecomb + dbrems + dcompton;
+    const double t = temperature;
+    const double ne = n_ionized();
+    const double nhn = n_neutral();
+    const double nhi = n_ionized();
+    const double sq = sqrt(t);
+    const double s5 = sqrt(t / 1e5);
+    double fit, fitd;
+    collision_fits(t, sq, s5, fit, fitd);
+    // excitation cooling and its derivative
+    const double e_exc = exp(-118348.0 / t);
+    const double exc = (7.5e-19 / (1.0 + s5) * e_exc) * Units::kErgsCentimetersCubedPerS;
+    const double c3 = 1.0 / 1e5, c2e = 118348.0;
+    const double dexc = ((7.5e-19 * e_exc * (c2e * c3 * t - 0.5 * c3 * (t * t) + c2e * s5)) /
+                         ((t * t) * s5 * ((1.0 + s5) * (1.0 + s5)))) *
+                        Units::kErgsCentimetersCubedPerS;
+    // case B recombination cooling and its derivative
+    const double lambda = 315614.0 / t;
+    const double l197 = pow(lambda, 1.97);
+    const double q = pow(lambda / 2.25, 0.376);
+    const double a = pow(1.0 + q, 3.72);
+    const double recomb_rate = (3.435e-30 * t * l197 / a) * Units::kErgsCentimetersCubedPerS;
+    const double c2r = 1.97, c3r = 0.376, c4r = 3.72;
+    const double drecomb_rate = (3.435e-30 * ((1.0 / (a * (1.0 + q))) *
+                                             (1.0 - 1.0 * c2r + (1.0 - 1.0 * c2r + c3r * c4r) * q) * l197)) *
+                                Units::kErgsCentimetersCubedPerS;
+    // Compton
+    const double xx = 2.727 / scale_factor;
+    const double x2 = xx * xx;
+    const double compton = (1.017e-37 * (x2 * x2) * (t - xx)) * Units::kErgsPerS;
+    const double dcompton = (1.017e-37 * (x2 * x2)) * Units::kErgsPerS;
+
+    const double coll = (exc + (1.27e-21 * fit) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
+    const double recomb = recomb_rate * ne * nhi;
+    const double brems = ((1.42e-27 * sq) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
+    lambda_c = coll + recomb + brems + compton * ne;
+    const double dcoll = (dexc + (1.27e-21 * fitd) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
+    const double drecomb = drecomb_rate * ne * nhi;
+    const double dbrems = ((1.42e-27 / (2.0 * sq)) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
+    dlambda_c = dcoll + drecomb + dbrems + dcompton * ne;
   }
 
-  // 312-319
-  __device__ double newly_ionized(double timestep) const {
-    double absorbed = 1.0 - exp(-n_neutral() * Units::kSigma * length);
-    double num_photons = timestep * rate;
-    return num_photons * absorbed;
-  }
+  // 312-319: photons absorbed per photon arriving, 1 - exp(-n_HI sigma size); both
+  // updates of an attempt use it with the x of the attempt's start
+  __device__ double absorbed_fraction() const { return 1.0 - exp(-n_neutral() * Units::kSigma * length); }
+
   // 304-310 (+ photoheating_rate 321-325)
-  __device__ double temperature_change(double timestep) const {
+  __device__ double temperature_change(double timestep, double absorbed) const {
     double k = (Units::kGamma - 1.0) * Units::kProtonMass / (density * Units::kBoltzmann);
-    double heating = (newly_ionized(timestep) / volume) *
+    double heating = ((timestep * rate * absorbed) / volume) *
                      (Units::kPhotonAverageEnergy - Units::kRydberg) / timestep;
     double lc, dlc;
     cooling(lc, dlc);
@@ -177,23 +146,35 @@ struct ChemSolver {
     double m = mu();
     return k * m * lambda * timestep / (1.0 - k * m * dlambdadt * timestep);
   }
-  // 334-354 (+ photoionization_rate 327-332)
-  __device__ double ionized_fraction_change(double timestep) const {
+  // 334-354 (+ photoionization_rate 327-332), case B rate 175-194 at the current
+  // (already updated) temperature
+  __device__ double ionized_fraction_change(double timestep, double absorbed) const {
+    const double t = temperature;
     double n_h = nh();
     double ne = n_ionized();
-    double alpha = case_b_rate();
-    double dalpha = case_b_rate_derivative();
-    double fit = collision_fit();
+    const double lambda = 315614.0 / t;
+    const double dlambda_dt = -315614.0 / (t * t);
+    const double sl = sqrt(lambda);
+    const double p = pow(lambda / 2.74, 0.407);
+    const double b = pow(1.0 + p, 2.242);
+    const double alpha = (2.753e-14 * (lambda * sl) / b) * Units::kCentimetersCubedPerS;
+    const double c2a = 0.407, c3a = 2.242;
+    const double da = -sl * (1.0 / (b * (p + 1.0))) * (c2a * c3a * p - 1.5 * p - 1.5);
+    const double dalpha = ((2.753e-14 * da) * Units::kCentimetersCubedPerS) * dlambda_dt;
+    const double sq = sqrt(t);
+    const double s5 = sqrt(t / 1e5);
+    double fit, fitd;
+    collision_fits(t, sq, s5, fit, fitd);
     double beta = (5.85e-11 * fit) * Units::kCentimetersCubedPerS;
-    double dbeta = (5.85e-11 * collision_fit_derivative()) * Units::kCentimetersCubedPerS;
-    double photo = (newly_ionized(timestep) / (n_neutral() * volume)) / timestep;
+    double dbeta = (5.85e-11 * fitd) * Units::kCentimetersCubedPerS;
+    double photo = (((timestep * rate) * absorbed) / (n_neutral() * volume)) / timestep;
     double c = beta * ne + photo;
     double m = mu();
     double d = alpha * ne;
     double xhii = x;
-    double rhsc = ne * temperature * m * 1.0 * dbeta;
+    double rhsc = ne * t * m * 1.0 * dbeta;
     double dcdx = n_h * beta - rhsc;
-    double rhsd = ne * temperature * m * 1.0 * dalpha;
+    double rhsd = ne * t * m * 1.0 * dalpha;
     double dddx = n_h * alpha - rhsd;
     double j = dcdx - (c + d) - xhii * (dcdx + dddx);
     return timestep * (c - xhii * (c + d)) / (1.0 - j * timestep);
@@ -225,11 +206,12 @@ struct ChemSolver {
 
   // try_timestep_update 371-392
   __device__ bool try_update(double timestep, double safety, Timescale& out) {
-    double tc = temperature_change(timestep);
+    const double absorbed = absorbed_fraction();
+    double tc = temperature_change(timestep, absorbed);
     double rec_t;
     if (!accept(temperature, tc, safety, timestep, rec_t)) return false;
     temperature += tc;
-    double xc = ionized_fraction_change(timestep);
+    double xc = ionized_fraction_change(timestep, absorbed);
     double rec_x;
     if (!accept(x, xc, safety, timestep, rec_x)) return false;
     x += xc;
