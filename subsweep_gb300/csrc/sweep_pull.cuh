@@ -22,6 +22,8 @@
 // itself reads precomputed per-position records and upwind slots (below).
 #pragma once
 
+#include <cuda/atomic>
+
 #include "sweep_device.cuh"
 
 namespace swk {
@@ -54,26 +56,21 @@ struct PullArgs {
   uint32_t count;             // number of positions when act is nullptr
 };
 
-// The words are only ever read and written whole and nothing else is ordered against
-// them inside a sweep, so the accesses need no memory clobber.
+// The words are only ever read and written whole (relaxed, device scope), and nothing
+// else is ordered against them inside a sweep.
+using WordRef = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
+
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
-  return v;
+  return WordRef(*const_cast<unsigned long long*>(p)).load(cuda::memory_order_relaxed);
 }
 
 // predicated form: returns 0 without touching memory when pred is false
 __device__ __forceinline__ unsigned long long ld_relaxed_u64_if(bool pred, const unsigned long long* p) {
-  unsigned long long v = 0;
-  asm volatile(
-      "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.relaxed.gpu.global.u64 %0, [%1];\n\t}"
-      : "+l"(v)
-      : "l"(p), "r"((uint32_t)pred));
-  return v;
+  return pred ? ld_relaxed_u64(p) : 0ull;
 }
 
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v));
+  WordRef(*p).store(v, cuda::memory_order_relaxed);
 }
 
 // {q, sweep << 1}: solved in `sweep`; {q, sweep << 1 | 1}: stamped (inactive in `sweep`)
@@ -548,6 +545,16 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   load_slots(a, cur, gl, s);
   if (idx(b + W) < count) load_slots(a, n1, gl, ns);
   bool have = idx(b) < count;
+  // the leader's cell data of the current task, loaded once per block
+  float src = 0.f, per = 0.f, att = 0.f;
+  auto load_cell = [&]() {
+    if (have && gl == 0) {
+      src = a.src_dir[cur.x];
+      per = __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x);
+      att = (float)a.att[cur.x];
+    }
+  };
+  load_cell();
   unsigned long long solved = 0, attempts = 0, w0 = 0;
   uint32_t wait_ns = 32;
   while (b * kGroups < count) {
@@ -555,12 +562,6 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
     unsigned long long w[kPullRounds];
 #pragma unroll
     for (int r = 0; r < kPullRounds; ++r) w[r] = ld_relaxed_u64_if(gl + r * kPullGroup < n_up, a.qe + s[r].x);
-    float src = 0.f, per = 0.f, att = 0.f;
-    if (have && gl == 0) {
-      src = a.src_dir[cur.x];
-      per = __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x);
-      att = (float)a.att[cur.x];
-    }
     float in = 0.f;
     bool bad = false;
 #pragma unroll
@@ -601,6 +602,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
       if (idx(b + W) < count) load_slots(a, n1, gl, ns);
       if (idx(b + 2 * W) < count) n2 = a.rec[p3];
       if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
+      load_cell();
     }
     if (any_commit) {
       w0 = 0;
