@@ -162,6 +162,33 @@ sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double*
 
 sw_status sw_get_stats(sw_handle* h, sw_stats* out);
 
+/* Global averages of the current state as the reference's time-series systems report
+ * them (compute_time_series_system, src/sweep/time_series.rs:61-155), reduced on the
+ * device: cell mass = density * volume (src/main.rs:195-203); a cell's photoionization
+ * rate is Solver::photoionization_rate over one year (src/sweep/chemistry_output.rs:15-28)
+ * with the rate summed over directions as Sweep::get_solver forms it
+ * (src/sweep/mod.rs:613-631).  Copies 48 bytes to the host, nothing per cell. */
+typedef struct {
+  double hydrogen_ionization_mass_average;
+  double hydrogen_ionization_volume_average;
+  double temperature_mass_average;       /* K */
+  double temperature_volume_average;     /* K */
+  double photoionization_rate_volume_average;           /* 1/s */
+  double weighted_photoionization_rate_volume_average;  /* 1/s, weighted by x_HII */
+} sw_time_series;
+sw_status sw_get_time_series(sw_handle* h, sw_time_series* out);
+
+/* Checkpoint and restart of the evolving state (no counterpart in the reference, which
+ * only remaps initial conditions): per-cell species, timestep levels, previous rates,
+ * change timescales, ionization times; the per-(cell, direction) transport state of the
+ * handle's precision; TimestepState, simulation time and sweep counter.  The grid,
+ * parameters and precision are not stored: load into a handle created from the same
+ * inputs (checked through cell, face, direction and level counts).  Statistics are not
+ * part of the state.  sw_checkpoint_size gives the buffer size in bytes. */
+sw_status sw_checkpoint_size(sw_handle* h, size_t* bytes);
+sw_status sw_save_state(sw_handle* h, void* buffer, size_t bytes);
+sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes);
+
 /* Same result as sw_get_dependency_counts, for callers that cannot allocate device
  * memory (a host engine whose GPU memory is owned by its own pool, code that must not
  * trigger the synchronisation cudaMalloc/cudaFree can cause): it stages the counts in

@@ -32,6 +32,12 @@ class OrcParams(ctypes.Structure):
                 ("prevent_cooling", c_int32), ("scale_factor", c_double), ("periodic_mode", c_int32)]
 
 
+# names of the reference's time-series outputs (src/sweep/time_series.rs:26-48)
+TIME_SERIES_NAMES = ("hydrogen_ionization_mass_average", "hydrogen_ionization_volume_average",
+                     "temperature_mass_average", "temperature_volume_average",
+                     "photoionization_rate_volume_average", "weighted_photoionization_rate_volume_average")
+
+
 def build() -> pathlib.Path:
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB
@@ -54,6 +60,7 @@ def load() -> ctypes.CDLL:
     lib.orc_sim_step.restype = ctypes.c_int
     lib.orc_sim_get_fields.argtypes = [c_void_p] + [c_void_p] * 6
     lib.orc_sim_get_rates.argtypes = [c_void_p] + [c_void_p] * 3
+    lib.orc_sim_time_series.argtypes = [c_void_p, c_void_p]
     lib.orc_sim_init_counts.argtypes = [c_void_p, c_int32, c_void_p]
     lib.orc_sim_init_counts.restype = c_int64
     lib.orc_sim_level_counts.argtypes = [c_void_p, c_void_p]
@@ -148,6 +155,11 @@ class OracleSweep:
         inc, outg, per = np.empty(shape), np.empty(shape), np.empty(shape)
         self._lib.orc_sim_get_rates(self._h, inc.ctypes.data, outg.ctypes.data, per.ctypes.data)
         return {"incoming": inc, "outgoing": outg, "periodic": per}
+
+    def time_series(self) -> dict:
+        out = np.empty(6)
+        self._lib.orc_sim_time_series(self._h, out.ctypes.data)
+        return dict(zip(TIME_SERIES_NAMES, (float(v) for v in out)))
 
     def dependency_counts(self, level: int) -> np.ndarray:
         out = np.zeros((self.num_cells, self.num_directions), np.uint8)

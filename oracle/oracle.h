@@ -74,6 +74,9 @@ void orc_sim_get_fields(const orc_sim* s, double* xhii, double* temperature, dou
                         double* rate, double* change_timescale, uint8_t* level);
 /* Per-(cell,dir) transport state, [cell][dir] layout.  Any pointer may be NULL. */
 void orc_sim_get_rates(const orc_sim* s, double* incoming, double* outgoing, double* periodic);
+/* time series (src/sweep/time_series.rs:61-155): mass / volume averaged x_HII, mass /
+   volume averaged T, volume averaged photoionization rate and its x_HII-weighted form */
+void orc_sim_time_series(const orc_sim* s, double* out6);
 /* Dependency counts of Sweep::init_counts (mod.rs:346-386) for the given level with the
  * current cell levels: out[cell*D + dir] (0 for inactive cells); returns #active cells. */
 int64_t orc_sim_init_counts(const orc_sim* s, int32_t level, uint8_t* out);

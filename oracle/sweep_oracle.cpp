@@ -588,6 +588,49 @@ void orc_sim_get_fields(const orc_sim* s, double* xhii, double* temperature, dou
   }
 }
 
+// Time series of the sweep (src/sweep/time_series.rs:61-155) at the current state:
+// out[0] mass-averaged and out[1] volume-averaged ionized hydrogen fraction, out[2]
+// mass- and out[3] volume-averaged temperature, out[4] volume-averaged
+// photoionization rate and out[5] the same weighted by the ionized fraction.  The
+// cell mass is density * volume (main.rs:195-203); a cell's photoionization rate is
+// Solver::photoionization_rate over one year (chemistry_output.rs:15-28) of the solver
+// that get_solver builds (mod.rs:613-631: the rate summed over directions, no floor).
+// Each sum runs over the cells in order, as compute_global_sum does on one rank.
+void orc_sim_time_series(const orc_sim* s, double* out) {
+  const double year = 3.15576e7;  // units/mod.rs: one year in seconds
+  double ionized_mass = 0.0, total_mass = 0.0, ionized_volume = 0.0, total_volume = 0.0;
+  double mass_weighted_t = 0.0, volume_weighted_t = 0.0, volume_weighted_rate = 0.0, weighted_rate = 0.0;
+  for (int64_t c = 0; c < s->n; ++c) {
+    const double mass = s->density[c] * s->volume[c];
+    double rate = 0.0;
+    for (int32_t d = 0; d < s->D; ++d) rate += s->get_rate(c, d);
+    Solver sv;
+    sv.x = s->xhii[c];
+    sv.temperature = s->temperature[c];
+    sv.density = s->density[c];
+    sv.volume = s->volume[c];
+    sv.length = s->size[c];
+    sv.rate = rate;
+    sv.scale_factor = s->p.scale_factor;
+    sv.has_floor = false;
+    const double gamma = sv.photoionization_rate(year);
+    ionized_mass += mass * s->xhii[c];
+    total_mass += mass;
+    ionized_volume += s->volume[c] * s->xhii[c];
+    total_volume += s->volume[c];
+    mass_weighted_t += s->temperature[c] * mass;
+    volume_weighted_t += s->temperature[c] * s->volume[c];
+    volume_weighted_rate += gamma * s->volume[c];
+    weighted_rate += gamma * s->xhii[c] * s->volume[c];
+  }
+  out[0] = ionized_mass / total_mass;
+  out[1] = ionized_volume / total_volume;
+  out[2] = mass_weighted_t / total_mass;
+  out[3] = volume_weighted_t / total_volume;
+  out[4] = volume_weighted_rate / total_volume;
+  out[5] = weighted_rate / total_volume;
+}
+
 void orc_sim_get_rates(const orc_sim* s, double* incoming, double* outgoing, double* periodic) {
   size_t nd = s->incoming.size();
   if (incoming) std::memcpy(incoming, s->incoming.data(), nd * sizeof(double));

@@ -33,6 +33,7 @@ ABI_SYMBOLS = (
     "sw_default_params", "sw_directions_from_num", "sw_create", "sw_step", "sw_get_fields",
     "sw_get_cell_state", "sw_set_fields", "sw_get_level_counts", "sw_get_dependency_counts",
     "sw_get_rates", "sw_get_stats", "sw_last_error", "sw_destroy", "sw_get_dependency_counts_noalloc",
+    "sw_get_time_series", "sw_checkpoint_size", "sw_save_state", "sw_load_state",
 )
 
 
@@ -76,6 +77,13 @@ class SwCellInit(ctypes.Structure):
         ("temperature", c_void_p),
         ("source", c_void_p),
     ]
+
+
+class SwTimeSeries(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_double) for name in (
+        "hydrogen_ionization_mass_average", "hydrogen_ionization_volume_average",
+        "temperature_mass_average", "temperature_volume_average",
+        "photoionization_rate_volume_average", "weighted_photoionization_rate_volume_average")]
 
 
 class SwStats(ctypes.Structure):
@@ -132,6 +140,10 @@ def load_gpu() -> ctypes.CDLL:
     lib.sw_get_rates.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
     lib.sw_get_dependency_counts_noalloc.argtypes = [c_void_p, c_int32, c_void_p]
     lib.sw_get_stats.argtypes = [c_void_p, ctypes.POINTER(SwStats)]
+    lib.sw_get_time_series.argtypes = [c_void_p, ctypes.POINTER(SwTimeSeries)]
+    lib.sw_checkpoint_size.argtypes = [c_void_p, ctypes.POINTER(ctypes.c_size_t)]
+    lib.sw_save_state.argtypes = [c_void_p, c_void_p, ctypes.c_size_t]
+    lib.sw_load_state.argtypes = [c_void_p, c_void_p, ctypes.c_size_t]
     lib.sw_last_error.argtypes = [c_void_p]
     lib.sw_last_error.restype = ctypes.c_char_p
     lib.sw_destroy.argtypes = [c_void_p]

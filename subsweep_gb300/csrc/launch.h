@@ -67,6 +67,8 @@ struct DevicePtrs {
   void* pull_slots;          // pull path: uint2 upwind slots of all positions
   uint32_t* act;             // pull path: compacted active positions of the current sweep
   uint32_t* chunk;           // pull path: compaction chunk offsets, count at [num_chunks]
+  int64_t active_cells;      // pull path: cells active in the sweep being launched
+  int compact_mode;          // pull path: 0 by density, 1 always compact, 2 never (lockstep)
   int level_blocks;          // resident blocks of the levelled kernel
   const uint32_t* periodic_cells;
   uint32_t n_periodic_cells;
@@ -100,6 +102,10 @@ struct PrecisionOps {
   // chunk_off[num_chunks]); phase 1, with pull_slots allocated, writes the slots.
   // nullptr on the push path.
   cudaError_t (*records)(const DevicePtrs&, int phase, unsigned long long* chunk_off, cudaStream_t);
+  // rate of every cell summed over directions (incoming + source/D + periodic),
+  // photons/s
+  cudaError_t (*cell_rates)(const DevicePtrs&, uint32_t last_epoch, double* out, cudaStream_t);
+  bool carry_neutral;  // the chemistry carries 1 - x_HII as its own state (yneu)
 };
 
 extern const PrecisionOps kOpsFP64;
@@ -125,5 +131,10 @@ cudaError_t launch_update_levels(const DevicePtrs&, int lowest_allowed, cudaStre
 cudaError_t launch_level_hist(const DevicePtrs&, cudaStream_t);
 cudaError_t launch_ionization_time(const DevicePtrs&, double time, cudaStream_t);
 cudaError_t launch_schedule_scatter(const DevicePtrs&, const uint16_t* task_level, uint32_t* cursor, cudaStream_t);
+// Time series from per-cell summed rates: `partial` holds kTimeSeriesPartials doubles,
+// `out6` receives the six averages (device memory).
+constexpr int kTimeSeriesPartials = 256 * 8;
+cudaError_t launch_time_series(const DevicePtrs&, const double* cell_rate, bool carry_neutral, double* partial,
+                               double* out6, cudaStream_t);
 
 }  // namespace swh

@@ -830,6 +830,80 @@ __global__ void k_photon_rate(uint32_t n, const R* incoming, int D, uint32_t Np,
   }
 }
 
+// Rate of every cell summed over directions as Sweep::get_solver forms it
+// (src/sweep/mod.rs:616-620): sum over d of get_rate(d) = (incoming + source/D) +
+// periodic (site.rs:53-56), in photons/s.
+template <typename R>
+__global__ void k_cell_rates(uint32_t n, const R* incoming, const R* periodic, const R* src_dir, int D, uint32_t Np,
+                             double rate_scale, double* out) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    double r = 0.0;
+    for (int d = 0; d < D; ++d) {
+      const size_t t = (size_t)d * Np + c;
+      r += ((double)incoming[t] + (double)src_dir[c]) + (double)periodic[t];
+    }
+    out[c] = r * rate_scale;
+  }
+}
+
+// Time series of the sweep (src/sweep/time_series.rs:61-155), two stages with a fixed
+// grid so the sums are deterministic: per-block partial sums of
+//   [0] mass * x, [1] mass, [2] volume * x, [3] volume, [4] T * mass, [5] T * volume,
+//   [6] Gamma * volume, [7] Gamma * x * volume,
+// with mass = density * volume (main.rs:195-203) and Gamma the photoionization rate
+// over one year of the cell's solver (chemistry_output.rs:15-28, hydrogen_only/mod.rs
+// 312-332), then the ratios.  `yneu`, when given, is the carried neutral fraction.
+constexpr int kSeriesThreads = 256;
+constexpr int kSeriesBlocks = 256;
+constexpr int kSeriesSums = 8;
+
+static __global__ void __launch_bounds__(kSeriesThreads) k_time_series_partial(
+    uint32_t n, const double* density, const double* volume, const double* size, const double* xhii,
+    const double* yneu, const double* temperature, const double* cell_rate, double* partial) {
+  const double year = 3.15576e7;  // units/mod.rs: one year in seconds
+  double acc[kSeriesSums] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const double x = xhii[c], v = volume[c], t = temperature[c];
+    const double mass = density[c] * v;
+    const double neutral = yneu ? yneu[c] : 1.0 - x;
+    const double nhn = density[c] / Units::kProtonMass * neutral;
+    const double absorbed = 1.0 - exp(-nhn * Units::kSigma * size[c]);
+    const double num = (year * cell_rate[c]) * absorbed;
+    const double gamma = (num / (nhn * v)) / year;
+    acc[0] += mass * x;
+    acc[1] += mass;
+    acc[2] += v * x;
+    acc[3] += v;
+    acc[4] += t * mass;
+    acc[5] += t * v;
+    acc[6] += gamma * v;
+    acc[7] += gamma * x * v;
+  }
+  __shared__ double sh[kSeriesSums][kSeriesThreads];
+  for (int k = 0; k < kSeriesSums; ++k) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int stride = kSeriesThreads / 2; stride > 0; stride >>= 1) {
+    if ((int)threadIdx.x < stride)
+      for (int k = 0; k < kSeriesSums; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + stride];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < kSeriesSums; ++k) partial[blockIdx.x * kSeriesSums + k] = sh[k][0];
+}
+
+static __global__ void k_time_series_final(const double* partial, int blocks, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s[kSeriesSums] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < blocks; ++b)
+    for (int k = 0; k < kSeriesSums; ++k) s[k] += partial[b * kSeriesSums + k];
+  out[0] = s[0] / s[1];
+  out[1] = s[2] / s[3];
+  out[2] = s[4] / s[1];
+  out[3] = s[5] / s[3];
+  out[4] = s[6] / s[3];
+  out[5] = s[7] / s[3];
+}
+
 // Convert a per-task array to FP64 photons/s in [cell][D] layout.
 template <typename R>
 __global__ void k_export_rates(uint32_t n, const R* src, int D, uint32_t Np, double rate_scale, double* out) {

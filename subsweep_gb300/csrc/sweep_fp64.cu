@@ -42,6 +42,16 @@ cudaError_t launch_schedule_scatter(const DevicePtrs& p, const uint16_t* task_le
   return cudaGetLastError();
 }
 
+cudaError_t launch_time_series(const DevicePtrs& p, const double* cell_rate, bool carry_neutral, double* partial,
+                               double* out6, cudaStream_t s) {
+  static_assert(kTimeSeriesPartials == swk::kSeriesBlocks * swk::kSeriesSums, "partial buffer size");
+  swk::k_time_series_partial<<<swk::kSeriesBlocks, swk::kSeriesThreads, 0, s>>>(
+      (uint32_t)p.num_cells, p.density, p.volume, p.size, p.xhii, carry_neutral ? p.yneu : nullptr, p.temperature,
+      cell_rate, partial);
+  swk::k_time_series_final<<<1, 32, 0, s>>>(partial, swk::kSeriesBlocks, out6);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ionization_time(const DevicePtrs& p, double time, cudaStream_t s) {
   swk::k_ionization_time<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.xhii,
                                                                      p.ionization_time, time);

@@ -92,6 +92,7 @@ struct sw_handle {
   int64_t stats_upwind_slots = 0;
   int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
   bool trace = false;  // SUBSWEEP_TRACE: one stderr line per level sweep
+  double* series_dev = nullptr;  // time-series partial sums and result (allocated on first use)
   uint32_t last_epoch = 0;  // pull path: sweep number of the last sweep of the last step
 
   ~sw_handle() {
@@ -546,6 +547,12 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (std::strcmp(env, "levels") == 0) h->force_path = 1;
     if (std::strcmp(env, "queue") == 0) h->force_path = 2;
   }
+  // SUBSWEEP_COMPACT=always|never overrides the mixed path's choice between compacting
+  // the active positions and stamping inactive tasks in the sweep (tests and tuning).
+  if (const char* env = std::getenv("SUBSWEEP_COMPACT")) {
+    if (std::strcmp(env, "always") == 0) p.compact_mode = 1;
+    if (std::strcmp(env, "never") == 0) p.compact_mode = 2;
+  }
   // SUBSWEEP_TRACE=1 prints one line per level sweep to stderr (level, active tasks,
   // transport kernel / transport / chemistry milliseconds, transport attempts).
   if (const char* env = std::getenv("SUBSWEEP_TRACE")) h->trace = env[0] != '\0' && env[0] != '0';
@@ -804,7 +811,9 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
       levelled = true;  // the pull path always walks the schedule (or the id order)
       h->p.epoch += 1;
       h->last_epoch = h->p.epoch;
-      if (level > 0) launches += 3;  // compaction of the active positions
+      h->p.active_cells = h->n_ge_host[level];
+      if (level > 0 && (h->p.compact_mode == 1 || (h->p.compact_mode == 0 && h->p.active_cells * 2 < h->N)))
+        launches += 3;  // compaction of the active positions
     } else {
       SW_CUDA(h, ops.init_counts(h->p, level, nullptr, !levelled, h->stream), "init_counts kernel");
       launches += 1;
@@ -963,6 +972,138 @@ sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double*
   }
   cudaFree(d_out);
   if (e != cudaSuccess) return h->cuda_fail(e, "export rates");
+  return SW_OK;
+}
+
+// Checkpoint layout: a header, then the device arrays of checkpoint_sections in order.
+struct CheckpointHeader {
+  uint64_t magic;
+  uint32_t version, precision;
+  int64_t num_cells, num_faces;
+  int32_t num_directions, num_levels;
+  uint32_t np, rate_bytes;
+  double sim_time;
+  int32_t ts_lowest, ts_first_done;
+  uint32_t epoch, last_epoch;
+};
+constexpr uint64_t kCheckpointMagic = 0x3154504357535553ull;  // "SUSWCPT1"
+
+struct CheckpointSection {
+  void* dev;
+  size_t bytes;
+};
+
+static std::vector<CheckpointSection> checkpoint_sections(sw_handle* h) {
+  const swh::DevicePtrs& p = h->p;
+  const size_t n = (size_t)h->N, nd = (size_t)h->Np * h->D, rb = (size_t)h->ops->rate_bytes;
+  std::vector<CheckpointSection> v = {
+      {p.xhii, n * 8},           {p.yneu, n * 8},          {p.temperature, n * 8}, {p.previous_rate, n * 8},
+      {p.change_timescale, n * 8}, {p.species_timestep, n * 8}, {p.ionization_time, n * 8}, {p.level, n},
+      {p.incoming, nd * rb},     {p.periodic, nd * rb},
+  };
+  if (h->ops->pull) {
+    v.push_back({p.qe, nd * 8});
+  } else {
+    v.push_back({p.outgoing, nd * rb});
+    v.push_back({p.pending, nd * rb});
+  }
+  return v;
+}
+
+static size_t checkpoint_bytes(sw_handle* h) {
+  size_t total = sizeof(CheckpointHeader);
+  for (const CheckpointSection& s : checkpoint_sections(h)) total += s.bytes;
+  return total;
+}
+
+sw_status sw_checkpoint_size(sw_handle* h, size_t* bytes) {
+  if (!h || !bytes) return SW_ERR_INVALID_ARG;
+  *bytes = checkpoint_bytes(h);
+  return SW_OK;
+}
+
+sw_status sw_save_state(sw_handle* h, void* buffer, size_t bytes) {
+  if (!h || !buffer) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  if (bytes < checkpoint_bytes(h)) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
+  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  CheckpointHeader hd{};
+  hd.magic = kCheckpointMagic;
+  hd.version = 1;
+  hd.precision = (uint32_t)h->params.precision;
+  hd.num_cells = h->N;
+  hd.num_faces = h->E;
+  hd.num_directions = h->D;
+  hd.num_levels = h->L;
+  hd.np = h->Np;
+  hd.rate_bytes = (uint32_t)h->ops->rate_bytes;
+  hd.sim_time = h->sim_time;
+  hd.ts_lowest = h->ts.lowest;
+  hd.ts_first_done = h->ts.first_done ? 1 : 0;
+  hd.epoch = h->p.epoch;
+  hd.last_epoch = h->last_epoch;
+  char* out = static_cast<char*>(buffer);
+  std::memcpy(out, &hd, sizeof(hd));
+  size_t off = sizeof(hd);
+  for (const CheckpointSection& s : checkpoint_sections(h)) {
+    SW_CUDA(h, cudaMemcpyAsync(out + off, s.dev, s.bytes, cudaMemcpyDeviceToHost, h->stream), "save state");
+    off += s.bytes;
+  }
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "save state");
+  return SW_OK;
+}
+
+sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes) {
+  if (!h || !buffer) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  if (bytes < sizeof(CheckpointHeader)) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
+  CheckpointHeader hd;
+  std::memcpy(&hd, buffer, sizeof(hd));
+  if (hd.magic != kCheckpointMagic || hd.version != 1) return h->fail(SW_ERR_INVALID_ARG, "not a checkpoint");
+  if (hd.precision != (uint32_t)h->params.precision || hd.num_cells != h->N || hd.num_faces != h->E ||
+      hd.num_directions != h->D || hd.num_levels != h->L || hd.np != h->Np ||
+      hd.rate_bytes != (uint32_t)h->ops->rate_bytes)
+    return h->fail(SW_ERR_INVALID_ARG, "checkpoint was written by a handle with another grid, parameters or precision");
+  if (bytes < checkpoint_bytes(h)) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
+  if (hd.ts_lowest < 0 || hd.ts_lowest >= h->L) return h->fail(SW_ERR_INVALID_ARG, "corrupt checkpoint header");
+  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  const char* in = static_cast<const char*>(buffer);
+  size_t off = sizeof(hd);
+  for (const CheckpointSection& s : checkpoint_sections(h)) {
+    SW_CUDA(h, cudaMemcpyAsync(s.dev, in + off, s.bytes, cudaMemcpyHostToDevice, h->stream), "load state");
+    off += s.bytes;
+  }
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "load state");
+  h->sim_time = hd.sim_time;
+  h->ts.lowest = hd.ts_lowest;
+  h->ts.first_done = hd.ts_first_done != 0;
+  h->p.epoch = hd.epoch;
+  h->last_epoch = hd.last_epoch;
+  // cells per level for the next step
+  SW_CUDA(h, swh::launch_level_hist(h->p, h->stream), "level histogram");
+  return sync_ctl(h);
+}
+
+sw_status sw_get_time_series(sw_handle* h, sw_time_series* out) {
+  if (!h || !out) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  if (!h->series_dev && !h->alloc(&h->series_dev, swh::kTimeSeriesPartials + 8))
+    return h->fail(SW_ERR_OOM, "device allocation of the time-series buffer failed");
+  double* partial = h->series_dev;
+  double* out6 = h->series_dev + swh::kTimeSeriesPartials;
+  SW_CUDA(h, h->ops->cell_rates(h->p, h->last_epoch, h->scratch, h->stream), "cell rate kernel");
+  SW_CUDA(h, swh::launch_time_series(h->p, h->scratch, h->ops->carry_neutral, partial, out6, h->stream),
+          "time series kernels");
+  double v[6];
+  SW_CUDA(h, cudaMemcpyAsync(v, out6, sizeof(v), cudaMemcpyDeviceToHost, h->stream), "read time series");
+  SW_CUDA(h, cudaStreamSynchronize(h->stream), "time series");
+  out->hydrogen_ionization_mass_average = v[0];
+  out->hydrogen_ionization_volume_average = v[1];
+  out->temperature_mass_average = v[2];
+  out->temperature_volume_average = v[3];
+  out->photoionization_rate_volume_average = v[4];
+  out->weighted_photoionization_rate_volume_average = v[5];
   return SW_OK;
 }
 

@@ -230,12 +230,20 @@ cudaError_t occupancy_pull(int* blocks_per_sm) {
                                                        swk::kPullThreads, 0);
 }
 
-// Sweeps above level 0 visit only the positions of active cells: a stable compaction of
-// the schedule (three launches) precedes the sweep kernel, which reads the count from
-// the device.
+// Sparse sweeps (above level 0, fewer than half of the cells active) visit only the
+// positions of active cells: a stable compaction of the schedule that also stamps the
+// inactive tasks' words (three launches) precedes the sweep kernel, which reads the
+// count from the device.  Dense sweeps visit every position; the kernel stamps the
+// inactive tasks itself.
 cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, level);
-  if (level > 0) {
+  const int variant = pull_variant();
+  // only the lockstep kernels test levels themselves
+  const bool lockstep = variant >= 90;
+  bool sparse = level > 0 && (p.active_cells * 2 < p.num_cells || !lockstep);
+  if (level > 0 && p.compact_mode == 1) sparse = true;
+  if (level > 0 && p.compact_mode == 2 && lockstep) sparse = false;
+  if (sparse) {
     const uint32_t nc = num_chunks(p);
     swk::k_compact_count<<<nc, swk::kCompactThreads, 0, s>>>(p.order, a.count, p.level, level, p.Np, p.chunk);
     swk::k_compact_scan<<<1, swk::kScanThreads, 0, s>>>(p.chunk, nc, p.chunk + nc);
@@ -247,8 +255,8 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
     a.act_count = p.chunk + nc;
   }
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel(pull_kernel(pull_variant()), dim3(p.level_blocks), dim3(swk::kPullThreads),
-                                     args, 0, s);
+  return cudaLaunchCooperativeKernel(pull_kernel(variant), dim3(p.level_blocks), dim3(swk::kPullThreads), args, 0,
+                                     s);
 }
 
 cudaError_t fold_pull(const DevicePtrs& p, cudaStream_t s) {
@@ -265,6 +273,12 @@ cudaError_t photon_rate(const DevicePtrs& p, uint32_t last_epoch, double* out, c
   return cudaGetLastError();
 }
 
+cudaError_t cell_rates(const DevicePtrs& p, uint32_t last_epoch, double* out, cudaStream_t s) {
+  swk::PullArgs a = pull_args(p, 0);
+  swk::k_cell_rates_pull<<<grid_for(p.num_cells, 128), 128, 0, s>>>(a, last_epoch, p.rate_scale, out);
+  return cudaGetLastError();
+}
+
 cudaError_t export_rates(const DevicePtrs& p, int which, uint32_t last_epoch, double* out, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, 0);
   swk::k_export_pull<<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(a, last_epoch, which, p.rate_scale, out);
@@ -274,6 +288,13 @@ cudaError_t export_rates(const DevicePtrs& p, int which, uint32_t last_epoch, do
 cudaError_t photon_rate(const DevicePtrs& p, uint32_t, double* out, cudaStream_t s) {
   swk::k_photon_rate<R><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
       (uint32_t)p.num_cells, static_cast<const R*>(p.incoming), p.D, p.Np, p.rate_scale, out);
+  return cudaGetLastError();
+}
+
+cudaError_t cell_rates(const DevicePtrs& p, uint32_t, double* out, cudaStream_t s) {
+  swk::k_cell_rates<R><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
+      (uint32_t)p.num_cells, static_cast<const R*>(p.incoming), static_cast<const R*>(p.periodic),
+      static_cast<const R*>(p.src_dir), p.D, p.Np, p.rate_scale, out);
   return cudaGetLastError();
 }
 
@@ -291,13 +312,13 @@ cudaError_t export_rates(const DevicePtrs& p, int which, uint32_t, double* out, 
 extern const PrecisionOps SWK_OPS = {
     SWK_NAME,       (int)sizeof(R), true,       occupancy,     attenuation, init_counts, sweep,
     occupancy_pull, sweep_pull,     kahn_round, schedule_seed, fold_pull,   chemistry,   photon_rate,
-    export_rates,   records,
+    export_rates,   records,        cell_rates, SWK_CARRY != 0,
 };
 #else
 extern const PrecisionOps SWK_OPS = {
     SWK_NAME,         (int)sizeof(R), false,      occupancy,     attenuation,   init_counts, sweep,
     occupancy_levels, sweep_levels,   kahn_round, schedule_seed, fold_periodic, chemistry,   photon_rate,
-    export_rates,     nullptr,
+    export_rates,     nullptr,        cell_rates, SWK_CARRY != 0,
 };
 #endif
 

@@ -545,19 +545,34 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   load_slots(a, cur, gl, s);
   if (idx(b + W) < count) load_slots(a, n1, gl, ns);
   bool have = idx(b) < count;
-  // the leader's cell data of the current task, loaded once per block
+  // the leader's cell data of the current task, loaded once per block; without a
+  // compacted list, a sweep above level 0 also tests the cell's level here
+  const bool check_level = a.act == nullptr && a.current_level > 0;
   float src = 0.f, per = 0.f, att = 0.f;
+  bool active = true;
   auto load_cell = [&]() {
-    if (have && gl == 0) {
-      src = a.src_dir[cur.x];
-      per = __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x);
-      att = (float)a.att[cur.x];
+    active = true;
+    if (have) {
+      if (check_level) active = a.level[cur.x] >= a.current_level;
+      if (gl == 0) {
+        src = a.src_dir[cur.x];
+        per = __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x);
+        att = (float)a.att[cur.x];
+      }
     }
   };
   load_cell();
   unsigned long long solved = 0, attempts = 0, w0 = 0;
   uint32_t wait_ns = 32;
   while (b * kGroups < count) {
+    if (have && !active) {  // inactive cell: keep its q, stamp the word with this sweep
+      if (gl == 0) {
+        const uint32_t t = rec_dir(cur) * a.Np + cur.x;
+        const unsigned long long own = ld_relaxed_u64(a.qe + t);
+        st_relaxed_u64(a.qe + t, (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
+      }
+      have = false;
+    }
     const uint32_t n_up = have ? rec_count(cur) : 0u;
     unsigned long long w[kPullRounds];
 #pragma unroll
@@ -670,6 +685,18 @@ __global__ void k_photon_rate_pull(PullArgs a, uint32_t last_epoch, double rate_
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < a.N; c += gridDim.x * blockDim.x) {
     double r = 0.0;
     for (int d = 0; d < a.D; ++d) r += (double)current_incoming(a, c, d, last_epoch);
+    out[c] = r * rate_scale;
+  }
+}
+
+// Rate of every cell summed over directions as Sweep::get_solver forms it
+// (src/sweep/mod.rs:616-620): sum over d of (incoming + source/D) + periodic, photons/s.
+__global__ void k_cell_rates_pull(PullArgs a, uint32_t last_epoch, double rate_scale, double* out) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < a.N; c += gridDim.x * blockDim.x) {
+    double r = 0.0;
+    for (int d = 0; d < a.D; ++d)
+      r += ((double)current_incoming(a, c, d, last_epoch) + (double)a.src_dir[c]) +
+           (double)a.periodic[(size_t)d * a.Np + c];
     out[c] = r * rate_scale;
   }
 }

@@ -198,6 +198,26 @@ class Sweep:
         self._check(self._lib.sw_get_rates(self._h, inc.ctypes.data, outg.ctypes.data, per.ctypes.data))
         return {"incoming": inc, "outgoing": outg, "periodic": per}
 
+    def time_series(self) -> dict:
+        """Global averages of the current state (the reference's time-series outputs,
+        src/sweep/time_series.rs:61-155), reduced on the device."""
+        s = _native.SwTimeSeries()
+        self._check(self._lib.sw_get_time_series(self._h, ctypes.byref(s)))
+        return {name: getattr(s, name) for name, _ in s._fields_}
+
+    def save_state(self) -> np.ndarray:
+        """Checkpoint of the evolving state as a byte array (see sw_save_state)."""
+        n = ctypes.c_size_t(0)
+        self._check(self._lib.sw_checkpoint_size(self._h, ctypes.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        self._check(self._lib.sw_save_state(self._h, buf.ctypes.data, buf.nbytes))
+        return buf
+
+    def load_state(self, buf: np.ndarray) -> None:
+        """Restore a checkpoint written by save_state of a handle with the same inputs."""
+        buf = np.ascontiguousarray(buf, np.uint8)
+        self._check(self._lib.sw_load_state(self._h, buf.ctypes.data, buf.nbytes))
+
     def stats(self) -> dict:
         s = _native.SwStats()
         self._check(self._lib.sw_get_stats(self._h, ctypes.byref(s)))

@@ -161,6 +161,29 @@ def test_mixed_precision_error_bounds():
     assert dt <= 1e-4, dt
 
 
+def test_mixed_compaction_and_in_kernel_stamping_agree(monkeypatch):
+    """Sweeps above level 0 either compact the active positions (stamping the inactive
+    tasks' words in the compaction) or stamp them in the sweep kernel.  The two paths
+    compute the same sums in the same order: fields and every rate agree bit for bit."""
+    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2)
+    out = {}
+    for mode in ("always", "never"):
+        monkeypatch.setenv("SUBSWEEP_COMPACT", mode)
+        gpu = Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
+                    precision="mixed")
+        for _ in range(6):
+            gpu.run_sweeps()
+        assert gpu.level_counts()[1:].min() > 0, "every level populated"
+        out[mode] = (gpu.fields(), gpu.rates(), gpu.cell_state()["level"])
+        gpu.close()
+    (fa, ra, la), (fb, rb, lb) = out["always"], out["never"]
+    np.testing.assert_array_equal(la, lb)
+    for k in fa:
+        np.testing.assert_array_equal(fa[k], fb[k], err_msg=k)
+    for k in ra:
+        np.testing.assert_array_equal(ra[k], rb[k], err_msg=k)
+
+
 def test_mixed_precision_c1_rates_and_periodic():
     """Pull-form rates (incoming, outgoing, periodic, PhotonRate) against the oracle's
     push-form ones on a periodic box with an ionization front, within FP32 accuracy."""
