@@ -167,6 +167,8 @@ def build_workload(name: str, n_per_side, nthreads: int):
         return workloads.c1_small_periodic(n_per_side=n_per_side or 32, nthreads=nthreads)
     if name == "c4":
         return workloads.c4_grf(n_per_side=n_per_side or 256, nthreads=nthreads)
+    if name == "c3":
+        return workloads.c3_batched(num_boxes=n_per_side or 256, nthreads=nthreads)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -392,7 +394,7 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c4"], default="c2")
+    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4"], default="c2")
     ap.add_argument("--n-per-side", type=int, default=None)
     ap.add_argument("--cpu-sample-side", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -66,6 +66,9 @@ typedef struct {
   double scale_factor;         /* Cosmology::scale_factor(); 1 when non-cosmological */
   int32_t precision;           /* sw_precision */
   int32_t device;              /* CUDA device ordinal; -1 = the calling thread's current device */
+  int32_t use_graphs;          /* mixed path: replay each step as one CUDA graph (captured again
+                                  when the step's set of sweeps changes); per-sweep timings are
+                                  then not recorded.  Default 0. */
 } sw_params;
 
 /* Face-neighbour CSR uploaded once (replaces the Cell component, grid/cell.rs:92-97).
@@ -113,6 +116,7 @@ typedef struct {
   int64_t schedule_levels;     /* Kahn levels of the schedule (0: cyclic grid, no schedule) */
   int64_t transport_attempts;  /* pull-path task attempts, retries included (tasks = success) */
   int64_t upwind_slots;        /* pull path: upwind LOCAL (face, direction) pairs of the grid */
+  int64_t graph_launches;      /* steps replayed from a CUDA graph */
 } sw_stats;
 
 /* Fill the reference's defaults (num_directions 84, levels 1, max_timestep 1 Myr). */

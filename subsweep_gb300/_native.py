@@ -54,6 +54,7 @@ class SwParams(ctypes.Structure):
         ("scale_factor", c_double),
         ("precision", c_int32),
         ("device", c_int32),
+        ("use_graphs", c_int32),
     ]
 
 
@@ -106,6 +107,7 @@ class SwStats(ctypes.Structure):
         ("schedule_levels", c_int64),
         ("transport_attempts", c_int64),
         ("upwind_slots", c_int64),
+        ("graph_launches", c_int64),
     ]
 
 

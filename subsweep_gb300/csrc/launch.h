@@ -60,6 +60,7 @@ struct DevicePtrs {
   uint32_t* queue;
   unsigned long long* qe;    // pull path: {q, sweep number} per task
   uint32_t epoch;            // pull path: number of the current level sweep
+  const uint32_t* epoch_base; // graph replay: sweep numbers are *epoch_base + epoch
   uint32_t* order;           // levelled schedule: task ids grouped by Kahn level
   const uint32_t* lvl;       // level offsets into order [num_sched_levels + 1]
   uint32_t num_sched_levels; // 0: no levelled schedule (cyclic graph)
@@ -129,7 +130,8 @@ sw_status handle_fail(sw_handle* h, sw_status st, const char* message);
 // Precision-independent kernels (compiled in sweep_fp64.cu).
 cudaError_t launch_update_levels(const DevicePtrs&, int lowest_allowed, cudaStream_t);
 cudaError_t launch_level_hist(const DevicePtrs&, cudaStream_t);
-cudaError_t launch_ionization_time(const DevicePtrs&, double time, cudaStream_t);
+// `time_dev`, when given, is read on the device instead of `time` (graph replay)
+cudaError_t launch_ionization_time(const DevicePtrs&, double time, cudaStream_t, const double* time_dev = nullptr);
 cudaError_t launch_schedule_scatter(const DevicePtrs&, const uint16_t* task_level, uint32_t* cursor, cudaStream_t);
 // Time series from per-cell summed rates: `partial` holds kTimeSeriesPartials doubles,
 // `out6` receives the six averages (device memory).

@@ -815,7 +815,9 @@ static __global__ void k_level_counts(SweepCtl* ctl, int num_levels) {
 }
 
 // IonizationTime write-back of run_sweep_system (src/sweep/mod.rs:731-738).
-static __global__ void k_ionization_time(uint32_t n, const double* xhii, double* ionization_time, double time) {
+static __global__ void k_ionization_time(uint32_t n, const double* xhii, double* ionization_time, double time,
+                                         const double* time_dev) {
+  if (time_dev) time = *time_dev;
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
     if (xhii[c] > 0.5 && isinf(ionization_time[c])) ionization_time[c] = time;
 }

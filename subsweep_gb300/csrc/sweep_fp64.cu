@@ -52,9 +52,9 @@ cudaError_t launch_time_series(const DevicePtrs& p, const double* cell_rate, boo
   return cudaGetLastError();
 }
 
-cudaError_t launch_ionization_time(const DevicePtrs& p, double time, cudaStream_t s) {
+cudaError_t launch_ionization_time(const DevicePtrs& p, double time, cudaStream_t s, const double* time_dev) {
   swk::k_ionization_time<<<grid_for_cells(p.num_cells), 256, 0, s>>>((uint32_t)p.num_cells, p.xhii,
-                                                                     p.ionization_time, time);
+                                                                     p.ionization_time, time, time_dev);
   return cudaGetLastError();
 }
 

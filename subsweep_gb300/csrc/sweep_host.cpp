@@ -93,9 +93,21 @@ struct sw_handle {
   int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
   bool trace = false;  // SUBSWEEP_TRACE: one stderr line per level sweep
   double* series_dev = nullptr;  // time-series partial sums and result (allocated on first use)
+  // graph replay of a step (pull path): the instantiated graph, the step shape it was
+  // captured for, and the pinned scalars its first node copies to the control block
+  bool graph_mode = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<int64_t> graph_key;
+  struct GraphScalars {
+    uint32_t epoch_base, pad;
+    double time;
+  }* graph_scalars = nullptr;
+  int64_t graph_captures = 0;
   uint32_t last_epoch = 0;  // pull path: sweep number of the last sweep of the last step
 
   ~sw_handle() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph_scalars) cudaFreeHost(graph_scalars);
     for (void* a : allocations) cudaFree(a);
     for (cudaEvent_t e : ev)
       if (e) cudaEventDestroy(e);
@@ -382,6 +394,7 @@ sw_status sw_default_params(sw_params* p) {
   p->scale_factor = 1.0;
   p->precision = SW_PRECISION_FP64;
   p->device = -1;
+  p->use_graphs = 0;
   return SW_OK;
 }
 
@@ -547,6 +560,10 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (std::strcmp(env, "levels") == 0) h->force_path = 1;
     if (std::strcmp(env, "queue") == 0) h->force_path = 2;
   }
+  // graph replay of steps: the pull path only (SUBSWEEP_GRAPH=0|1 overrides the parameter)
+  h->graph_mode = P.use_graphs != 0;
+  if (const char* env = std::getenv("SUBSWEEP_GRAPH")) h->graph_mode = std::atoi(env) != 0;
+  if (!h->ops->pull) h->graph_mode = false;
   // SUBSWEEP_COMPACT=always|never overrides the mixed path's choice between compacting
   // the active positions and stamping inactive tasks in the sweep (tests and tuning).
   if (const char* env = std::getenv("SUBSWEEP_COMPACT")) {
@@ -784,11 +801,116 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   return SW_OK;
 }
 
+// One step of the pull path replayed as a CUDA graph: the same launches as sw_step
+// (per sweep: control reset, attenuation, transport, periodic fold, chemistry; then the
+// level update and the ionization times), captured once per step shape (lowest allowed
+// level before and after, and each sweep's level and compaction choice).  The sweep
+// numbers and the end time live in the control block, copied from pinned host memory by
+// the graph's first node; the error flag stays set across the step's sweeps, so a stall
+// ends the remaining sweeps at once, and is read when the step has finished.
+static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
+  const swh::PrecisionOps& ops = *h->ops;
+  swh::DevicePtrs& p = h->p;
+  std::vector<int> levels;
+  uint64_t expected = 0;
+  TimestepState after = h->ts;
+  after.advance();
+  std::vector<int64_t> key = {h->ts.lowest, after.lowest};
+  for (int level : h->ts.sweep_order()) {
+    if (h->n_ge_host[level] == 0) continue;  // Sweep::run_sweeps skips empty levels (mod.rs:262)
+    levels.push_back(level);
+    expected += (uint64_t)h->n_ge_host[level] * (uint64_t)h->D;
+    const bool sparse = level > 0 && (p.compact_mode == 1 || (p.compact_mode == 0 && h->n_ge_host[level] * 2 < h->N));
+    key.push_back(level * 2 + (sparse ? 1 : 0));
+  }
+  if (!h->graph_scalars) {
+    void* ptr = nullptr;
+    SW_CUDA(h, cudaMallocHost(&ptr, sizeof(sw_handle::GraphScalars)), "pinned graph scalars");
+    h->graph_scalars = static_cast<sw_handle::GraphScalars*>(ptr);
+  }
+  if (!h->graph_exec || key != h->graph_key) {
+    if (h->graph_exec) {
+      cudaGraphExecDestroy(h->graph_exec);
+      h->graph_exec = nullptr;
+    }
+    SW_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin graph capture");
+    cudaError_t ce = cudaMemcpyAsync(&p.ctl->epoch_base, h->graph_scalars, sizeof(sw_handle::GraphScalars),
+                                     cudaMemcpyHostToDevice, h->stream);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(&p.ctl->error, 0, sizeof(uint32_t), h->stream);
+    swh::DevicePtrs q = p;
+    q.epoch_base = &p.ctl->epoch_base;
+    for (size_t k = 0; k < levels.size() && ce == cudaSuccess; ++k) {
+      const int level = levels[k];
+      q.epoch = (uint32_t)(k + 1);
+      q.active_cells = h->n_ge_host[level];
+      ce = cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, error), h->stream);
+      if (ce == cudaSuccess) ce = ops.attenuation(q, level, h->stream);
+      if (ce == cudaSuccess) ce = ops.sweep_levels(q, level, h->stream);
+      if (ce == cudaSuccess) ce = ops.fold_periodic(q, h->stream);
+      if (ce == cudaSuccess) ce = ops.chemistry(q, level, h->stream);
+    }
+    if (ce == cudaSuccess) ce = swh::launch_update_levels(p, after.lowest, h->stream);
+    if (ce == cudaSuccess) ce = swh::launch_ionization_time(p, 0.0, h->stream, &p.ctl->time);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t end = cudaStreamEndCapture(h->stream, &graph);
+    if (ce == cudaSuccess) ce = end;
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&h->graph_exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      h->graph_exec = nullptr;
+      return h->cuda_fail(ce, "graph capture of a step");
+    }
+    h->graph_key = key;
+    h->graph_captures += 1;
+  }
+  const double elapsed = h->ts.current_max_timestep();
+  h->graph_scalars->epoch_base = p.epoch;
+  h->graph_scalars->time = h->sim_time + elapsed;
+  const unsigned long long tasks_before = h->ctl_host.tasks;
+  SW_CUDA(h, cudaEventRecord(h->ev[5], h->stream), "event");
+  SW_CUDA(h, cudaGraphLaunch(h->graph_exec, h->stream), "graph launch");
+  SW_CUDA(h, cudaEventRecord(h->ev[1], h->stream), "event");
+  sw_status st = sync_ctl(h);
+  if (st != SW_OK) return st;
+  p.epoch += (uint32_t)levels.size();
+  h->last_epoch = p.epoch;
+  const uint32_t err = h->ctl_host.error;
+  if (err & (swk::kErrStall | swk::kErrQueue))
+    return h->fail(SW_ERR_STALLED, "a sweep of the step stalled: tasks left unsolved after a %.1f s wait "
+                   "(dependency cycle; flags 0x%x)", p.timeout_ns * 1e-9, err);
+  if (err & swk::kErrClamp)
+    return h->fail(SW_ERR_INVALID_ARG, "x_HII floor above 1 - 1e-10 in the chemistry clamp (reference panics)");
+  h->ts = after;
+  h->sim_time += elapsed;
+  float step_ms = 0.f;
+  cudaEventElapsedTime(&step_ms, h->ev[5], h->ev[1]);
+  const int64_t n = (int64_t)levels.size();
+  h->stats.step_ms += step_ms;
+  h->stats.steps += 1;
+  h->stats.level_sweeps += n;
+  h->stats.levelled_sweeps += n;
+  h->stats.transport_launches += n;
+  h->stats.graph_launches += 1;
+  h->stats.tasks = (int64_t)h->ctl_host.tasks;
+  h->stats.chem_cells = (int64_t)h->ctl_host.chem_cells;
+  h->stats.chem_attempts = (int64_t)h->ctl_host.chem_attempts;
+  h->stats.chem_failures = (int64_t)h->ctl_host.chem_failures;
+  h->stats.transport_attempts = (int64_t)h->ctl_host.attempts;
+  h->stats.simulation_time = h->sim_time;
+  if (time_elapsed_out) *time_elapsed_out = elapsed;
+  const uint64_t solved = h->ctl_host.tasks - tasks_before;
+  if (solved != expected)
+    return h->fail(SW_ERR_STALLED, "sweep solved %llu of %llu tasks: the dependency graph has a cycle",
+                   (unsigned long long)solved, (unsigned long long)expected);
+  return SW_OK;
+}
+
 sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   if (!h) return SW_ERR_INVALID_ARG;
   h->last_error.clear();
   const swh::PrecisionOps& ops = *h->ops;
   SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  if (h->graph_mode) return step_graph(h, time_elapsed_out);
   uint64_t expected = 0;
   std::vector<int> order = h->ts.sweep_order();
   unsigned long long tasks_before = h->ctl_host.tasks;

@@ -172,6 +172,7 @@ swk::PullArgs pull_args(const DevicePtrs& p, int level) {
   a.ctl = p.ctl;
   a.current_level = level;
   a.epoch = p.epoch;
+  a.epoch_base = p.epoch_base;
   a.timeout_ns = p.timeout_ns;
   a.rec = static_cast<const uint4*>(p.pull_rec);
   a.slots = static_cast<const uint2*>(p.pull_slots);
@@ -248,7 +249,7 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
     swk::k_compact_count<<<nc, swk::kCompactThreads, 0, s>>>(p.order, a.count, p.level, level, p.Np, p.chunk);
     swk::k_compact_scan<<<1, swk::kScanThreads, 0, s>>>(p.chunk, nc, p.chunk + nc);
     swk::k_compact_scatter<<<nc, swk::kCompactThreads, 0, s>>>(p.order, a.count, p.level, level, p.Np, p.chunk,
-                                                               p.act, p.qe, p.epoch);
+                                                               p.act, p.qe, p.epoch_base, p.epoch);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     a.act = p.act;

@@ -54,7 +54,13 @@ struct PullArgs {
   const uint32_t* act;        // compacted active positions, or nullptr: every position
   const uint32_t* act_count;  // device count of act (written by the compaction)
   uint32_t count;             // number of positions when act is nullptr
+  const uint32_t* epoch_base; // graph replay: the sweep number is *epoch_base + epoch
 };
+
+// the sweep number of a launch (a step replayed from a graph keeps its base on the device)
+__device__ __forceinline__ uint32_t sweep_number(const PullArgs& a) {
+  return a.epoch_base ? *a.epoch_base + a.epoch : a.epoch;
+}
 
 // The words are only ever read and written whole (relaxed, device scope), and nothing
 // else is ordered against them inside a sweep.
@@ -342,7 +348,9 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_scan(uint32_t* chunk, 
 __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(const uint32_t* order, uint32_t total,
                                                                      const uint8_t* level, int cur, uint32_t Np,
                                                                      const uint32_t* chunk, uint32_t* act,
-                                                                     unsigned long long* qe, uint32_t sweep) {
+                                                                     unsigned long long* qe, const uint32_t* epoch_base,
+                                                                     uint32_t epoch) {
+  const uint32_t sweep = epoch_base ? *epoch_base + epoch : epoch;
   const float inv_np = 1.0f / (float)Np;
   const uint32_t first = blockIdx.x * kCompactChunk + threadIdx.x * kCompactPer;
   uint32_t bits = active_bits(order, total, level, cur, Np, inv_np, first);
@@ -401,7 +409,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArg
   const uint32_t V = gridDim.x * (kPullThreads / kPullGroup) * K;
   const uint32_t v0 = (blockIdx.x * (kPullThreads / kPullGroup) + (threadIdx.x / kPullGroup)) * K;
   const uint32_t count = a.act ? *a.act_count : a.count;
-  const uint32_t sweep = a.epoch;
+  const uint32_t sweep = sweep_number(a);
   PullCursor<K> q;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
@@ -530,7 +538,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   const uint32_t gmask = ((1u << kPullGroup) - 1u) << gfirst;
   const uint32_t W = gridDim.x * (kPullThreads / 32);
   const uint32_t count = a.act ? *a.act_count : a.count;
-  const uint32_t sweep = a.epoch;
+  const uint32_t sweep = sweep_number(a);
   uint32_t b = blockIdx.x * (kPullThreads / 32) + threadIdx.x / 32;
   // this group's position index in block bb
   auto idx = [&](uint32_t bb) { return bb * kGroups + g; };

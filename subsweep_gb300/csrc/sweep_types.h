@@ -37,6 +37,10 @@ struct SweepCtl {
   unsigned long long attempts;  // task attempts of the pull transport (retries included)
   uint32_t n_ge[32];       // number of cells with level >= l (current level assignment)
   uint32_t hist[32];       // scratch level histogram
+  // scalars of a step replayed from a CUDA graph, copied in by the graph's first node
+  uint32_t epoch_base;     // sweep number before the step's first sweep
+  uint32_t pad2;
+  double time;             // simulation time at the end of the step
 };
 
 }  // namespace swk

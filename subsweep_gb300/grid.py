@@ -113,6 +113,27 @@ def poisson_points(n: int, box: float, seed: int) -> np.ndarray:
     return pts[morton_order(ijk)]
 
 
+def concatenate(grids: list) -> Grid:
+    """Block-diagonal union of independent grids: one CSR whose components never share a
+    face (LOCAL and LOCAL_PERIODIC neighbour ids are offset into each grid's own cell
+    range; boundary faces keep their id).  A sweep over the union computes, for every
+    component, what a sweep over that grid alone computes.  Generator positions are
+    shifted along x so the components do not overlap in space."""
+    offsets = np.cumsum([0] + [g.num_cells for g in grids])
+    face_offsets = np.cumsum([0] + [g.num_faces for g in grids])
+    row_ptr = np.concatenate([g.row_ptr[:-1] + fo for g, fo in zip(grids, face_offsets[:-1])] +
+                             [np.array([face_offsets[-1]], np.int64)]).astype(np.int64)
+    nbr = np.concatenate([np.where(g.kind <= 1, g.nbr + np.int32(o), g.nbr) for g, o in zip(grids, offsets[:-1])])
+    shift = np.cumsum([0.0] + [float(g.box_size[0]) for g in grids])
+    position = np.concatenate([g.position + np.array([sx, 0.0, 0.0]) for g, sx in zip(grids, shift[:-1])])
+    return Grid(row_ptr=row_ptr, nbr=nbr.astype(np.int32), kind=np.concatenate([g.kind for g in grids]),
+                area=np.concatenate([g.area for g in grids]), normal=np.concatenate([g.normal for g in grids]),
+                volume=np.concatenate([g.volume for g in grids]), size=np.concatenate([g.size for g in grids]),
+                position=position, box_size=np.array([shift[-1], max(float(g.box_size[1]) for g in grids),
+                                                      max(float(g.box_size[2]) for g in grids)]),
+                periodic=all(g.periodic for g in grids))
+
+
 def nearest_cells(grid: Grid, positions: np.ndarray) -> np.ndarray:
     """Index of the cell whose generator is nearest to each position (Euclidean, not
     periodic, like the kd-tree lookup of src/source_systems.rs:61-72)."""

@@ -77,7 +77,7 @@ class Sweep:
 
     def __init__(self, params: SweepParameters, grid: Grid, density, ionized_hydrogen_fraction,
                  temperature, source, precision: str = "fp64", scale_factor: float = 1.0,
-                 device: int = -1):
+                 device: int = -1, use_graphs: bool = False):
         self._lib = _native.load_gpu()
         self.params = params
         self.num_cells = grid.num_cells
@@ -105,6 +105,7 @@ class Sweep:
         p.num_tasks_to_solve_before_send_receive = params.num_tasks_to_solve_before_send_receive
         p.scale_factor = scale_factor
         p.precision = {"fp64": _native.SW_PRECISION_FP64, "mixed": _native.SW_PRECISION_MIXED}[precision]
+        p.use_graphs = int(use_graphs)
         p.device = device
 
         def arr(a, dt):

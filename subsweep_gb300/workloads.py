@@ -10,6 +10,10 @@ and point sources placed on their nearest cell.
       84 directions, 1 level, max_timestep 1 Myr, threshold 1e-5 photons/s
   C2  128^3, lognormal n_H (ln-sigma 1, mean 1e-3), 64 sources log-uniform in
       1e48..1e50 at random positions, 84 directions, 4 levels, safety 0.1
+  C3  256 independent periodic Poisson-point boxes of N log-uniform in 8^3..40^3
+      cells, each with a uniform n_H log-uniform in 1e-4..1e-2 and 1-4 sources
+      log-uniform in 1e48..1e49 photons/s, 32 directions, 2 levels; run as one grid
+      (block-diagonal union), so one sweep launch covers every box
   C4  256^3, n_H = exp(GRF), P(k) ~ k^-2, ln-sigma 1.5, mean 2e-4, 1000 sources at
       the densest cells with rates proportional to density (1e52 total),
       84 directions, 4 levels
@@ -83,6 +87,36 @@ def c2_lognormal(n_per_side: int = 128, seed: int = 2, num_directions: int = 84,
     return Workload(f"C2 periodic jittered-lattice Voronoi {n_per_side}^3 lognormal, {num_directions} dirs, "
                     f"{num_levels} levels", params, g, mass_density_from_number_density(n_h), np.full(n, 1e-10),
                     np.full(n, 1e4), src, steps=4)
+
+
+def c3_box(rng: np.random.Generator, seed: int, min_cells: int = 512, max_cells: int = 64000,
+           nthreads: int = 0):
+    """One box of the C3 batch: (grid, n_H per cell, source per cell)."""
+    n = int(round(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))))
+    box = MEGAPARSEC * n ** (1.0 / 3.0) / 32.0
+    g = gridmod.voronoi(gridmod.poisson_points(n, box, seed), box, periodic=True, nthreads=nthreads)
+    n_h = np.full(g.num_cells, 10.0 ** rng.uniform(-4.0, -2.0))
+    k = int(rng.integers(1, 5))
+    src = gridmod.place_sources(g, rng.uniform(0.0, box, size=(k, 3)), 10.0 ** rng.uniform(48.0, 49.0, size=k))
+    return g, n_h, src
+
+
+def c3_batched(num_boxes: int = 256, seed: int = 3, min_cells: int = 512, max_cells: int = 64000,
+               num_directions: int = 32, num_levels: int = 2, nthreads: int = 0, boxes=None) -> Workload:
+    """C3: independent boxes run as one block-diagonal grid.  `boxes` may pass
+    precomputed (grid, n_H, source) triples."""
+    rng = np.random.default_rng(seed)
+    if boxes is None:
+        boxes = [c3_box(rng, seed * 100003 + b, min_cells, max_cells, nthreads) for b in range(num_boxes)]
+    g = gridmod.concatenate([b[0] for b in boxes])
+    n_h = np.concatenate([b[1] for b in boxes])
+    src = np.concatenate([b[2] for b in boxes])
+    n = g.num_cells
+    params = SweepParameters(directions=num_directions, num_timestep_levels=num_levels, periodic=True,
+                             max_timestep=1.0 * MEGAYEAR, timestep_safety_factor=0.1)
+    return Workload(f"C3 {len(boxes)} periodic Poisson Voronoi boxes of {min_cells}..{max_cells} cells "
+                    f"({n} total), {num_directions} dirs, {num_levels} levels", params, g,
+                    mass_density_from_number_density(n_h), np.full(n, 1e-10), np.full(n, 1e4), src, steps=4)
 
 
 def gaussian_random_field(m: int, ln_sigma: float, seed: int) -> np.ndarray:
