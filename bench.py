@@ -246,10 +246,10 @@ def run_reference(args, dist: Dist):
 
 
 # --------------------------------------------------------------------------- GPU arm
-def time_precision(w, precision: str, device: int, warmup: int, steps: int, dist: Dist):
+def time_precision(w, precision: str, device: int, warmup: int, steps: int, dist: Dist, graphs: bool = False):
     from subsweep_gb300 import Sweep
     s = Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
-              precision=precision, device=device)
+              precision=precision, device=device, use_graphs=graphs and precision == "mixed")
     for _ in range(warmup):
         s.run_sweeps()
     dist.barrier()
@@ -281,7 +281,7 @@ def run_ours(args, dist: Dist):
     handles = {}
     precisions = ("fp64", "mixed") if args.precision == "both" else (args.precision,)
     for precision in precisions:
-        s, d, clocks = time_precision(w, precision, device, args.warmup, args.steps, dist)
+        s, d, clocks = time_precision(w, precision, device, args.warmup, args.steps, dist, graphs=args.graphs)
         handles[precision] = s
         step_s = d["step_ms"] / 1e3
         max_step_s = dist.allreduce(step_s, "max")
@@ -353,7 +353,7 @@ def run_ours(args, dist: Dist):
         "vs_baseline": None,
         "dtype": "f32 transport + f64 chemistry" if head == "mixed" else "f64",
         "data": "synthetic",
-        "config": dict(w.describe(), precision=head, replicas=args.gpus,
+        "config": dict(w.describe(), precision=head, replicas=args.gpus, cuda_graph_steps=bool(args.graphs),
                        l2="per-(cell,dir) state of %.1f GB per array > 129 MB L2; no flush needed" %
                           (n * ((w.params.num_directions() + 7) // 8 * 8) * 4 / 1e9),
                        grid_build_s=round(grid_s, 1)),
@@ -398,6 +398,7 @@ def main():
     ap.add_argument("--n-per-side", type=int, default=None)
     ap.add_argument("--cpu-sample-side", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--graphs", action="store_true", help="replay each mixed-path step as one CUDA graph")
     ap.add_argument("--precision", choices=["both", "fp64", "mixed"], default="both",
                     help="GPU arithmetic(s) to time; value reports the mixed path when it runs")
     args = ap.parse_args()

@@ -66,9 +66,10 @@ typedef struct {
   double scale_factor;         /* Cosmology::scale_factor(); 1 when non-cosmological */
   int32_t precision;           /* sw_precision */
   int32_t device;              /* CUDA device ordinal; -1 = the calling thread's current device */
-  int32_t use_graphs;          /* mixed path: replay each step as one CUDA graph (captured again
-                                  when the step's set of sweeps changes); per-sweep timings are
-                                  then not recorded.  Default 0. */
+  int32_t use_graphs;          /* replay each step as one CUDA graph (captured again
+                                  when the step's set of sweeps changes); the transport kernel
+                                  time is still recorded, the sweep / chemistry split is not.
+                                  Default 0. */
 } sw_params;
 
 /* Face-neighbour CSR uploaded once (replaces the Cell component, grid/cell.rs:92-97).
@@ -121,6 +122,16 @@ typedef struct {
 
 /* Fill the reference's defaults (num_directions 84, levels 1, max_timestep 1 Myr). */
 sw_status sw_default_params(sw_params* p);
+
+/* Batched mode (many independent small simulations, the C3 configuration): one handle
+ * over the block-diagonal union of n_boxes grids, each with its own initial fields.
+ * Box b's cells occupy the index range [sum of the earlier boxes' num_cells, + its own)
+ * in every per-cell array of the handle (sw_get_fields, ...), and its neighbour indices
+ * are local to the box.  Every box evolves exactly as a handle over that box alone
+ * would (same parameters); one launch per sweep covers all boxes.  The reference has no
+ * batched mode; this is the batch entry point planned for its GPU plugin. */
+sw_status sw_create_batch(const sw_params* params, int32_t n_boxes, const sw_grid_csr* grids,
+                          const sw_cell_init* inits, sw_handle** out);
 
 /* Directions::from_num (src/sweep/direction/mod.rs:58-75): writes num*3 doubles. */
 sw_status sw_directions_from_num(int32_t num, double* out);

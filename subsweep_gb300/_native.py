@@ -33,7 +33,7 @@ ABI_SYMBOLS = (
     "sw_default_params", "sw_directions_from_num", "sw_create", "sw_step", "sw_get_fields",
     "sw_get_cell_state", "sw_set_fields", "sw_get_level_counts", "sw_get_dependency_counts",
     "sw_get_rates", "sw_get_stats", "sw_last_error", "sw_destroy", "sw_get_dependency_counts_noalloc",
-    "sw_get_time_series", "sw_checkpoint_size", "sw_save_state", "sw_load_state",
+    "sw_get_time_series", "sw_checkpoint_size", "sw_save_state", "sw_load_state", "sw_create_batch",
 )
 
 
@@ -144,6 +144,8 @@ def load_gpu() -> ctypes.CDLL:
     lib.sw_get_stats.argtypes = [c_void_p, ctypes.POINTER(SwStats)]
     lib.sw_get_time_series.argtypes = [c_void_p, ctypes.POINTER(SwTimeSeries)]
     lib.sw_checkpoint_size.argtypes = [c_void_p, ctypes.POINTER(ctypes.c_size_t)]
+    lib.sw_create_batch.argtypes = [ctypes.POINTER(SwParams), c_int32, ctypes.POINTER(SwGridCsr),
+                                    ctypes.POINTER(SwCellInit), ctypes.POINTER(c_void_p)]
     lib.sw_save_state.argtypes = [c_void_p, c_void_p, ctypes.c_size_t]
     lib.sw_load_state.argtypes = [c_void_p, c_void_p, ctypes.c_size_t]
     lib.sw_last_error.argtypes = [c_void_p]

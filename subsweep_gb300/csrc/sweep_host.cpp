@@ -103,10 +103,12 @@ struct sw_handle {
     double time;
   }* graph_scalars = nullptr;
   int64_t graph_captures = 0;
+  std::vector<cudaEvent_t> graph_ev;  // start / end of each sweep's transport inside the graph
   uint32_t last_epoch = 0;  // pull path: sweep number of the last sweep of the last step
 
   ~sw_handle() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (cudaEvent_t e : graph_ev) cudaEventDestroy(e);
     if (graph_scalars) cudaFreeHost(graph_scalars);
     for (void* a : allocations) cudaFree(a);
     for (cudaEvent_t e : ev)
@@ -560,10 +562,9 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (std::strcmp(env, "levels") == 0) h->force_path = 1;
     if (std::strcmp(env, "queue") == 0) h->force_path = 2;
   }
-  // graph replay of steps: the pull path only (SUBSWEEP_GRAPH=0|1 overrides the parameter)
+  // graph replay of steps (SUBSWEEP_GRAPH=0|1 overrides the parameter)
   h->graph_mode = P.use_graphs != 0;
   if (const char* env = std::getenv("SUBSWEEP_GRAPH")) h->graph_mode = std::atoi(env) != 0;
-  if (!h->ops->pull) h->graph_mode = false;
   // SUBSWEEP_COMPACT=always|never overrides the mixed path's choice between compacting
   // the active positions and stamping inactive tasks in the sweep (tests and tuning).
   if (const char* env = std::getenv("SUBSWEEP_COMPACT")) {
@@ -801,17 +802,20 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   return SW_OK;
 }
 
-// One step of the pull path replayed as a CUDA graph: the same launches as sw_step
-// (per sweep: control reset, attenuation, transport, periodic fold, chemistry; then the
-// level update and the ionization times), captured once per step shape (lowest allowed
-// level before and after, and each sweep's level and compaction choice).  The sweep
+// One step replayed as a CUDA graph: the same launches as sw_step (per sweep: control
+// reset, attenuation, dependency counts on the push path, transport, periodic fold,
+// chemistry; then the level update and the ionization times), captured once per step
+// shape (lowest allowed level before and after, and each sweep's level and kernel
+// choice).  The sweep
 // numbers and the end time live in the control block, copied from pinned host memory by
 // the graph's first node; the error flag stays set across the step's sweeps, so a stall
-// ends the remaining sweeps at once, and is read when the step has finished.
+// ends the remaining sweeps at once, and is read when the step has finished.  Event
+// nodes around each sweep's transport give the transport kernel time.
 static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
   const swh::PrecisionOps& ops = *h->ops;
   swh::DevicePtrs& p = h->p;
   std::vector<int> levels;
+  std::vector<bool> variants;
   uint64_t expected = 0;
   TimestepState after = h->ts;
   after.advance();
@@ -820,8 +824,17 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     if (h->n_ge_host[level] == 0) continue;  // Sweep::run_sweeps skips empty levels (mod.rs:262)
     levels.push_back(level);
     expected += (uint64_t)h->n_ge_host[level] * (uint64_t)h->D;
-    const bool sparse = level > 0 && (p.compact_mode == 1 || (p.compact_mode == 0 && h->n_ge_host[level] * 2 < h->N));
-    key.push_back(level * 2 + (sparse ? 1 : 0));
+    // pull path: compaction or not; push path: levelled schedule or ready queue
+    bool variant;
+    if (ops.pull) {
+      variant = level > 0 && (p.compact_mode == 1 || (p.compact_mode == 0 && h->n_ge_host[level] * 2 < h->N));
+    } else {
+      variant = p.num_sched_levels > 0 && (uint64_t)h->n_ge_host[level] * 16 >= (uint64_t)h->N;
+      if (h->force_path == 1) variant = p.num_sched_levels > 0;
+      if (h->force_path == 2) variant = false;
+    }
+    variants.push_back(variant);
+    key.push_back(level * 2 + (variant ? 1 : 0));
   }
   if (!h->graph_scalars) {
     void* ptr = nullptr;
@@ -832,6 +845,11 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     if (h->graph_exec) {
       cudaGraphExecDestroy(h->graph_exec);
       h->graph_exec = nullptr;
+    }
+    while (h->graph_ev.size() < 2 * levels.size()) {
+      cudaEvent_t e;
+      SW_CUDA(h, cudaEventCreate(&e), "event");
+      h->graph_ev.push_back(e);
     }
     SW_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin graph capture");
     cudaError_t ce = cudaMemcpyAsync(&p.ctl->epoch_base, h->graph_scalars, sizeof(sw_handle::GraphScalars),
@@ -845,7 +863,11 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
       q.active_cells = h->n_ge_host[level];
       ce = cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, error), h->stream);
       if (ce == cudaSuccess) ce = ops.attenuation(q, level, h->stream);
-      if (ce == cudaSuccess) ce = ops.sweep_levels(q, level, h->stream);
+      if (ce == cudaSuccess && !ops.pull) ce = ops.init_counts(q, level, nullptr, !variants[k], h->stream);
+      if (ce == cudaSuccess) ce = cudaEventRecord(h->graph_ev[2 * k], h->stream);
+      if (ce == cudaSuccess) ce = (ops.pull || variants[k]) ? ops.sweep_levels(q, level, h->stream)
+                                                            : ops.sweep(q, level, h->stream);
+      if (ce == cudaSuccess) ce = cudaEventRecord(h->graph_ev[2 * k + 1], h->stream);
       if (ce == cudaSuccess) ce = ops.fold_periodic(q, h->stream);
       if (ce == cudaSuccess) ce = ops.chemistry(q, level, h->stream);
     }
@@ -875,9 +897,13 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
   p.epoch += (uint32_t)levels.size();
   h->last_epoch = p.epoch;
   const uint32_t err = h->ctl_host.error;
-  if (err & (swk::kErrStall | swk::kErrQueue))
+  if (err & (swk::kErrStall | swk::kErrQueue)) {
+    // leave the queue empty so the handle stays usable for inspection
+    if (p.queue) cudaMemsetAsync(p.queue, 0xff, (size_t)h->Np * h->D * sizeof(uint32_t), h->stream);
+    cudaStreamSynchronize(h->stream);
     return h->fail(SW_ERR_STALLED, "a sweep of the step stalled: tasks left unsolved after a %.1f s wait "
                    "(dependency cycle; flags 0x%x)", p.timeout_ns * 1e-9, err);
+  }
   if (err & swk::kErrClamp)
     return h->fail(SW_ERR_INVALID_ARG, "x_HII floor above 1 - 1e-10 in the chemistry clamp (reference panics)");
   h->ts = after;
@@ -885,10 +911,15 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
   float step_ms = 0.f;
   cudaEventElapsedTime(&step_ms, h->ev[5], h->ev[1]);
   const int64_t n = (int64_t)levels.size();
+  for (int64_t k = 0; k < n; ++k) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->graph_ev[2 * k], h->graph_ev[2 * k + 1]) == cudaSuccess)
+      h->stats.transport_kernel_ms += ms;
+  }
   h->stats.step_ms += step_ms;
   h->stats.steps += 1;
   h->stats.level_sweeps += n;
-  h->stats.levelled_sweeps += n;
+  for (bool v : variants) h->stats.levelled_sweeps += (ops.pull || v) ? 1 : 0;
   h->stats.transport_launches += n;
   h->stats.graph_launches += 1;
   h->stats.tasks = (int64_t)h->ctl_host.tasks;
@@ -903,6 +934,60 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     return h->fail(SW_ERR_STALLED, "sweep solved %llu of %llu tasks: the dependency graph has a cycle",
                    (unsigned long long)solved, (unsigned long long)expected);
   return SW_OK;
+}
+
+sw_status sw_create_batch(const sw_params* params, int32_t n_boxes, const sw_grid_csr* grids,
+                          const sw_cell_init* inits, sw_handle** out) {
+  if (!out) return create_fail(SW_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (!params || !grids || !inits || n_boxes < 1) return create_fail(SW_ERR_INVALID_ARG, "invalid batch arguments");
+  int64_t n = 0, e = 0;
+  for (int32_t b = 0; b < n_boxes; ++b) {
+    const sw_grid_csr& g = grids[b];
+    const sw_cell_init& in = inits[b];
+    if (g.num_cells < 1 || !g.row_ptr || !g.nbr || !g.kind || !g.area || !g.normal || !g.volume || !g.size ||
+        !in.density || !in.ionized_hydrogen_fraction || !in.temperature || !in.source)
+      return create_fail(SW_ERR_INVALID_ARG, "box %d: missing array", b);
+    if (g.row_ptr[0] != 0 || g.row_ptr[g.num_cells] < 0) return create_fail(SW_ERR_INVALID_ARG, "box %d: bad row_ptr", b);
+    // neighbour indices must stay inside the box before they are offset into the union
+    for (int64_t f = 0; f < g.row_ptr[g.num_cells]; ++f)
+      if (g.kind[f] != SW_FACE_BOUNDARY && (g.nbr[f] < 0 || g.nbr[f] >= g.num_cells))
+        return create_fail(SW_ERR_INVALID_ARG, "box %d: face %lld has neighbour %d outside the box", b,
+                           (long long)f, g.nbr[f]);
+    n += g.num_cells;
+    e += g.row_ptr[g.num_cells];
+  }
+  if (n > (int64_t)INT32_MAX) return create_fail(SW_ERR_UNSUPPORTED, "batch of %lld cells", (long long)n);
+  std::vector<int64_t> row_ptr(n + 1);
+  std::vector<int32_t> nbr(e);
+  std::vector<uint8_t> kind(e);
+  std::vector<double> area(e), normal(3 * e), volume(n), size(n), density(n), x(n), t(n), src(n);
+  int64_t c0 = 0, f0 = 0;
+  for (int32_t b = 0; b < n_boxes; ++b) {
+    const sw_grid_csr& g = grids[b];
+    const sw_cell_init& in = inits[b];
+    const int64_t nb = g.num_cells, eb = g.row_ptr[nb];
+    for (int64_t c = 0; c < nb; ++c) row_ptr[c0 + c] = f0 + g.row_ptr[c];
+    for (int64_t f = 0; f < eb; ++f) {
+      kind[f0 + f] = g.kind[f];
+      nbr[f0 + f] = g.kind[f] == SW_FACE_BOUNDARY ? g.nbr[f] : (int32_t)(g.nbr[f] + c0);
+    }
+    std::copy(g.area, g.area + eb, area.begin() + f0);
+    std::copy(g.normal, g.normal + 3 * eb, normal.begin() + 3 * f0);
+    std::copy(g.volume, g.volume + nb, volume.begin() + c0);
+    std::copy(g.size, g.size + nb, size.begin() + c0);
+    std::copy(in.density, in.density + nb, density.begin() + c0);
+    std::copy(in.ionized_hydrogen_fraction, in.ionized_hydrogen_fraction + nb, x.begin() + c0);
+    std::copy(in.temperature, in.temperature + nb, t.begin() + c0);
+    std::copy(in.source, in.source + nb, src.begin() + c0);
+    c0 += nb;
+    f0 += eb;
+  }
+  row_ptr[n] = e;
+  const sw_grid_csr u = {n, row_ptr.data(), nbr.data(), kind.data(), area.data(), normal.data(), volume.data(),
+                         size.data()};
+  const sw_cell_init ui = {density.data(), x.data(), t.data(), src.data()};
+  return sw_create(params, &u, &ui, out);
 }
 
 sw_status sw_step(sw_handle* h, double* time_elapsed_out) {

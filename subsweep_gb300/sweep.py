@@ -78,9 +78,29 @@ class Sweep:
     def __init__(self, params: SweepParameters, grid: Grid, density, ionized_hydrogen_fraction,
                  temperature, source, precision: str = "fp64", scale_factor: float = 1.0,
                  device: int = -1, use_graphs: bool = False):
+        self._setup(params, precision, scale_factor, device, use_graphs)
+        g, init = self._csr(grid, density, ionized_hydrogen_fraction, temperature, source)
+        self._finish(self._lib.sw_create(ctypes.byref(self._p), ctypes.byref(g), ctypes.byref(init),
+                                         ctypes.byref(self._hnew)), grid.num_cells)
+
+    @classmethod
+    def batch(cls, params: SweepParameters, boxes, precision: str = "fp64", scale_factor: float = 1.0,
+              device: int = -1, use_graphs: bool = False) -> "Sweep":
+        """One handle over independent boxes (sw_create_batch): `boxes` holds
+        (grid, density, ionized_hydrogen_fraction, temperature, source) per box; per-cell
+        results are concatenated in box order."""
+        self = cls.__new__(cls)
+        self._setup(params, precision, scale_factor, device, use_graphs)
+        parts = [self._csr(*box) for box in boxes]
+        grids = (_native.SwGridCsr * len(parts))(*[g for g, _ in parts])
+        inits = (_native.SwCellInit * len(parts))(*[i for _, i in parts])
+        self._finish(self._lib.sw_create_batch(ctypes.byref(self._p), len(parts), grids, inits,
+                                               ctypes.byref(self._hnew)), sum(b[0].num_cells for b in boxes))
+        return self
+
+    def _setup(self, params, precision, scale_factor, device, use_graphs):
         self._lib = _native.load_gpu()
         self.params = params
-        self.num_cells = grid.num_cells
         self.num_directions = params.num_directions()
         self.precision = precision
         p = _native.SwParams()
@@ -107,7 +127,10 @@ class Sweep:
         p.precision = {"fp64": _native.SW_PRECISION_FP64, "mixed": _native.SW_PRECISION_MIXED}[precision]
         p.use_graphs = int(use_graphs)
         p.device = device
+        self._p = p
+        self._hnew = ctypes.c_void_p()
 
+    def _csr(self, grid, density, ionized_hydrogen_fraction, temperature, source):
         def arr(a, dt):
             a = np.ascontiguousarray(a, dtype=dt)
             self._keep.append(a)
@@ -124,12 +147,14 @@ class Sweep:
             ionized_hydrogen_fraction=arr(np.broadcast_to(ionized_hydrogen_fraction, (n,)), np.float64),
             temperature=arr(np.broadcast_to(temperature, (n,)), np.float64),
             source=arr(np.broadcast_to(source, (n,)), np.float64))
-        h = ctypes.c_void_p()
-        st = self._lib.sw_create(ctypes.byref(p), ctypes.byref(g), ctypes.byref(init), ctypes.byref(h))
+        return g, init
+
+    def _finish(self, st, num_cells):
         self._keep = []
         if st != _native.SW_OK:
             raise SweepError(st, self._lib.sw_last_error(None).decode())
-        self._h = h
+        self._h = self._hnew
+        self.num_cells = num_cells
 
     # -- lifecycle -------------------------------------------------------------
     def close(self):

@@ -11,7 +11,7 @@ import pytest
 
 from oracle import binding
 from subsweep_gb300 import grid as gridmod, workloads
-from subsweep_gb300.sweep import Sweep
+from subsweep_gb300.sweep import Sweep, SweepError
 
 from test_gpu_parity import oracle_dirs
 
@@ -94,3 +94,36 @@ def test_gpu_batch_equals_boxes_bitwise():
         np.testing.assert_allclose(fb["photon_rate"][sl], fs["photon_rate"], rtol=1e-6)
         g.close()
     gb.close()
+
+
+def test_batch_rejects_neighbour_outside_box():
+    """sw_create_batch checks every box's neighbour ids before offsetting them (no CUDA
+    call is made for an invalid batch)."""
+    boxes = small_boxes(k=2, seed=13)
+    g, n_h, src = boxes[1]
+    bad = gridmod.Grid(**{**g.__dict__, "nbr": g.nbr.copy()})
+    bad.nbr[np.flatnonzero(bad.kind == 0)[0]] = bad.num_cells  # one past the box
+    w = workloads.c3_batched(boxes=boxes, num_directions=16)
+    dens = w.density[: boxes[0][0].num_cells]
+    args = [(boxes[0][0], dens, 1e-10, 1e4, boxes[0][2]), (bad, w.density[boxes[0][0].num_cells:], 1e-10, 1e4, src)]
+    with pytest.raises(SweepError) as e:
+        Sweep.batch(w.params, args, precision="mixed")
+    assert "outside the box" in str(e.value)
+
+
+@pytest.mark.gpu
+def test_create_batch_equals_union():
+    boxes = small_boxes(k=3, seed=14)
+    w = workloads.c3_batched(boxes=boxes, num_directions=32)
+    off = np.cumsum([0] + [b[0].num_cells for b in boxes])
+    args = [(b[0], w.density[off[k]:off[k + 1]], 1e-10, 1e4, b[2]) for k, b in enumerate(boxes)]
+    a = Sweep.batch(w.params, args, precision="mixed")
+    u = Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source, precision="mixed")
+    assert a.num_cells == u.num_cells
+    for _ in range(3):
+        assert a.run_sweeps() == u.run_sweeps()
+    fa, fu = a.fields(), u.fields()
+    for k in fa:
+        np.testing.assert_array_equal(fa[k], fu[k], err_msg=k)
+    a.close()
+    u.close()

@@ -1,4 +1,4 @@
-"""Steps replayed from a CUDA graph (mixed path, use_graphs) against direct launches.
+"""Steps replayed from a CUDA graph (use_graphs) against direct launches.
 
 The graph holds the same launches with the sweep numbers and the end time read from
 the device, so fields, levels, rates and the time series agree bit for bit.  A
@@ -44,13 +44,32 @@ def test_graph_steps_equal_direct_steps(name):
     graph.close()
 
 
-def test_graph_step_reports_stall():
+def test_fp64_graph_steps_match_direct_steps():
+    """The push path replayed from a graph: its FP64 atomics sum in arrival order, so
+    graph and direct steps agree to rounding, levels exactly."""
+    w = workloads.c2_lognormal(n_per_side=10, num_directions=16, num_levels=3, nthreads=2)
+    mk = lambda g: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
+                         precision="fp64", use_graphs=g)
+    direct, graph = mk(False), mk(True)
+    for _ in range(4):
+        assert graph.run_sweeps() == direct.run_sweeps()
+    np.testing.assert_array_equal(graph.cell_state()["level"], direct.cell_state()["level"])
+    fd, fg = direct.fields(), graph.fields()
+    for k in ("ionized_hydrogen_fraction", "temperature"):
+        np.testing.assert_allclose(fg[k], fd[k], rtol=1e-10, err_msg=k)
+    assert graph.stats()["graph_launches"] == 4
+    direct.close()
+    graph.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_graph_step_reports_stall(precision):
     from tests.test_abi import _cyclic_grid
     g = _cyclic_grid()
     n = g.num_cells
     p = SweepParameters(directions=[[0.0, 0.0, 1.0]], num_timestep_levels=1, periodic=False, max_timestep=1.0)
     s = Sweep(p, g, density=np.full(n, 1e-24), ionized_hydrogen_fraction=np.full(n, 1e-10),
-              temperature=np.full(n, 1e4), source=np.zeros(n), precision="mixed", use_graphs=True)
+              temperature=np.full(n, 1e4), source=np.zeros(n), precision=precision, use_graphs=True)
     with pytest.raises(SweepError) as e:
         s.run_sweeps()
     assert e.value.status == _native.SW_ERR_STALLED
