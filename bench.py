@@ -296,6 +296,7 @@ def run_ours(args, dist: Dist):
     # error of the mixed path against the FP64 drop-in after identical steps
     head = "mixed" if "mixed" in results else "fp64"
     sched_levels = int(handles[head].stats()["schedule_levels"])
+    pull_variant = int(handles[head].stats()["pull_variant"])
     err = None
     if len(results) == 2:
         fm, ff = handles["mixed"].fields(), handles["fp64"].fields()
@@ -304,6 +305,10 @@ def run_ours(args, dist: Dist):
             "max_rel_dT": float((np.abs(fm["temperature"] - ff["temperature"]) / ff["temperature"]).max()),
             "levels_equal_fraction": float((handles["mixed"].cell_state()["level"] ==
                                             handles["fp64"].cell_state()["level"]).mean()),
+            # FP32 rates are stored in units of 2^-96 of the total source: rates below
+            # 1e-20 of the total luminosity are compared against that floor
+            "max_rel_photon_rate": float((np.abs(fm["photon_rate"] - ff["photon_rate"]) /
+                                          np.maximum(np.abs(ff["photon_rate"]), 1e-20 * float(w.source.sum()))).max()),
         }
         handles["fp64"].close()
 
@@ -378,6 +383,7 @@ def run_ours(args, dist: Dist):
         "cpu_baseline": cpu,
         "stats": {"tasks": d["tasks"], "levelled_sweeps": d["levelled_sweeps"],
                   "transport_attempts": d["transport_attempts"],
+                  "pull_variant": pull_variant,
                   "sweeps": d["level_sweeps"], "schedule_levels": sched_levels,
                   "chem_attempts": d["chem_attempts"], "transport_kernel_ms": d["transport_kernel_ms"],
                   "sweep_ms": d["sweep_ms"], "chem_ms": d["chem_ms"], "level_ms": d["level_ms"],

@@ -70,6 +70,10 @@ typedef struct {
                                   when the step's set of sweeps changes); the transport kernel
                                   time is still recorded, the sweep / chemistry split is not.
                                   Default 0. */
+  int32_t autotune;            /* mixed path: the first sweeps try each transport kernel variant
+                                  (cells per warp, resident blocks per SM) and keep the fastest
+                                  per task; every variant computes identical results.
+                                  Default 1. */
 } sw_params;
 
 /* Face-neighbour CSR uploaded once (replaces the Cell component, grid/cell.rs:92-97).
@@ -118,6 +122,7 @@ typedef struct {
   int64_t transport_attempts;  /* pull-path task attempts, retries included (tasks = success) */
   int64_t upwind_slots;        /* pull path: upwind LOCAL (face, direction) pairs of the grid */
   int64_t graph_launches;      /* steps replayed from a CUDA graph */
+  int64_t pull_variant;        /* mixed path: transport kernel variant in use (autotuned or set) */
 } sw_stats;
 
 /* Fill the reference's defaults (num_directions 84, levels 1, max_timestep 1 Myr). */

@@ -55,6 +55,7 @@ class SwParams(ctypes.Structure):
         ("precision", c_int32),
         ("device", c_int32),
         ("use_graphs", c_int32),
+        ("autotune", c_int32),
     ]
 
 
@@ -108,6 +109,7 @@ class SwStats(ctypes.Structure):
         ("transport_attempts", c_int64),
         ("upwind_slots", c_int64),
         ("graph_launches", c_int64),
+        ("pull_variant", c_int64),
     ]
 
 

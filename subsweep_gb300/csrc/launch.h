@@ -70,6 +70,9 @@ struct DevicePtrs {
   uint32_t* chunk;           // pull path: compaction chunk offsets, count at [num_chunks]
   int64_t active_cells;      // pull path: cells active in the sweep being launched
   int compact_mode;          // pull path: 0 by density, 1 always compact, 2 never (lockstep)
+  int pull_variant;          // pull path: transport kernel variant (0: the default)
+  int num_sms;
+  int level_bps_cap;         // SUBSWEEP_LEVEL_BLOCKS_PER_SM, 0: each kernel's occupancy limit
   int level_blocks;          // resident blocks of the levelled kernel
   const uint32_t* periodic_cells;
   uint32_t n_periodic_cells;
@@ -107,7 +110,14 @@ struct PrecisionOps {
   // photons/s
   cudaError_t (*cell_rates)(const DevicePtrs&, uint32_t last_epoch, double* out, cudaStream_t);
   bool carry_neutral;  // the chemistry carries 1 - x_HII as its own state (yneu)
+  // pull path: transport kernel variants the autotuner tries (count, ids); 0 on the push path
+  int num_tune_variants;
+  const int* tune_variants;
 };
+
+// pull path: transport kernel variant used without autotuning (lockstep blocks of four
+// positions, 4 target blocks per SM)
+constexpr int kDefaultPullVariant = 94;
 
 extern const PrecisionOps kOpsFP64;
 extern const PrecisionOps kOpsMixed;

@@ -103,6 +103,12 @@ struct sw_handle {
     double time;
   }* graph_scalars = nullptr;
   int64_t graph_captures = 0;
+  int64_t graph_kernels = 0;  // kernel launches in the captured step
+  // autotuning of the pull transport kernel: trials of ops->tune_variants, one per sweep
+  bool autotune = false;
+  bool tuned = false;
+  int tune_index = 0;
+  std::vector<double> tune_ns;  // ns per task of each candidate
   std::vector<cudaEvent_t> graph_ev;  // start / end of each sweep's transport inside the graph
   uint32_t last_epoch = 0;  // pull path: sweep number of the last sweep of the last step
 
@@ -397,6 +403,7 @@ sw_status sw_default_params(sw_params* p) {
   p->precision = SW_PRECISION_FP64;
   p->device = -1;
   p->use_graphs = 0;
+  p->autotune = 1;
   return SW_OK;
 }
 
@@ -562,6 +569,17 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (std::strcmp(env, "levels") == 0) h->force_path = 1;
     if (std::strcmp(env, "queue") == 0) h->force_path = 2;
   }
+  // transport kernel variant: SUBSWEEP_PULL_VARIANT fixes it, else the autotuner picks
+  // it (sw_params.autotune; SUBSWEEP_AUTOTUNE=0|1 overrides)
+  p.num_sms = sms;
+  if (const char* env = std::getenv("SUBSWEEP_LEVEL_BLOCKS_PER_SM")) p.level_bps_cap = std::atoi(env);
+  h->autotune = P.autotune != 0;
+  if (const char* env = std::getenv("SUBSWEEP_AUTOTUNE")) h->autotune = std::atoi(env) != 0;
+  if (const char* env = std::getenv("SUBSWEEP_PULL_VARIANT")) {
+    p.pull_variant = std::atoi(env);
+    h->autotune = false;
+  }
+  if (h->ops->num_tune_variants == 0) h->autotune = false;
   // graph replay of steps (SUBSWEEP_GRAPH=0|1 overrides the parameter)
   h->graph_mode = P.use_graphs != 0;
   if (const char* env = std::getenv("SUBSWEEP_GRAPH")) h->graph_mode = std::atoi(env) != 0;
@@ -819,7 +837,7 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
   uint64_t expected = 0;
   TimestepState after = h->ts;
   after.advance();
-  std::vector<int64_t> key = {h->ts.lowest, after.lowest};
+  std::vector<int64_t> key = {h->ts.lowest, after.lowest, p.pull_variant};
   for (int level : h->ts.sweep_order()) {
     if (h->n_ge_host[level] == 0) continue;  // Sweep::run_sweeps skips empty levels (mod.rs:262)
     levels.push_back(level);
@@ -857,6 +875,14 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     if (ce == cudaSuccess) ce = cudaMemsetAsync(&p.ctl->error, 0, sizeof(uint32_t), h->stream);
     swh::DevicePtrs q = p;
     q.epoch_base = &p.ctl->epoch_base;
+    int64_t kernels = 3;  // level update (two kernels) and ionization times
+    for (size_t k = 0; k < levels.size(); ++k) {
+      // attenuation, transport, chemistry, the periodic fold, and the counts (push) or
+      // the compaction (pull, sparse sweeps)
+      kernels += 3 + (p.n_periodic_cells > 0 ? 1 : 0);
+      if (!ops.pull) kernels += 1;
+      else if (variants[k]) kernels += 3;
+    }
     for (size_t k = 0; k < levels.size() && ce == cudaSuccess; ++k) {
       const int level = levels[k];
       q.epoch = (uint32_t)(k + 1);
@@ -864,10 +890,11 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
       ce = cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, error), h->stream);
       if (ce == cudaSuccess) ce = ops.attenuation(q, level, h->stream);
       if (ce == cudaSuccess && !ops.pull) ce = ops.init_counts(q, level, nullptr, !variants[k], h->stream);
-      if (ce == cudaSuccess) ce = cudaEventRecord(h->graph_ev[2 * k], h->stream);
+      // external records: event nodes that are recorded when the graph runs
+      if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(h->graph_ev[2 * k], h->stream, cudaEventRecordExternal);
       if (ce == cudaSuccess) ce = (ops.pull || variants[k]) ? ops.sweep_levels(q, level, h->stream)
                                                             : ops.sweep(q, level, h->stream);
-      if (ce == cudaSuccess) ce = cudaEventRecord(h->graph_ev[2 * k + 1], h->stream);
+      if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(h->graph_ev[2 * k + 1], h->stream, cudaEventRecordExternal);
       if (ce == cudaSuccess) ce = ops.fold_periodic(q, h->stream);
       if (ce == cudaSuccess) ce = ops.chemistry(q, level, h->stream);
     }
@@ -884,6 +911,7 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     }
     h->graph_key = key;
     h->graph_captures += 1;
+    h->graph_kernels = kernels;
   }
   const double elapsed = h->ts.current_max_timestep();
   h->graph_scalars->epoch_base = p.epoch;
@@ -916,12 +944,14 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     if (cudaEventElapsedTime(&ms, h->graph_ev[2 * k], h->graph_ev[2 * k + 1]) == cudaSuccess)
       h->stats.transport_kernel_ms += ms;
   }
+  (void)cudaGetLastError();  // a failed timing query must not surface at the next launch
   h->stats.step_ms += step_ms;
   h->stats.steps += 1;
   h->stats.level_sweeps += n;
   for (bool v : variants) h->stats.levelled_sweeps += (ops.pull || v) ? 1 : 0;
   h->stats.transport_launches += n;
   h->stats.graph_launches += 1;
+  h->stats.kernel_launches += h->graph_kernels;
   h->stats.tasks = (int64_t)h->ctl_host.tasks;
   h->stats.chem_cells = (int64_t)h->ctl_host.chem_cells;
   h->stats.chem_attempts = (int64_t)h->ctl_host.chem_attempts;
@@ -995,7 +1025,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   h->last_error.clear();
   const swh::PrecisionOps& ops = *h->ops;
   SW_CUDA(h, cudaSetDevice(h->device), "select device");
-  if (h->graph_mode) return step_graph(h, time_elapsed_out);
+  if (h->graph_mode && (h->tuned || !h->autotune)) return step_graph(h, time_elapsed_out);
   uint64_t expected = 0;
   std::vector<int> order = h->ts.sweep_order();
   unsigned long long tasks_before = h->ctl_host.tasks;
@@ -1014,6 +1044,8 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     bool levelled = h->p.num_sched_levels > 0 && (uint64_t)h->n_ge_host[level] * 16 >= (uint64_t)h->N;
     if (h->force_path == 1) levelled = h->p.num_sched_levels > 0;
     if (h->force_path == 2) levelled = false;
+    const bool trial = ops.pull && h->autotune && !h->tuned;
+    if (trial) h->p.pull_variant = ops.tune_variants[h->tune_index];
     if (ops.pull) {
       levelled = true;  // the pull path always walks the schedule (or the id order)
       h->p.epoch += 1;
@@ -1043,9 +1075,20 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
     cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
     cudaEventElapsedTime(&k, h->ev[6], h->ev[7]);
+    (void)cudaGetLastError();  // timing queries are best effort
     sweep_ms += a;
     chem_ms += b;
     kernel_ms += k;
+    if (trial) {  // one autotuning trial per sweep; the fastest variant per task is kept
+      h->tune_ns.push_back(1e6 * k / std::max(1.0, (double)h->n_ge_host[level] * h->D));
+      if (++h->tune_index == ops.num_tune_variants) {
+        int best = 0;
+        for (int i = 1; i < ops.num_tune_variants; ++i)
+          if (h->tune_ns[i] < h->tune_ns[best]) best = i;
+        h->p.pull_variant = ops.tune_variants[best];
+        h->tuned = true;
+      }
+    }
     h->stats.transport_launches += 1;
     if (h->trace) {
       swk::SweepCtl c{};
@@ -1083,6 +1126,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   cudaEventElapsedTime(&level_ms, h->ev[3], h->ev[4]);
   float step_ms = 0.f;
   cudaEventElapsedTime(&step_ms, h->ev[5], h->ev[1]);
+  (void)cudaGetLastError();
   h->stats.step_ms += step_ms;
   h->stats.transport_kernel_ms += kernel_ms;
   h->stats.kernel_launches += launches;
@@ -1318,6 +1362,7 @@ sw_status sw_get_stats(sw_handle* h, sw_stats* out) {
   if (!h || !out) return SW_ERR_INVALID_ARG;
   h->stats.schedule_levels = h->stats_schedule_levels;
   h->stats.upwind_slots = h->stats_upwind_slots;
+  h->stats.pull_variant = h->ops->pull ? (h->p.pull_variant > 0 ? h->p.pull_variant : swh::kDefaultPullVariant) : 0;
   *out = h->stats;
   return SW_OK;
 }

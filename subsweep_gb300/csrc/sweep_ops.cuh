@@ -204,7 +204,6 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 // Variants of the pull kernel: independent cursors (10 * cursors per group + target
 // blocks per SM) or warp-lockstep blocks of four positions (90 + blocks per SM).
 // SUBSWEEP_PULL_VARIANT picks one.
-constexpr int kDefaultPullVariant = 94;
 
 const void* pull_kernel(int variant) {
   switch (variant) {
@@ -217,13 +216,37 @@ const void* pull_kernel(int variant) {
     case 94: return (const void*)swk::k_sweep_pull_lock<4>;
     case 95: return (const void*)swk::k_sweep_pull_lock<5>;
     case 96: return (const void*)swk::k_sweep_pull_lock<6>;
-    default: return (const void*)swk::k_sweep_pull<1, 4>;
+    case 14: return (const void*)swk::k_sweep_pull<1, 4>;
+    default: return nullptr;
   }
 }
 
-int pull_variant() {
-  const char* env = std::getenv("SUBSWEEP_PULL_VARIANT");
-  return env ? std::atoi(env) : kDefaultPullVariant;
+// the variant in use: set on the handle (autotuner or SUBSWEEP_PULL_VARIANT), else the
+// default; an unknown number selects the default
+int pull_variant(const DevicePtrs* p = nullptr) {
+  int v = kDefaultPullVariant;
+  if (p && p->pull_variant > 0) {
+    v = p->pull_variant;
+  } else if (const char* env = std::getenv("SUBSWEEP_PULL_VARIANT")) {
+    v = std::atoi(env);
+  }
+  return pull_kernel(v) ? v : kDefaultPullVariant;
+}
+
+// candidates of the autotuner: lockstep blocks of four positions at 4, 5 and 6 target
+// blocks per SM, one independent cursor per group at 4 blocks, two at 2 blocks
+constexpr int kTuneVariants[] = {94, 95, 96, 14, 22};
+
+// cooperative grid of a kernel: its occupancy limit (capped by
+// SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM
+cudaError_t coop_grid(const DevicePtrs& p, const void* fn, int* grid) {
+  int bps = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, swk::kPullThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (bps < 1) return cudaErrorInvalidConfiguration;
+  if (p.level_bps_cap >= 1 && p.level_bps_cap < bps) bps = p.level_bps_cap;
+  *grid = bps * p.num_sms;
+  return cudaSuccess;
 }
 
 cudaError_t occupancy_pull(int* blocks_per_sm) {
@@ -238,7 +261,7 @@ cudaError_t occupancy_pull(int* blocks_per_sm) {
 // inactive tasks itself.
 cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, level);
-  const int variant = pull_variant();
+  const int variant = pull_variant(&p);
   // only the lockstep kernels test levels themselves
   const bool lockstep = variant >= 90;
   bool sparse = level > 0 && (p.active_cells * 2 < p.num_cells || !lockstep);
@@ -255,9 +278,12 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
     a.act = p.act;
     a.act_count = p.chunk + nc;
   }
+  const void* fn = pull_kernel(variant);
+  int grid = 0;
+  cudaError_t e = coop_grid(p, fn, &grid);
+  if (e != cudaSuccess) return e;
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel(pull_kernel(variant), dim3(p.level_blocks), dim3(swk::kPullThreads), args, 0,
-                                     s);
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(swk::kPullThreads), args, 0, s);
 }
 
 cudaError_t fold_pull(const DevicePtrs& p, cudaStream_t s) {
@@ -314,12 +340,14 @@ extern const PrecisionOps SWK_OPS = {
     SWK_NAME,       (int)sizeof(R), true,       occupancy,     attenuation, init_counts, sweep,
     occupancy_pull, sweep_pull,     kahn_round, schedule_seed, fold_pull,   chemistry,   photon_rate,
     export_rates,   records,        cell_rates, SWK_CARRY != 0,
+    (int)(sizeof(kTuneVariants) / sizeof(int)), kTuneVariants,
 };
 #else
 extern const PrecisionOps SWK_OPS = {
     SWK_NAME,         (int)sizeof(R), false,      occupancy,     attenuation,   init_counts, sweep,
     occupancy_levels, sweep_levels,   kahn_round, schedule_seed, fold_periodic, chemistry,   photon_rate,
     export_rates,     nullptr,        cell_rates, SWK_CARRY != 0,
+    0, nullptr,
 };
 #endif
 

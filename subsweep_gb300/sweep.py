@@ -77,20 +77,20 @@ class Sweep:
 
     def __init__(self, params: SweepParameters, grid: Grid, density, ionized_hydrogen_fraction,
                  temperature, source, precision: str = "fp64", scale_factor: float = 1.0,
-                 device: int = -1, use_graphs: bool = False):
-        self._setup(params, precision, scale_factor, device, use_graphs)
+                 device: int = -1, use_graphs: bool = False, autotune: bool = True):
+        self._setup(params, precision, scale_factor, device, use_graphs, autotune)
         g, init = self._csr(grid, density, ionized_hydrogen_fraction, temperature, source)
         self._finish(self._lib.sw_create(ctypes.byref(self._p), ctypes.byref(g), ctypes.byref(init),
                                          ctypes.byref(self._hnew)), grid.num_cells)
 
     @classmethod
     def batch(cls, params: SweepParameters, boxes, precision: str = "fp64", scale_factor: float = 1.0,
-              device: int = -1, use_graphs: bool = False) -> "Sweep":
+              device: int = -1, use_graphs: bool = False, autotune: bool = True) -> "Sweep":
         """One handle over independent boxes (sw_create_batch): `boxes` holds
         (grid, density, ionized_hydrogen_fraction, temperature, source) per box; per-cell
         results are concatenated in box order."""
         self = cls.__new__(cls)
-        self._setup(params, precision, scale_factor, device, use_graphs)
+        self._setup(params, precision, scale_factor, device, use_graphs, autotune)
         parts = [self._csr(*box) for box in boxes]
         grids = (_native.SwGridCsr * len(parts))(*[g for g, _ in parts])
         inits = (_native.SwCellInit * len(parts))(*[i for _, i in parts])
@@ -98,7 +98,7 @@ class Sweep:
                                                ctypes.byref(self._hnew)), sum(b[0].num_cells for b in boxes))
         return self
 
-    def _setup(self, params, precision, scale_factor, device, use_graphs):
+    def _setup(self, params, precision, scale_factor, device, use_graphs, autotune):
         self._lib = _native.load_gpu()
         self.params = params
         self.num_directions = params.num_directions()
@@ -126,6 +126,7 @@ class Sweep:
         p.scale_factor = scale_factor
         p.precision = {"fp64": _native.SW_PRECISION_FP64, "mixed": _native.SW_PRECISION_MIXED}[precision]
         p.use_graphs = int(use_graphs)
+        p.autotune = int(autotune)
         p.device = device
         self._p = p
         self._hnew = ctypes.c_void_p()

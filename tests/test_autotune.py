@@ -1,0 +1,39 @@
+"""Autotuning of the mixed path's transport kernel.
+
+The first sweeps of a handle try each candidate variant (lockstep blocks of four
+positions at 4, 5 and 6 target blocks per SM; one and two independent cursors per
+group) and keep the fastest per task.  Every variant sums in the same order, so a tuned
+handle, with or without graph replay after tuning, matches a handle fixed on the
+default variant bit for bit.
+"""
+import numpy as np
+import pytest
+
+from subsweep_gb300 import workloads
+from subsweep_gb300.sweep import Sweep
+
+pytestmark = pytest.mark.gpu
+
+CANDIDATES = {94, 95, 96, 14, 22}
+
+
+@pytest.mark.parametrize("use_graphs", [False, True])
+def test_autotuned_equals_fixed(use_graphs, monkeypatch):
+    monkeypatch.delenv("SUBSWEEP_PULL_VARIANT", raising=False)
+    monkeypatch.delenv("SUBSWEEP_AUTOTUNE", raising=False)
+    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2)
+    mk = lambda tune, graphs: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature,
+                                    w.source, precision="mixed", autotune=tune, use_graphs=graphs)
+    tuned, fixed = mk(True, use_graphs), mk(False, False)
+    for _ in range(6):  # the first steps have 1, 1, 2, 4 and 8 sweeps; tuning needs 5
+        assert tuned.run_sweeps() == fixed.run_sweeps()
+    ft, ff = tuned.fields(), fixed.fields()
+    for k in ft:
+        np.testing.assert_array_equal(ft[k], ff[k], err_msg=k)
+    st = tuned.stats()
+    assert st["pull_variant"] in CANDIDATES
+    assert fixed.stats()["pull_variant"] == 94
+    if use_graphs:
+        assert 0 < st["graph_launches"] < 6  # replay starts once tuning is done
+    tuned.close()
+    fixed.close()

@@ -15,8 +15,9 @@ pytestmark = pytest.mark.gpu
 
 
 def make(w, use_graphs):
+    # without autotuning every step is replayed (tuning runs its trial sweeps directly)
     return Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
-                 precision="mixed", use_graphs=use_graphs)
+                 precision="mixed", use_graphs=use_graphs, autotune=False)
 
 
 @pytest.mark.parametrize("name", ["c2", "c3"])
