@@ -106,8 +106,10 @@ struct ChemSolver {
                         Units::kErgsCentimetersCubedPerS;
     // case B recombination cooling and its derivative
     const double lambda = 315614.0 / t;
-    const double l197 = pow(lambda, 1.97);
-    const double q = pow(lambda / 2.25, 0.376);
+    // lambda^1.97 and (lambda / 2.25)^0.376 from one logarithm
+    const double ln_lambda = log(lambda);
+    const double l197 = exp(1.97 * ln_lambda);
+    const double q = exp(0.376 * (ln_lambda - 0.81093021621632877));  // ln 2.25
     const double a = pow(1.0 + q, 3.72);
     const double recomb_rate = (3.435e-30 * t * l197 / a) * Units::kErgsCentimetersCubedPerS;
     const double c2r = 1.97, c3r = 0.376, c4r = 3.72;
