@@ -144,7 +144,7 @@ def mean_downwind_faces(grid, directions: np.ndarray, sample: int = 60000, seed:
     return float((dots > 0).sum() / (len(cells) * directions.shape[0])) if counts.sum() else 0.0
 
 
-# DRAM bytes per task of the pull transport kernel, measured by ncu
+# DRAM bytes per task of the pull transport kernel (lockstep variant), measured by ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on a level-0 launch of the C2 grid at
 # 64^3 (22,020,096 tasks): 2.254 GB per launch.  The per-launch traffic at other sizes
 # is scaled by the tasks of a launch.
