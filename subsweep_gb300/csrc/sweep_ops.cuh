@@ -202,8 +202,8 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 }
 
 // Variants of the pull kernel: independent cursors (10 * cursors per group + target
-// blocks per SM) or warp-lockstep blocks of four positions (90 + blocks per SM).
-// SUBSWEEP_PULL_VARIANT picks one.
+// blocks per SM), warp-lockstep blocks of four positions (90 + blocks per SM) and their
+// nested-loop form (80 + blocks per SM).  SUBSWEEP_PULL_VARIANT picks one.
 
 const void* pull_kernel(int variant) {
   switch (variant) {
@@ -217,6 +217,9 @@ const void* pull_kernel(int variant) {
     case 95: return (const void*)swk::k_sweep_pull_lock<5>;
     case 96: return (const void*)swk::k_sweep_pull_lock<6>;
     case 14: return (const void*)swk::k_sweep_pull<1, 4>;
+    case 84: return (const void*)swk::k_sweep_pull_lock2<4>;
+    case 85: return (const void*)swk::k_sweep_pull_lock2<5>;
+    case 86: return (const void*)swk::k_sweep_pull_lock2<6>;
     default: return nullptr;
   }
 }
@@ -234,8 +237,9 @@ int pull_variant(const DevicePtrs* p = nullptr) {
 }
 
 // candidates of the autotuner: lockstep blocks of four positions at 4, 5 and 6 target
-// blocks per SM, one independent cursor per group at 4 blocks, two at 2 blocks
-constexpr int kTuneVariants[] = {94, 95, 96, 14, 22};
+// blocks per SM, the nested-loop lockstep form at 4, one independent cursor per group
+// at 4 blocks, two at 2 blocks
+constexpr int kTuneVariants[] = {94, 95, 96, 84, 14, 22};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM
@@ -263,7 +267,7 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, level);
   const int variant = pull_variant(&p);
   // only the lockstep kernels test levels themselves
-  const bool lockstep = variant >= 90;
+  const bool lockstep = variant >= 80;
   bool sparse = level > 0 && (p.active_cells * 2 < p.num_cells || !lockstep);
   if (level > 0 && p.compact_mode == 1) sparse = true;
   if (level > 0 && p.compact_mode == 2 && lockstep) sparse = false;

@@ -653,6 +653,133 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   if (lane == 0 && attempts) atomicAdd(&a.ctl->attempts, attempts);
 }
 
+// Lockstep variant with an outer loop over blocks and an inner retry loop: everything
+// a retry does not change (word addresses, predicates, weights, commit address, cell
+// data) is set up once per block, and the next block's record and slot loads are issued
+// when a block starts, so they overlap its waits.  Same additions in the same order as
+// the other variants.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(PullArgs a) {
+  constexpr uint32_t kGroups = 32 / kPullGroup;
+  static_assert(kPullRounds == 2, "two slot rounds per lane");
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = lane & (kPullGroup - 1);
+  const uint32_t g = lane / kPullGroup;
+  const uint32_t gmask = ((1u << kPullGroup) - 1u) << (g * kPullGroup);
+  const uint32_t W = gridDim.x * (kPullThreads / 32);
+  const uint32_t count = a.act ? *a.act_count : a.count;
+  const uint32_t sweep = sweep_number(a);
+  const bool check_level = a.act == nullptr && a.current_level > 0;
+  uint32_t b = blockIdx.x * (kPullThreads / 32) + threadIdx.x / 32;
+  auto idx = [&](uint32_t bb) { return bb * kGroups + g; };
+  // pipeline: record + slots of block b, record of b + W, position of b + 2W
+  const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+  uint4 cur = z, n1 = z;
+  uint2 s[kPullRounds];
+  uint32_t p2 = 0;
+  if (idx(b) < count) cur = a.rec[pull_pos(a, idx(b))];
+  if (idx(b + W) < count) n1 = a.rec[pull_pos(a, idx(b + W))];
+  if (idx(b + 2 * W) < count) p2 = pull_pos(a, idx(b + 2 * W));
+  load_slots(a, cur, gl, s);
+  uint32_t solved = 0, attempts = 0;
+  bool stop = false;
+  while (!stop && b * kGroups < count) {
+    // next block's pipeline stages, issued now
+    uint2 ns[kPullRounds];
+    uint4 n2 = z;
+    uint32_t p3 = 0;
+    if (idx(b + W) < count) load_slots(a, n1, gl, ns);
+    if (idx(b + 2 * W) < count) n2 = a.rec[p2];
+    if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
+    // this block's task
+    bool have = idx(b) < count;
+    const uint32_t t = rec_dir(cur) * a.Np + cur.x;
+    float src = 0.f, per = 0.f, att = 0.f;
+    if (have) {
+      if (check_level && a.level[cur.x] < a.current_level) {  // inactive: keep q, stamp the word
+        if (gl == 0) {
+          const unsigned long long own = ld_relaxed_u64(a.qe + t);
+          st_relaxed_u64(a.qe + t, (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
+        }
+        have = false;
+      } else if (gl == 0) {
+        src = a.src_dir[cur.x];
+        per = __ldcg(a.periodic + t);
+        att = (float)a.att[cur.x];
+      }
+    }
+    const uint32_t n_up = have ? rec_count(cur) : 0u;
+    const bool p0 = gl < n_up, p1 = gl + kPullGroup < n_up;
+    const unsigned long long* q0 = a.qe + s[0].x;
+    const unsigned long long* q1 = a.qe + s[1].x;
+    const float wt0 = __uint_as_float(s[0].y), wt1 = __uint_as_float(s[1].y);
+    const bool big = n_up > (uint32_t)(kPullRounds * kPullGroup);
+    unsigned long long w0 = 0;
+    uint32_t wait_ns = 32;
+    while (true) {
+      const unsigned long long x0 = ld_relaxed_u64_if(p0, q0);
+      const unsigned long long x1 = ld_relaxed_u64_if(p1, q1);
+      bool bad = (p0 && !word_current(x0, sweep)) || (p1 && !word_current(x1, sweep));
+      float in = p0 ? fmaf(wt0, __uint_as_float((uint32_t)x0), 0.f) : 0.f;
+      if (p1) in = fmaf(wt1, __uint_as_float((uint32_t)x1), in);
+      if (big) {
+        for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
+          const uint2 sj = a.slots[rec_offset(cur) + j];
+          const unsigned long long wn = ld_relaxed_u64(a.qe + sj.x);
+          bad = bad || !word_current(wn, sweep);
+          in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
+        }
+      }
+      const uint32_t badmask = __ballot_sync(0xffffffffu, bad);
+#pragma unroll
+      for (int o = 1; o < kPullGroup; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, kPullGroup);
+      const bool commit = have && (badmask & gmask) == 0u;
+      if (have && gl == 0) ++attempts;
+      if (commit && gl == 0) {
+        const float rt = (in + src) + per;                      // Site::get_rate, site.rs:53-56
+        const float out = (rt < a.threshold) ? 0.f : rt * att;  // get_outgoing_rate
+        a.incoming[t] = in;
+        st_relaxed_u64(a.qe + t, pack_qe(out * __uint_as_float(cur.y), sweep));
+        ++solved;
+      }
+      have = have && !commit;
+      if (!__any_sync(0xffffffffu, have)) break;
+      if (__any_sync(0xffffffffu, commit)) {
+        w0 = 0;
+        wait_ns = 32;
+        continue;
+      }
+      int expired = 0;
+      if (lane == 0) {
+        const unsigned long long now = globaltimer_ns();
+        if (w0 == 0) w0 = now;
+        expired = (now - w0 > a.timeout_ns) || (*(volatile uint32_t*)&a.ctl->error != 0);
+      }
+      if (__shfl_sync(0xffffffffu, expired, 0)) {
+        if (lane == 0) atomicOr(&a.ctl->error, kErrStall);
+        stop = true;
+        break;
+      }
+      __nanosleep(wait_ns);
+      wait_ns = min(wait_ns * 2, 256u);
+    }
+    // advance the pipeline by one block
+    b += W;
+    cur = n1;
+#pragma unroll
+    for (int r = 0; r < kPullRounds; ++r) s[r] = ns[r];
+    n1 = n2;
+    p2 = p3;
+  }
+  unsigned long long ts = solved, ta = attempts;
+  for (int o = 16; o > 0; o >>= 1) {
+    ts += __shfl_xor_sync(0xffffffffu, ts, o);
+    ta += __shfl_xor_sync(0xffffffffu, ta, o);
+  }
+  if (lane == 0 && ts) atomicAdd(&a.ctl->tasks, ts);
+  if (lane == 0 && ta) atomicAdd(&a.ctl->attempts, ta);
+}
+
 // Gathered incoming rate of (c, d): sum over upwind LOCAL faces of |s| q(n, d), or
 // over LOCAL_PERIODIC faces when `periodic_faces`.
 __device__ __forceinline__ float gather_in(const PullArgs& a, uint32_t c, uint32_t d, bool periodic_faces) {
