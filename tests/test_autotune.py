@@ -25,7 +25,8 @@ def test_autotuned_equals_fixed(use_graphs, monkeypatch):
     mk = lambda tune, graphs: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature,
                                     w.source, precision="mixed", autotune=tune, use_graphs=graphs)
     tuned, fixed = mk(True, use_graphs), mk(False, False)
-    for _ in range(6):  # the first steps have 1, 1, 2, 4 and 8 sweeps; tuning needs 6
+    steps = 8  # the first steps have 1, 1, 2, 4 and 8 sweeps; tuning needs one per candidate
+    for _ in range(steps):
         assert tuned.run_sweeps() == fixed.run_sweeps()
     ft, ff = tuned.fields(), fixed.fields()
     for k in ft:
@@ -34,6 +35,6 @@ def test_autotuned_equals_fixed(use_graphs, monkeypatch):
     assert st["pull_variant"] in CANDIDATES
     assert fixed.stats()["pull_variant"] == 94
     if use_graphs:
-        assert 0 < st["graph_launches"] < 6  # replay starts once tuning is done
+        assert 0 < st["graph_launches"] < steps  # replay starts once tuning is done
     tuned.close()
     fixed.close()
