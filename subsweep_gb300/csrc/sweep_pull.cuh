@@ -528,14 +528,25 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArg
 // positions b = w, w + W, ... (group g of the warp takes position 4b + g) and advances
 // all four together once every one has committed, so the pipeline shift is a
 // warp-uniform branch and the four groups' records and slots are contiguous.
-template <int kMinBlocks>
+// this lane's slots l, l + G, ... (RR of them) of the task whose record is r
+template <int G, int RR>
+__device__ __forceinline__ void load_slots_g(const PullArgs& a, const uint4& r, uint32_t gl, uint2 (&s)[RR]) {
+  const uint32_t n = rec_count(r);
+  const uint2* base = a.slots + rec_offset(r);
+#pragma unroll
+  for (int k = 0; k < RR; ++k)
+    if (gl + k * G < n) s[k] = __ldg(base + gl + k * G);
+}
+
+template <int kMinBlocks, int G = kPullGroup>
 __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(PullArgs a) {
-  constexpr uint32_t kGroups = 32 / kPullGroup;
+  constexpr int RR = kPullGroup * kPullRounds / G;  // slot rounds per lane (16 slots in registers)
+  constexpr uint32_t kGroups = 32 / G;
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t gl = lane & (kPullGroup - 1);
-  const uint32_t g = lane / kPullGroup;
-  const uint32_t gfirst = g * kPullGroup;
-  const uint32_t gmask = ((1u << kPullGroup) - 1u) << gfirst;
+  const uint32_t gl = lane & (G - 1);
+  const uint32_t g = lane / G;
+  const uint32_t gfirst = g * G;
+  const uint32_t gmask = ((1u << G) - 1u) << gfirst;
   const uint32_t W = gridDim.x * (kPullThreads / 32);
   const uint32_t count = a.act ? *a.act_count : a.count;
   const uint32_t sweep = sweep_number(a);
@@ -544,14 +555,14 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   auto idx = [&](uint32_t bb) { return bb * kGroups + g; };
   const uint4 z = make_uint4(0u, 0u, 0u, 0u);
   uint4 cur = z, n1 = z, n2 = z;
-  uint2 s[kPullRounds], ns[kPullRounds];
+  uint2 s[RR], ns[RR];
   uint32_t p3 = 0;
   if (idx(b) < count) cur = a.rec[pull_pos(a, idx(b))];
   if (idx(b + W) < count) n1 = a.rec[pull_pos(a, idx(b + W))];
   if (idx(b + 2 * W) < count) n2 = a.rec[pull_pos(a, idx(b + 2 * W))];
   if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
-  load_slots(a, cur, gl, s);
-  if (idx(b + W) < count) load_slots(a, n1, gl, ns);
+  load_slots_g<G, RR>(a, cur, gl, s);
+  if (idx(b + W) < count) load_slots_g<G, RR>(a, n1, gl, ns);
   bool have = idx(b) < count;
   // the leader's cell data of the current task, loaded once per block; without a
   // compacted list, a sweep above level 0 also tests the cell's level here
@@ -582,19 +593,19 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
       have = false;
     }
     const uint32_t n_up = have ? rec_count(cur) : 0u;
-    unsigned long long w[kPullRounds];
+    unsigned long long w[RR];
 #pragma unroll
-    for (int r = 0; r < kPullRounds; ++r) w[r] = ld_relaxed_u64_if(gl + r * kPullGroup < n_up, a.qe + s[r].x);
+    for (int r = 0; r < RR; ++r) w[r] = ld_relaxed_u64_if(gl + r * G < n_up, a.qe + s[r].x);
     float in = 0.f;
     bool bad = false;
 #pragma unroll
-    for (int r = 0; r < kPullRounds; ++r) {
-      if (gl + r * kPullGroup < n_up) {
+    for (int r = 0; r < RR; ++r) {
+      if (gl + r * G < n_up) {
         bad = bad || !word_current(w[r], sweep);
         in = fmaf(__uint_as_float(s[r].y), __uint_as_float((uint32_t)w[r]), in);
       }
     }
-    for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
+    for (uint32_t j = gl + RR * G; j < n_up; j += G) {
       const uint2 sj = a.slots[rec_offset(cur) + j];
       const unsigned long long wn = ld_relaxed_u64(a.qe + sj.x);
       bad = bad || !word_current(wn, sweep);
@@ -602,7 +613,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
     }
     const uint32_t badmask = __ballot_sync(0xffffffffu, bad);
 #pragma unroll
-    for (int o = 1; o < kPullGroup; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, kPullGroup);
+    for (int o = 1; o < G; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, G);
     const bool commit = have && (badmask & gmask) == 0u;
     if (have && gl == 0) ++attempts;
     if (commit && gl == 0) {
@@ -619,10 +630,10 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
       b += W;
       cur = n1;
 #pragma unroll
-      for (int r = 0; r < kPullRounds; ++r) s[r] = ns[r];
+      for (int r = 0; r < RR; ++r) s[r] = ns[r];
       n1 = n2;
       have = idx(b) < count;
-      if (idx(b + W) < count) load_slots(a, n1, gl, ns);
+      if (idx(b + W) < count) load_slots_g<G, RR>(a, n1, gl, ns);
       if (idx(b + 2 * W) < count) n2 = a.rec[p3];
       if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
       load_cell();
