@@ -137,3 +137,13 @@ def _cyclic_grid():
                         kind=np.zeros(e, np.uint8), area=np.ones(e), normal=np.array(nrms),
                         volume=np.ones(3), size=np.ones(3), position=np.zeros((3, 3)),
                         box_size=np.ones(3), periodic=False)
+
+
+def test_stats_fields_used_by_smoke_and_bench():
+    """smoke() and bench.py read these sw_stats fields by name."""
+    from subsweep_gb300 import _native
+    names = {n for n, _ in _native.SwStats._fields_}
+    for k in ("tasks", "chem_cells", "level_sweeps", "step_ms", "transport_kernel_ms", "transport_launches",
+              "kernel_launches", "levelled_sweeps", "schedule_levels", "transport_attempts", "chem_attempts",
+              "sweep_ms", "chem_ms", "level_ms", "pull_variant", "graph_launches"):
+        assert k in names, k
