@@ -64,6 +64,9 @@ struct DevicePtrs {
   uint32_t* order;           // levelled schedule: task ids grouped by Kahn level
   const uint32_t* lvl;       // level offsets into order [num_sched_levels + 1]
   uint32_t num_sched_levels; // 0: no levelled schedule (cyclic graph)
+  void* push_rec;            // push path: uint4 record per schedule position (or null)
+  uint32_t* push_tgt;        // push path: downwind targets (neighbour | kind << 30)
+  double* push_frac;         // push path: downwind fractions eff / total (FP64)
   void* pull_rec;            // pull path: uint4 task record per schedule position
   void* pull_slots;          // pull path: uint2 upwind slots of all positions
   uint32_t* act;             // pull path: compacted active positions of the current sweep
@@ -113,6 +116,9 @@ struct PrecisionOps {
   // pull path: transport kernel variants the autotuner tries (count, ids); 0 on the push path
   int num_tune_variants;
   const int* tune_variants;
+  // push path, once per grid: precomputed downwind fractions (phases as records);
+  // nullptr on the pull path
+  cudaError_t (*push_records)(const DevicePtrs&, int phase, unsigned long long* scratch, cudaStream_t);
 };
 
 // pull path: transport kernel variant used without autotuning (lockstep blocks of four

@@ -326,6 +326,71 @@ sw_status build_schedule(sw_handle* h) {
   return SW_OK;
 }
 
+// Push path: precomputed downwind fractions of every schedule position, when they fit
+// (records within a quarter and records + slots within half of the free device
+// memory; SUBSWEEP_FP64_RECORDS=0 never builds them, =1 always tries).  Without them
+// the transport computes the geometry on the fly.
+sw_status build_push_records(sw_handle* h) {
+  swh::DevicePtrs& p = h->p;
+  if (!h->ops->push_records || p.num_sched_levels == 0) return SW_OK;
+  int mode = -1;
+  if (const char* env = std::getenv("SUBSWEEP_FP64_RECORDS")) mode = std::atoi(env) != 0 ? 1 : 0;
+  if (mode == 0) return SW_OK;
+  const int64_t positions = h->N * (int64_t)h->D;
+  const size_t nc = (size_t)((positions + swk::kCompactChunk - 1) / swk::kCompactChunk);
+  const size_t rec_bytes = (size_t)positions * sizeof(uint4);
+  size_t free_b = 0, total_b = 0;
+  SW_CUDA(h, cudaMemGetInfo(&free_b, &total_b), "memory info");
+  if (mode < 0 && rec_bytes > free_b / 4) return SW_OK;
+  struct DeviceScratch {
+    void* ptr = nullptr;
+    ~DeviceScratch() {
+      if (ptr) cudaFree(ptr);
+    }
+  } rec_mem, off_mem;
+  if (cudaMalloc(&rec_mem.ptr, rec_bytes) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return SW_OK;  // no room: the geometry path
+  }
+  SW_CUDA(h, cudaMalloc(&off_mem.ptr, (nc + 1) * sizeof(unsigned long long)), "record scratch");
+  auto* chunk_off = static_cast<unsigned long long*>(off_mem.ptr);
+  p.push_rec = rec_mem.ptr;
+  cudaError_t ce = h->ops->push_records(p, 0, chunk_off, h->stream);
+  unsigned long long total = 0;
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(&total, chunk_off + nc, sizeof(total), cudaMemcpyDeviceToHost, h->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+  p.push_rec = nullptr;
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "downwind fraction count kernels");
+  const size_t slot_bytes = (size_t)total * (sizeof(uint32_t) + sizeof(double));
+  if (mode < 0 && rec_bytes + slot_bytes > free_b / 2) return SW_OK;
+  uint32_t* tgt = nullptr;
+  double* frac = nullptr;
+  if (!h->alloc(&tgt, std::max<unsigned long long>(total, 1)) || !h->alloc(&frac, std::max<unsigned long long>(total, 1))) {
+    (void)cudaGetLastError();
+    return SW_OK;
+  }
+  p.push_rec = rec_mem.ptr;
+  p.push_tgt = tgt;
+  p.push_frac = frac;
+  ce = h->ops->push_records(p, 1, chunk_off, h->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+  uint32_t err = 0;
+  if (ce == cudaSuccess) ce = cudaMemcpy(&err, &p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost);
+  if (ce != cudaSuccess) {
+    p.push_rec = nullptr;
+    return h->cuda_fail(ce, "downwind fraction kernel");
+  }
+  if (err & swk::kErrRecords) {
+    p.push_rec = nullptr;
+    return h->fail(SW_ERR_CUDA, "downwind classification disagrees with its count");
+  }
+  h->allocations.push_back(rec_mem.ptr);  // kept for the handle's lifetime
+  rec_mem.ptr = nullptr;
+  h->stats_upwind_slots = (int64_t)total;
+  return SW_OK;
+}
+
 // Pull path: task records and upwind slots of every schedule position (after the
 // schedule, or the id order of a cyclic grid, is in place).
 sw_status build_records(sw_handle* h) {
@@ -771,7 +836,8 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     uint4* rec = nullptr;
     uint32_t *act = nullptr, *chunk = nullptr;
     const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
-    if (ok && pull) ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act, nd) && h->alloc(&chunk, chunks);
+    if (ok) ok = h->alloc(&chunk, chunks);
+    if (ok && pull) ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act, nd);
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
@@ -814,6 +880,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   {
     sw_status st = build_schedule(h);
     if (st == SW_OK) st = build_records(h);
+    if (st == SW_OK) st = build_push_records(h);
     if (st != SW_OK) return bail(st);
   }
   *out = h;

@@ -9,6 +9,8 @@
 #include "sweep_device.cuh"
 #if SWK_PULL
 #include "sweep_pull.cuh"
+#else
+#include "sweep_push_records.cuh"
 #endif
 
 namespace swh {
@@ -83,14 +85,51 @@ cudaError_t occupancy_levels(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep_sched<R>, swk::kLevelThreads, 0);
 }
 
+// The levelled push transport: over the precomputed downwind fractions when the grid
+// has them, else computing the geometry on the fly.
 cudaError_t sweep_levels(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::SweepArgs<R> a = sweep_args(p, level);
-  const uint32_t* order = p.order;
   uint32_t total = (uint32_t)(p.num_cells * p.D);
+#if !SWK_PULL
+  if (p.push_rec) {
+    const uint4* rec = static_cast<const uint4*>(p.push_rec);
+    const uint32_t* tgt = p.push_tgt;
+    const double* frac = p.push_frac;
+    int bps = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, swk::k_sweep_sched_rec<R>,
+                                                                  swk::kLevelThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (p.level_bps_cap >= 1 && p.level_bps_cap < bps) bps = p.level_bps_cap;
+    void* args[] = {&a, &rec, &total, &tgt, &frac};
+    return cudaLaunchCooperativeKernel((const void*)swk::k_sweep_sched_rec<R>, dim3(bps * p.num_sms),
+                                       dim3(swk::kLevelThreads), args, 0, s);
+  }
+#endif
+  const uint32_t* order = p.order;
   void* args[] = {&a, &order, &total};
   return cudaLaunchCooperativeKernel((const void*)swk::k_sweep_sched<R>, dim3(p.level_blocks),
                                      dim3(swk::kLevelThreads), args, 0, s);
 }
+
+#if !SWK_PULL
+// push path, once per grid: phase 0 writes the records' counts and the 64-bit scan of
+// the chunk totals into `scratch` (total at scratch[num_chunks]); phase 1, with
+// push_tgt / push_frac allocated, the offsets and the slots.
+cudaError_t push_records(const DevicePtrs& p, int phase, unsigned long long* scratch, cudaStream_t s) {
+  swk::SweepArgs<R> a = sweep_args(p, 0);
+  uint4* rec = static_cast<uint4*>(p.push_rec);
+  const uint32_t total = (uint32_t)(p.num_cells * p.D);
+  const uint32_t nc = (total + swk::kCompactChunk - 1) / swk::kCompactChunk;
+  if (phase == 0) {
+    swk::k_push_rec_count<R><<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(a, p.order, total, rec);
+    swk::k_push_chunk_sums<R><<<nc, swk::kCompactThreads, 0, s>>>(rec, total, p.chunk);
+    swk::k_push_scan64<R><<<1, 1024, 0, s>>>(p.chunk, nc, scratch);
+  } else {
+    swk::k_push_slots<R><<<nc, swk::kCompactThreads, 0, s>>>(a, rec, total, scratch, p.push_tgt, p.push_frac);
+  }
+  return cudaGetLastError();
+}
+#endif
 
 // Seed of the schedule: dependency counts with every cell active (the caller has set
 // all levels >= 0), tasks without dependencies appended to `order`.
@@ -344,14 +383,14 @@ extern const PrecisionOps SWK_OPS = {
     SWK_NAME,       (int)sizeof(R), true,       occupancy,     attenuation, init_counts, sweep,
     occupancy_pull, sweep_pull,     kahn_round, schedule_seed, fold_pull,   chemistry,   photon_rate,
     export_rates,   records,        cell_rates, SWK_CARRY != 0,
-    (int)(sizeof(kTuneVariants) / sizeof(int)), kTuneVariants,
+    (int)(sizeof(kTuneVariants) / sizeof(int)), kTuneVariants, nullptr,
 };
 #else
 extern const PrecisionOps SWK_OPS = {
     SWK_NAME,         (int)sizeof(R), false,      occupancy,     attenuation,   init_counts, sweep,
     occupancy_levels, sweep_levels,   kahn_round, schedule_seed, fold_periodic, chemistry,   photon_rate,
     export_rates,     nullptr,        cell_rates, SWK_CARRY != 0,
-    0, nullptr,
+    0, nullptr,       push_records,
 };
 #endif
 

@@ -75,10 +75,12 @@ def test_c1_small_fp64_parity():
     run_and_compare(w, steps=4)
 
 
-@pytest.mark.parametrize("transport", ["levels", "queue"])
-def test_c2_small_lognormal_levels_fp64_parity(transport, monkeypatch):
-    """Both transport kernels: the levelled schedule and the dependency-driven queue."""
+@pytest.mark.parametrize("transport,records", [("levels", "1"), ("levels", "0"), ("queue", "0")])
+def test_c2_small_lognormal_levels_fp64_parity(transport, records, monkeypatch):
+    """Both transport kernels: the levelled schedule (over the precomputed downwind
+    fractions, or computing the geometry on the fly) and the dependency-driven queue."""
     monkeypatch.setenv("SUBSWEEP_TRANSPORT", transport)
+    monkeypatch.setenv("SUBSWEEP_FP64_RECORDS", records)
     w = workloads.c2_lognormal(n_per_side=12, num_directions=84, num_levels=4, nthreads=2)
     gpu, orc = run_and_compare(w, steps=6)
     # the level hierarchy must actually be exercised
