@@ -120,7 +120,9 @@ typedef struct {
   int64_t levelled_sweeps;     /* level sweeps run on the precomputed levelled schedule */
   int64_t schedule_levels;     /* Kahn levels of the schedule (0: cyclic grid, no schedule) */
   int64_t transport_attempts;  /* pull-path task attempts, retries included (tasks = success) */
-  int64_t upwind_slots;        /* pull path: upwind LOCAL (face, direction) pairs of the grid */
+  int64_t upwind_slots;        /* precomputed (face, direction) pairs of the grid: upwind LOCAL
+                                  ones on the pull path, downwind LOCAL / LOCAL_PERIODIC ones on
+                                  the push path (0 when the push path computes geometry) */
   int64_t graph_launches;      /* steps replayed from a CUDA graph */
   int64_t pull_variant;        /* mixed path: transport kernel variant in use (autotuned or set) */
 } sw_stats;
