@@ -69,7 +69,12 @@ struct DevicePtrs {
   double* push_frac;         // push path: downwind fractions eff / total (FP64)
   void* pull_rec;            // pull path: uint4 task record per schedule position
   void* pull_slots;          // pull path: uint2 upwind slots of all positions
-  uint32_t* act;             // pull path: compacted active positions of the current sweep
+  uint32_t* act_lv[32];      // pull path: compacted active positions per level (lazily allocated)
+  uint32_t* act_counts;      // pull path: their lengths [32] (device)
+  uint32_t* pos_of_task;     // pull path: schedule position of every task (inverse order)
+  uint32_t* act_bits;        // pull path: one bit per schedule position (sparse compaction)
+  int sparse_sweep;          // pull path: this launch runs over the compacted list of its level
+  int compact_now;           // pull path: ... and builds that list first
   uint32_t* chunk;           // pull path: compaction chunk offsets, count at [num_chunks]
   int64_t active_cells;      // pull path: cells active in the sweep being launched
   int compact_mode;          // pull path: 0 by density, 1 always compact, 2 never (lockstep)

@@ -673,6 +673,7 @@ struct ChemArgs {
   double* species_timestep;
   double max_timestep;
   double threshold;
+  double rate_floor;       // mixed path: rates below it count as below the threshold (0: FP64)
   double safety;
   double scale_factor;
   int prevent_cooling;
@@ -708,7 +709,12 @@ __global__ void k_chemistry(ChemArgs<R> a) {
       rate = (double)s * a.rate_scale + a.source[c];
     }
     double relative_change;
-    if (fabs(rate) < fabs(a.threshold)) {  // chemistry/mod.rs:79-81
+    // chemistry/mod.rs:79-81.  The mixed path also treats a rate below the smallest
+    // value its FP32 transport carries at full precision as insignificant: there the
+    // FP64 path sees a smooth exponential tail, FP32 an underflowed zero, and the
+    // reference's relative change of a zero rate (0/0, capped at 1/epsilon) would send
+    // the cell to the deepest level.
+    if (fabs(rate) < fabs(a.threshold) || fabs(rate) < a.rate_floor) {
       relative_change = 0.0;
     } else {  // chemistry/mod.rs:73-77
       relative_change = fabs(fmin(fabs(fabs(rate - a.previous_rate[c]) / rate), 1.0 / DBL_EPSILON));

@@ -92,6 +92,7 @@ struct sw_handle {
   int64_t stats_upwind_slots = 0;
   int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
   bool trace = false;  // SUBSWEEP_TRACE: one stderr line per level sweep
+  uint32_t act_valid = 0;  // pull path: levels whose compacted list is current this step
   double* series_dev = nullptr;  // time-series partial sums and result (allocated on first use)
   // graph replay of a step (pull path): the instantiated graph, the step shape it was
   // captured for, and the pinned scalars its first node copies to the control block
@@ -834,10 +835,12 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     bool ok = h->alloc(&inc, nd * rb) && h->alloc(&per, nd * rb) && h->alloc(&cnt, nd / 4) &&
               h->alloc(&order, nd) && h->alloc(&ctl, 1);
     uint4* rec = nullptr;
-    uint32_t *act = nullptr, *chunk = nullptr;
+    uint32_t *act_counts = nullptr, *chunk = nullptr, *pos_of_task = nullptr, *act_bits = nullptr;
     const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
     if (ok) ok = h->alloc(&chunk, chunks);
-    if (ok && pull) ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act, nd);
+    if (ok && pull)
+      ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
+           h->alloc(&act_bits, (nd + 31) / 32);
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
@@ -857,7 +860,9 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     cudaMemset(ctl, 0, sizeof(swk::SweepCtl));
     p.qe = qe;
     p.pull_rec = rec;
-    p.act = act;
+    p.act_counts = act_counts;
+    p.pos_of_task = pos_of_task;
+    p.act_bits = act_bits;
     p.chunk = chunk;
     p.incoming = inc;
     p.outgoing = outg;
@@ -896,6 +901,28 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
 // the graph's first node; the error flag stays set across the step's sweeps, so a stall
 // ends the remaining sweeps at once, and is read when the step has finished.  Event
 // nodes around each sweep's transport give the transport kernel time.
+// Pull path: whether the sweep of `level` runs over the compacted list of its active
+// positions (above level 0, fewer than half of the cells active, or a transport
+// variant that cannot test levels itself; SUBSWEEP_COMPACT overrides), and that list's
+// buffer, allocated on first use.
+static bool pull_sparse(sw_handle* h, int level) {
+  const swh::DevicePtrs& p = h->p;
+  if (level <= 0) return false;
+  const int v = p.pull_variant > 0 ? p.pull_variant : swh::kDefaultPullVariant;
+  if (p.compact_mode == 1) return true;
+  if (p.compact_mode == 2 && v >= 80) return false;
+  return h->n_ge_host[level] * 2 < h->N || v < 80;
+}
+
+static sw_status ensure_act_list(sw_handle* h, int level) {
+  if (h->p.act_lv[level]) return SW_OK;
+  uint32_t* buf = nullptr;
+  if (!h->alloc(&buf, (size_t)h->Np * h->D))
+    return h->fail(SW_ERR_OOM, "device allocation of the active positions of level %d failed", level);
+  h->p.act_lv[level] = buf;
+  return SW_OK;
+}
+
 static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
   const swh::PrecisionOps& ops = *h->ops;
   swh::DevicePtrs& p = h->p;
@@ -912,7 +939,11 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     // pull path: compaction or not; push path: levelled schedule or ready queue
     bool variant;
     if (ops.pull) {
-      variant = level > 0 && (p.compact_mode == 1 || (p.compact_mode == 0 && h->n_ge_host[level] * 2 < h->N));
+      variant = pull_sparse(h, level);
+      if (variant) {
+        sw_status st = ensure_act_list(h, level);  // allocations stay outside the capture
+        if (st != SW_OK) return st;
+      }
     } else {
       variant = p.num_sched_levels > 0 && (uint64_t)h->n_ge_host[level] * 16 >= (uint64_t)h->N;
       if (h->force_path == 1) variant = p.num_sched_levels > 0;
@@ -943,17 +974,26 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     swh::DevicePtrs q = p;
     q.epoch_base = &p.ctl->epoch_base;
     int64_t kernels = 3;  // level update (two kernels) and ionization times
+    uint32_t compacted = 0;  // pull path: levels whose list the step has built so far
+    std::vector<int> compact_now(levels.size(), 0);
     for (size_t k = 0; k < levels.size(); ++k) {
       // attenuation, transport, chemistry, the periodic fold, and the counts (push) or
-      // the compaction (pull, sparse sweeps)
+      // the compaction at a sparse level's first sweep (pull)
       kernels += 3 + (p.n_periodic_cells > 0 ? 1 : 0);
-      if (!ops.pull) kernels += 1;
-      else if (variants[k]) kernels += 3;
+      if (!ops.pull) {
+        kernels += 1;
+      } else if (variants[k] && !((compacted >> levels[k]) & 1u)) {
+        compact_now[k] = 1;
+        compacted |= 1u << levels[k];
+        kernels += 4;
+      }
     }
     for (size_t k = 0; k < levels.size() && ce == cudaSuccess; ++k) {
       const int level = levels[k];
       q.epoch = (uint32_t)(k + 1);
       q.active_cells = h->n_ge_host[level];
+      q.sparse_sweep = (ops.pull && variants[k]) ? 1 : 0;
+      q.compact_now = compact_now[k];
       ce = cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, error), h->stream);
       if (ce == cudaSuccess) ce = ops.attenuation(q, level, h->stream);
       if (ce == cudaSuccess && !ops.pull) ce = ops.init_counts(q, level, nullptr, !variants[k], h->stream);
@@ -1003,6 +1043,7 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
     return h->fail(SW_ERR_INVALID_ARG, "x_HII floor above 1 - 1e-10 in the chemistry clamp (reference panics)");
   h->ts = after;
   h->sim_time += elapsed;
+  h->act_valid = 0;  // the step's level update changed the active sets
   float step_ms = 0.f;
   cudaEventElapsedTime(&step_ms, h->ev[5], h->ev[1]);
   const int64_t n = (int64_t)levels.size();
@@ -1111,15 +1152,25 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     bool levelled = h->p.num_sched_levels > 0 && (uint64_t)h->n_ge_host[level] * 16 >= (uint64_t)h->N;
     if (h->force_path == 1) levelled = h->p.num_sched_levels > 0;
     if (h->force_path == 2) levelled = false;
-    const bool trial = ops.pull && h->autotune && !h->tuned;
+    // autotuning trials on dense sweeps only: sparse ones always run the lockstep kernel
+    const bool trial = ops.pull && h->autotune && !h->tuned && !pull_sparse(h, level);
     if (trial) h->p.pull_variant = ops.tune_variants[h->tune_index];
     if (ops.pull) {
       levelled = true;  // the pull path always walks the schedule (or the id order)
       h->p.epoch += 1;
       h->last_epoch = h->p.epoch;
       h->p.active_cells = h->n_ge_host[level];
-      if (level > 0 && (h->p.compact_mode == 1 || (h->p.compact_mode == 0 && h->p.active_cells * 2 < h->N)))
-        launches += 3;  // compaction of the active positions
+      h->p.sparse_sweep = pull_sparse(h, level) ? 1 : 0;
+      h->p.compact_now = 0;
+      if (h->p.sparse_sweep) {
+        sw_status st = ensure_act_list(h, level);
+        if (st != SW_OK) return st;
+        if (!((h->act_valid >> level) & 1u)) {  // first sweep of this level in the step
+          h->p.compact_now = 1;
+          h->act_valid |= 1u << level;
+          launches += 4;  // compaction of the active positions
+        }
+      }
     } else {
       SW_CUDA(h, ops.init_counts(h->p, level, nullptr, !levelled, h->stream), "init_counts kernel");
       launches += 1;
@@ -1183,6 +1234,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   h->ts.advance();
   SW_CUDA(h, cudaEventRecord(h->ev[3], h->stream), "event");
   SW_CUDA(h, swh::launch_update_levels(h->p, h->ts.lowest, h->stream), "level kernels");
+  h->act_valid = 0;  // levels change: the compacted lists are rebuilt next step
   SW_CUDA(h, cudaEventRecord(h->ev[4], h->stream), "event");
   h->sim_time += elapsed;
   SW_CUDA(h, swh::launch_ionization_time(h->p, h->sim_time, h->stream), "ionization time kernel");
@@ -1398,6 +1450,7 @@ sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes) {
   h->p.epoch = hd.epoch;
   h->last_epoch = hd.last_epoch;
   // cells per level for the next step
+  h->act_valid = 0;
   SW_CUDA(h, swh::launch_level_hist(h->p, h->stream), "level histogram");
   return sync_ctl(h);
 }

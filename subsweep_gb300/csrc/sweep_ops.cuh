@@ -3,6 +3,7 @@
 // (R = float, carried neutral fraction); each defines SWK_R, SWK_CARRY and SWK_OPS.
 #pragma once
 
+#include <cmath>
 #include <cstdlib>
 
 #include "launch.h"
@@ -183,6 +184,10 @@ cudaError_t chemistry(const DevicePtrs& p, int level, cudaStream_t s) {
   a.species_timestep = p.species_timestep;
   a.max_timestep = p.max_timestep;
   a.threshold = p.threshold;
+  // FP32 transport: 2^-120 of the stored rate unit (normal FP32, full 24-bit precision,
+  // 6 binary orders above the subnormal range; the unit is 2^(e - 96) of the total
+  // source, so the floor is ~1e-65 of the total luminosity)
+  a.rate_floor = sizeof(R) == 4 ? std::ldexp(1.0, -120) * p.rate_scale : 0.0;
   a.safety = p.chem_safety;
   a.scale_factor = p.scale_factor;
   a.prevent_cooling = p.prevent_cooling;
@@ -230,6 +235,7 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
   uint4* rec = static_cast<uint4*>(p.pull_rec);
   const uint32_t nc = num_chunks(p);
   if (phase == 0) {
+    swk::k_invert_order<<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(p.order, a.count, p.pos_of_task);
     swk::k_pull_rec_count<<<grid_for(p.num_cells * p.D, 256), 256, 0, s>>>(a, p.order, a.count, rec);
     swk::k_pull_slot_chunks<<<nc, swk::kCompactThreads, 0, s>>>(rec, a.count, p.chunk);
     swk::k_scan_chunks64<<<1, swk::kScanThreads, 0, s>>>(p.chunk, nc, chunk_off);
@@ -276,9 +282,10 @@ int pull_variant(const DevicePtrs* p = nullptr) {
 }
 
 // candidates of the autotuner: lockstep blocks of four positions at 4, 5 and 6 target
-// blocks per SM, the nested-loop lockstep form at 4, one independent cursor per group
-// at 4 blocks, two at 2 blocks
-constexpr int kTuneVariants[] = {94, 95, 96, 84, 14, 22};
+// blocks per SM and the nested-loop lockstep form at 4 (the independent-cursor variants
+// measured slower everywhere and would cost trial sweeps: a sweep of a tiny active set
+// is not a trial, so a step may offer a single dense sweep)
+constexpr int kTuneVariants[] = {94, 95, 96, 84};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM
@@ -297,31 +304,36 @@ cudaError_t occupancy_pull(int* blocks_per_sm) {
                                                        swk::kPullThreads, 0);
 }
 
-// Sparse sweeps (above level 0, fewer than half of the cells active) visit only the
-// positions of active cells: a stable compaction of the schedule that also stamps the
-// inactive tasks' words (three launches) precedes the sweep kernel, which reads the
-// count from the device.  Dense sweeps visit every position; the kernel stamps the
+// Sparse sweeps (chosen by the host: above level 0 with fewer than half of the cells
+// active) visit only the positions of active cells, from a stable compaction of the
+// schedule built at the level's first sweep of a step (three launches; the kernel reads
+// the count from the device).  Dense sweeps visit every position; the kernel stamps the
 // inactive tasks itself.
 cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, level);
   const int variant = pull_variant(&p);
-  // only the lockstep kernels test levels themselves
-  const bool lockstep = variant >= 80;
-  bool sparse = level > 0 && (p.active_cells * 2 < p.num_cells || !lockstep);
-  if (level > 0 && p.compact_mode == 1) sparse = true;
-  if (level > 0 && p.compact_mode == 2 && lockstep) sparse = false;
-  if (sparse) {
-    const uint32_t nc = num_chunks(p);
-    swk::k_compact_count<<<nc, swk::kCompactThreads, 0, s>>>(p.order, a.count, p.level, level, p.Np, p.chunk);
-    swk::k_compact_scan<<<1, swk::kScanThreads, 0, s>>>(p.chunk, nc, p.chunk + nc);
-    swk::k_compact_scatter<<<nc, swk::kCompactThreads, 0, s>>>(p.order, a.count, p.level, level, p.Np, p.chunk,
-                                                               p.act, p.qe, p.epoch_base, p.epoch);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    a.act = p.act;
-    a.act_count = p.chunk + nc;
+  if (p.sparse_sweep) {
+    uint32_t* act = p.act_lv[level];
+    uint32_t* cnt = p.act_counts + level;
+    if (!act) return cudaErrorInvalidValue;
+    if (p.compact_now) {  // mark the active cells' positions, then compact the bitmap
+      const uint32_t words = (a.count + 31) / 32;
+      const uint32_t nb = (words + swk::kBitsThreads - 1) / swk::kBitsThreads;
+      cudaError_t e = cudaMemsetAsync(p.act_bits, 0, (size_t)words * sizeof(uint32_t), s);
+      if (e != cudaSuccess) return e;
+      swk::k_mark_active<<<grid_for(p.num_cells, 256), 256, 0, s>>>(p.level, level, (uint32_t)p.num_cells, p.D,
+                                                                      p.Np, p.pos_of_task, p.act_bits);
+      swk::k_bits_count<<<nb, swk::kBitsThreads, 0, s>>>(p.act_bits, words, p.chunk);
+      swk::k_compact_scan<<<1, swk::kScanThreads, 0, s>>>(p.chunk, nb, cnt);
+      swk::k_bits_scatter<<<nb, swk::kBitsThreads, 0, s>>>(p.act_bits, words, p.chunk, act);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    a.act = act;
+    a.act_count = cnt;
   }
-  const void* fn = pull_kernel(variant);
+  // sparse sweeps run the lockstep kernel, which tests the upwind cells' levels
+  const void* fn = pull_kernel(p.sparse_sweep ? kDefaultPullVariant : variant);
   int grid = 0;
   cudaError_t e = coop_grid(p, fn, &grid);
   if (e != cudaSuccess) return e;

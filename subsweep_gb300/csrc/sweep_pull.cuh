@@ -8,9 +8,11 @@
 //   q(c, d) = out(c, d) / A(c, d)
 // together with the number of the sweep that produced it, as one 64-bit word
 // {q bits, sweep << 1 | stamped}, and a task gathers q from its upwind neighbours once
-// all their words carry the current sweep number.  Before a sweep above level 0, the
-// tasks of inactive cells are stamped with the sweep number (stamped bit set) and keep
-// their q: an inactive neighbour's flux persists, as in the reference.  The word is
+// every active one's word carries the current sweep number; an inactive neighbour keeps
+// the q of its last solve (its flux persists, as in the reference).  In a sweep above
+// level 0 over all positions the tasks of inactive cells stamp their words with the
+// sweep number (stamped bit set); over a compacted list of the active positions the
+// consumer tests the neighbour's level instead.  The word is
 // written and read in single 64-bit accesses, so there are no atomics, no counters and
 // no fences on this path.  Tasks are visited in the levelled schedule order, every
 // upwind task lies at an earlier schedule position, and a task whose inputs are not
@@ -262,58 +264,6 @@ __global__ void __launch_bounds__(kCompactThreads) k_pull_slots(PullArgs a, uint
 }
 
 // ---------------------------------------------------------------------------------------
-// Stable compaction of the schedule positions whose cell is active in a sweep of
-// `level` (level[c] >= level): counts per chunk, an exclusive scan of the counts, and
-// the scatter.  Each thread owns kCompactPer consecutive positions.
-
-__device__ __forceinline__ uint32_t active_bits(const uint32_t* order, uint32_t total, const uint8_t* level,
-                                                int cur, uint32_t Np, float inv_np, uint32_t first) {
-  uint32_t bits = 0;
-#pragma unroll
-  for (int k = 0; k < kCompactPer; ++k) {
-    const uint32_t p = first + k;
-    if (p < total) {
-      uint32_t c, d;
-      split_task(order[p], Np, inv_np, c, d);
-      if (level[c] >= cur) bits |= 1u << k;
-    }
-  }
-  return bits;
-}
-
-// exclusive block-wide prefix sum of v (kCompactThreads threads); returns the block total
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& excl) {
-  __shared__ uint32_t warp_sum[kCompactThreads / 32];
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t x = v;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= (uint32_t)o) x += y;
-  }
-  if (lane == 31) warp_sum[warp] = x;
-  __syncthreads();
-  uint32_t base = 0, total = 0;
-  for (int w = 0; w < kCompactThreads / 32; ++w) {
-    const uint32_t ws = warp_sum[w];
-    if ((uint32_t)w < warp) base += ws;
-    total += ws;
-  }
-  __syncthreads();
-  excl = base + x - v;
-  return total;
-}
-
-__global__ void __launch_bounds__(kCompactThreads) k_compact_count(const uint32_t* order, uint32_t total,
-                                                                   const uint8_t* level, int cur, uint32_t Np,
-                                                                   uint32_t* chunk) {
-  const float inv_np = 1.0f / (float)Np;
-  const uint32_t first = blockIdx.x * kCompactChunk + threadIdx.x * kCompactPer;
-  const uint32_t n = __popc(active_bits(order, total, level, cur, Np, inv_np, first));
-  uint32_t excl;
-  const uint32_t sum = block_exclusive_scan(n, excl);
-  if (threadIdx.x == 0) chunk[blockIdx.x] = sum;
-}
-
 // exclusive scan of the chunk counts in place (one block); the total goes to *count
 __global__ void __launch_bounds__(kScanThreads) k_compact_scan(uint32_t* chunk, uint32_t n, uint32_t* count) {
   __shared__ uint32_t warp_sum[kScanThreads / 32];
@@ -342,27 +292,65 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_scan(uint32_t* chunk, 
   if (threadIdx.x == 0) *count = carry;
 }
 
-// Also stamps the words of the inactive tasks with the sweep number (stamped bit set),
-// so the sweep's readiness test is the sweep number alone.  Nothing else touches the
-// words between the previous kernel and the sweep.
-__global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(const uint32_t* order, uint32_t total,
-                                                                     const uint8_t* level, int cur, uint32_t Np,
-                                                                     const uint32_t* chunk, uint32_t* act,
-                                                                     unsigned long long* qe, const uint32_t* epoch_base,
-                                                                     uint32_t epoch) {
-  const uint32_t sweep = epoch_base ? *epoch_base + epoch : epoch;
-  const float inv_np = 1.0f / (float)Np;
-  const uint32_t first = blockIdx.x * kCompactChunk + threadIdx.x * kCompactPer;
-  uint32_t bits = active_bits(order, total, level, cur, Np, inv_np, first);
-  uint32_t excl;
-  block_exclusive_scan(__popc(bits), excl);
-  for (int k = 0; k < kCompactPer; ++k)
-    if (first + k < total && !((bits >> k) & 1u))
-      reinterpret_cast<uint32_t*>(qe + order[first + k])[1] = (sweep << 1) | 1u;
-  uint32_t o = chunk[blockIdx.x] + excl;
+// ---------------------------------------------------------------------------------------
+// Compaction of a sparse level from a bitmap: the inverse of the schedule order gives
+// each active cell's D positions, which set one bit each; a count / scan / scatter over
+// the bitmap words then yields the active positions in schedule order.  The work is the
+// active cells' tasks plus one pass over N*D/8 bytes.
+
+__global__ void k_invert_order(const uint32_t* order, uint32_t total, uint32_t* pos_of_task) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x)
+    pos_of_task[order[p]] = p;
+}
+
+__global__ void k_mark_active(const uint8_t* level, int cur, uint32_t n, int D, uint32_t Np,
+                              const uint32_t* pos_of_task, uint32_t* bitmap) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    if (level[c] < cur) continue;
+    for (int d = 0; d < D; ++d) {
+      const uint32_t p = pos_of_task[(size_t)d * Np + c];
+      atomicOr(bitmap + (p >> 5), 1u << (p & 31u));
+    }
+  }
+}
+
+constexpr int kBitsThreads = 256;  // one bitmap word per thread, kBitsThreads words per chunk
+
+__global__ void __launch_bounds__(kBitsThreads) k_bits_count(const uint32_t* bitmap, uint32_t words, uint32_t* chunk) {
+  const uint32_t w = blockIdx.x * kBitsThreads + threadIdx.x;
+  uint32_t n = w < words ? __popc(bitmap[w]) : 0u;
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  __shared__ uint32_t ws[kBitsThreads / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t s = 0;
+    for (int i = 0; i < kBitsThreads / 32; ++i) s += ws[i];
+    chunk[blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kBitsThreads) k_bits_scatter(const uint32_t* bitmap, uint32_t words,
+                                                               const uint32_t* chunk, uint32_t* act) {
+  const uint32_t w = blockIdx.x * kBitsThreads + threadIdx.x;
+  uint32_t bits = w < words ? bitmap[w] : 0u;
+  // block-exclusive prefix of the per-thread counts
+  __shared__ uint32_t ws[kBitsThreads / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t mine = __popc(bits);
+  uint32_t x = mine;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  uint32_t base = 0;
+  for (uint32_t i = 0; i < warp; ++i) base += ws[i];
+  uint32_t o = chunk[blockIdx.x] + base + x - mine;
   while (bits) {
     const int k = __ffs(bits) - 1;
-    act[o++] = first + k;
+    act[o++] = w * 32u + (uint32_t)k;
     bits &= bits - 1;
   }
 }
@@ -564,9 +552,12 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   load_slots_g<G, RR>(a, cur, gl, s);
   if (idx(b + W) < count) load_slots_g<G, RR>(a, n1, gl, ns);
   bool have = idx(b) < count;
-  // the leader's cell data of the current task, loaded once per block; without a
-  // compacted list, a sweep above level 0 also tests the cell's level here
+  // the leader's cell data of the current task, loaded once per block.  Above level 0,
+  // a sweep over every position tests each task's cell level here and stamps the
+  // words of inactive tasks; a sweep over a compacted list of active positions
+  // (`sparse`) instead tests the upwind cells' levels when their words are not current.
   const bool check_level = a.act == nullptr && a.current_level > 0;
+  const bool sparse = a.act != nullptr && a.current_level > 0;
   float src = 0.f, per = 0.f, att = 0.f;
   bool active = true;
   auto load_cell = [&]() {
@@ -593,22 +584,30 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
       have = false;
     }
     const uint32_t n_up = have ? rec_count(cur) : 0u;
+    const uint32_t dnp = rec_dir(cur) * a.Np;
     unsigned long long w[RR];
+    uint32_t lv[RR];
 #pragma unroll
-    for (int r = 0; r < RR; ++r) w[r] = ld_relaxed_u64_if(gl + r * G < n_up, a.qe + s[r].x);
+    for (int r = 0; r < RR; ++r) {
+      const bool pr = gl + r * G < n_up;
+      w[r] = ld_relaxed_u64_if(pr, a.qe + s[r].x);
+      lv[r] = (sparse && pr) ? a.level[s[r].x - dnp] : 0xffu;
+    }
     float in = 0.f;
     bool bad = false;
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
       if (gl + r * G < n_up) {
-        bad = bad || !word_current(w[r], sweep);
+        // an upwind cell inactive in this sweep keeps the q of its last solve
+        bad = bad || (!word_current(w[r], sweep) && lv[r] >= (uint32_t)a.current_level);
         in = fmaf(__uint_as_float(s[r].y), __uint_as_float((uint32_t)w[r]), in);
       }
     }
     for (uint32_t j = gl + RR * G; j < n_up; j += G) {
       const uint2 sj = a.slots[rec_offset(cur) + j];
       const unsigned long long wn = ld_relaxed_u64(a.qe + sj.x);
-      bad = bad || !word_current(wn, sweep);
+      const uint32_t lj = sparse ? a.level[sj.x - dnp] : 0xffu;
+      bad = bad || (!word_current(wn, sweep) && lj >= (uint32_t)a.current_level);
       in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
     }
     const uint32_t badmask = __ballot_sync(0xffffffffu, bad);
