@@ -61,6 +61,7 @@ struct DevicePtrs {
   unsigned long long* qe;    // pull path: {q, sweep number} per task
   uint32_t epoch;            // pull path: number of the current level sweep
   const uint32_t* epoch_base; // graph replay: sweep numbers are *epoch_base + epoch
+  uint32_t* cell_sweep;      // pull path: number of the last sweep that solved each cell
   uint32_t* order;           // levelled schedule: task ids grouped by Kahn level
   const uint32_t* lvl;       // level offsets into order [num_sched_levels + 1]
   uint32_t num_sched_levels; // 0: no levelled schedule (cyclic graph)
@@ -72,6 +73,8 @@ struct DevicePtrs {
   uint32_t* act_lv[32];      // pull path: compacted active positions per level (lazily allocated)
   uint32_t* act_counts;      // pull path: their lengths [32] (device)
   uint32_t* pos_of_task;     // pull path: schedule position of every task (inverse order)
+  uint8_t* fold_cnt;         // pull path: upwind periodic faces per (periodic cell, direction)
+  void* fold_slots;          // pull path: their uint2 {upwind task, weight}, 4 per entry
   uint32_t* act_bits;        // pull path: one bit per schedule position (sparse compaction)
   int sparse_sweep;          // pull path: this launch runs over the compacted list of its level
   int compact_now;           // pull path: ... and builds that list first

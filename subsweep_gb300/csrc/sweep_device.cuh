@@ -641,9 +641,13 @@ __global__ void k_fold_periodic(R* periodic, R* pending, const uint32_t* cells, 
 // (hydrogen_only/mod.rs:72-88); direction-independent, so computed once per cell.
 template <bool kCarryNeutral>
 __global__ void k_attenuation(uint32_t n, const uint8_t* level, int current_level, const double* density,
-                              const double* xhii, const double* yneu, const double* size, double* att) {
+                              const double* xhii, const double* yneu, const double* size, double* att,
+                              uint32_t* cell_sweep, const uint32_t* epoch_base, uint32_t epoch) {
+  // pull path: the number of the sweep that solves each active cell
+  const uint32_t sweep = cell_sweep ? (epoch_base ? *epoch_base + epoch : epoch) : 0u;
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
     if (level[c] < current_level) continue;
+    if (cell_sweep) cell_sweep[c] = sweep;
     const double neutral = kCarryNeutral ? yneu[c] : (1.0 - xhii[c]);
     const double nhn = density[c] / Units::kProtonMass * neutral;
     att[c] = exp(-nhn * Units::kSigma * size[c]);

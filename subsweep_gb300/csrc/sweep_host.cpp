@@ -752,6 +752,17 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (!pcells.empty()) cudaMemcpy(d_pc, pcells.data(), pcells.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     p.periodic_cells = d_pc;
     p.n_periodic_cells = (uint32_t)pcells.size();
+    if (h->ops->pull && !pcells.empty()) {  // the fold's precomputed upwind periodic faces
+      uint8_t* fcnt = nullptr;
+      uint2* fslots = nullptr;
+      const size_t entries = pcells.size() * (size_t)D;
+      if (!h->alloc(&fcnt, entries) || !h->alloc(&fslots, entries * 4)) {
+        h->fail(SW_ERR_OOM, "device allocation of the periodic fold slots failed");
+        return bail(SW_ERR_OOM);
+      }
+      p.fold_cnt = fcnt;
+      p.fold_slots = fslots;
+    }
   }
   // directions
   {
@@ -836,11 +847,12 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
               h->alloc(&order, nd) && h->alloc(&ctl, 1);
     uint4* rec = nullptr;
     uint32_t *act_counts = nullptr, *chunk = nullptr, *pos_of_task = nullptr, *act_bits = nullptr;
+    uint32_t* cell_sweep = nullptr;
     const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
     if (ok) ok = h->alloc(&chunk, chunks);
     if (ok && pull)
       ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
-           h->alloc(&act_bits, (nd + 31) / 32);
+           h->alloc(&act_bits, (nd + 31) / 32) && h->alloc(&cell_sweep, (size_t)h->Np);
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
@@ -852,6 +864,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     cudaMemset(cnt, 0, nd);
     if (pull) {
       cudaMemset(qe, 0, nd * sizeof(unsigned long long));
+      cudaMemset(cell_sweep, 0, (size_t)h->Np * sizeof(uint32_t));
     } else {
       cudaMemset(outg, 0, nd * rb);
       cudaMemset(pend, 0, nd * rb);
@@ -863,6 +876,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     p.act_counts = act_counts;
     p.pos_of_task = pos_of_task;
     p.act_bits = act_bits;
+    p.cell_sweep = cell_sweep;
     p.chunk = chunk;
     p.incoming = inc;
     p.outgoing = outg;
@@ -1146,7 +1160,6 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     expected += (uint64_t)h->n_ge_host[level] * (uint64_t)h->D;
     SW_CUDA(h, cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset queue");
     SW_CUDA(h, cudaEventRecord(h->ev[0], h->stream), "event");
-    SW_CUDA(h, ops.attenuation(h->p, level, h->stream), "attenuation kernel");
     // Sweeps with at least 1/16 of the cells active walk the precomputed schedule;
     // sparser ones use the dependency-driven queue, which touches only active tasks.
     bool levelled = h->p.num_sched_levels > 0 && (uint64_t)h->n_ge_host[level] * 16 >= (uint64_t)h->N;
@@ -1171,7 +1184,10 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
           launches += 4;  // compaction of the active positions
         }
       }
-    } else {
+    }
+    // after the pull path's sweep number advanced: attenuation records it per solved cell
+    SW_CUDA(h, ops.attenuation(h->p, level, h->stream), "attenuation kernel");
+    if (!ops.pull) {
       SW_CUDA(h, ops.init_counts(h->p, level, nullptr, !levelled, h->stream), "init_counts kernel");
       launches += 1;
     }
@@ -1373,6 +1389,7 @@ static std::vector<CheckpointSection> checkpoint_sections(sw_handle* h) {
   };
   if (h->ops->pull) {
     v.push_back({p.qe, nd * 8});
+    v.push_back({p.cell_sweep, n * 4});
   } else {
     v.push_back({p.outgoing, nd * rb});
     v.push_back({p.pending, nd * rb});

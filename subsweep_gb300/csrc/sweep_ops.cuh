@@ -61,7 +61,8 @@ cudaError_t occupancy(int* blocks_per_sm) {
 
 cudaError_t attenuation(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::k_attenuation<kCarry><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
-      (uint32_t)p.num_cells, p.level, level, p.density, p.xhii, p.yneu, p.size, p.att);
+      (uint32_t)p.num_cells, p.level, level, p.density, p.xhii, p.yneu, p.size, p.att, p.cell_sweep,
+      p.epoch_base, p.epoch);
   return cudaGetLastError();
 }
 
@@ -217,6 +218,7 @@ swk::PullArgs pull_args(const DevicePtrs& p, int level) {
   a.current_level = level;
   a.epoch = p.epoch;
   a.epoch_base = p.epoch_base;
+  a.cell_sweep = p.cell_sweep;
   a.timeout_ns = p.timeout_ns;
   a.rec = static_cast<const uint4*>(p.pull_rec);
   a.slots = static_cast<const uint2*>(p.pull_slots);
@@ -242,6 +244,9 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
   } else {
     swk::k_pull_slots<<<nc, swk::kCompactThreads, 0, s>>>(a, rec, a.count, chunk_off,
                                                           static_cast<uint2*>(p.pull_slots));
+    if (p.n_periodic_cells > 0)
+      swk::k_fold_build<<<grid_for((int64_t)p.n_periodic_cells * p.D, 256), 256, 0, s>>>(
+          a, p.periodic_cells, p.n_periodic_cells, p.fold_cnt, static_cast<uint2*>(p.fold_slots));
   }
   return cudaGetLastError();
 }
@@ -344,8 +349,9 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
 cudaError_t fold_pull(const DevicePtrs& p, cudaStream_t s) {
   if (p.n_periodic_cells == 0) return cudaSuccess;
   swk::PullArgs a = pull_args(p, 0);
-  swk::k_fold_pull<<<grid_for((int64_t)p.n_periodic_cells * p.D, 256), 256, 0, s>>>(
-      a, static_cast<float*>(p.periodic), p.periodic_cells, p.n_periodic_cells);
+  const dim3 grid((p.n_periodic_cells + 255) / 256, p.D);
+  swk::k_fold_pull<<<grid, 256, 0, s>>>(a, static_cast<float*>(p.periodic), p.periodic_cells, p.n_periodic_cells,
+                                        p.fold_cnt, static_cast<const uint2*>(p.fold_slots));
   return cudaGetLastError();
 }
 
