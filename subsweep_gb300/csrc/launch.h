@@ -62,6 +62,9 @@ struct DevicePtrs {
   uint32_t epoch;            // pull path: number of the current level sweep
   const uint32_t* epoch_base; // graph replay: sweep numbers are *epoch_base + epoch
   uint32_t* cell_sweep;      // pull path: number of the last sweep that solved each cell
+  void* cellpack;            // pull path: uint2 per cell {(float) attenuation or inactive mark, source / D}
+  float* per_pos;            // pull path: periodic source of every schedule position
+  uint32_t lvl_words;        // level offsets allocated (a multiple of 4, >= num_sched_levels + 1)
   uint32_t* order;           // levelled schedule: task ids grouped by Kahn level
   const uint32_t* lvl;       // level offsets into order [num_sched_levels + 1]
   uint32_t num_sched_levels; // 0: no levelled schedule (cyclic graph)

@@ -642,15 +642,22 @@ __global__ void k_fold_periodic(R* periodic, R* pending, const uint32_t* cells, 
 template <bool kCarryNeutral>
 __global__ void k_attenuation(uint32_t n, const uint8_t* level, int current_level, const double* density,
                               const double* xhii, const double* yneu, const double* size, double* att,
-                              uint32_t* cell_sweep, const uint32_t* epoch_base, uint32_t epoch) {
-  // pull path: the number of the sweep that solves each active cell
+                              uint32_t* cell_sweep, const uint32_t* epoch_base, uint32_t epoch, uint2* cellpack,
+                              const float* src32) {
+  // pull path: the number of the sweep that solves each active cell, and per cell the
+  // pair {(float) attenuation, source / D} (attenuation 0xffffffff: inactive)
   const uint32_t sweep = cell_sweep ? (epoch_base ? *epoch_base + epoch : epoch) : 0u;
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-    if (level[c] < current_level) continue;
+    if (level[c] < current_level) {
+      if (cellpack) cellpack[c] = make_uint2(0xffffffffu, 0u);
+      continue;
+    }
     if (cell_sweep) cell_sweep[c] = sweep;
     const double neutral = kCarryNeutral ? yneu[c] : (1.0 - xhii[c]);
     const double nhn = density[c] / Units::kProtonMass * neutral;
-    att[c] = exp(-nhn * Units::kSigma * size[c]);
+    const double at = exp(-nhn * Units::kSigma * size[c]);
+    att[c] = at;
+    if (cellpack) cellpack[c] = make_uint2(__float_as_uint((float)at), __float_as_uint(src32[c]));
   }
 }
 

@@ -313,8 +313,12 @@ sw_status build_schedule(sw_handle* h) {
     return SW_OK;
   }
   uint32_t* d_lvl;
-  if (!h->alloc(&d_lvl, lvl.size())) return h->fail(SW_ERR_OOM, "device allocation of the schedule failed");
+  // padded to a multiple of four entries: the staged wavefront kernel copies them whole
+  const size_t lvl_words = (lvl.size() + 3) & ~(size_t)3;
+  if (!h->alloc(&d_lvl, lvl_words)) return h->fail(SW_ERR_OOM, "device allocation of the schedule failed");
+  SW_CUDA(h, cudaMemset(d_lvl, 0, lvl_words * sizeof(uint32_t)), "schedule");
   SW_CUDA(h, cudaMemcpy(d_lvl, lvl.data(), lvl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload schedule");
+  p.lvl_words = (uint32_t)lvl_words;
   // rewrite each level's segment in task-id order (counting sort by level)
   SW_CUDA(h, cudaMalloc(&cursor_scratch.ptr, lvl.size() * sizeof(uint32_t)), "schedule scratch");
   uint32_t* cursor = static_cast<uint32_t*>(cursor_scratch.ptr);
@@ -412,7 +416,8 @@ sw_status build_records(sw_handle* h) {
           "read slot total");
   SW_CUDA(h, cudaStreamSynchronize(h->stream), "task records");
   uint2* slots = nullptr;
-  if (!h->alloc(&slots, std::max<unsigned long long>(total, 1)))
+  // two slots of padding: the staged wavefront kernel copies 16-byte aligned ranges
+  if (!h->alloc(&slots, total + 2))
     return h->fail(SW_ERR_OOM, "device allocation of the upwind slots (%llu MB) failed", (total * 8) >> 20);
   p.pull_slots = slots;
   SW_CUDA(h, h->ops->records(p, 1, chunk_off, h->stream), "upwind slot kernel");
@@ -848,15 +853,18 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     uint4* rec = nullptr;
     uint32_t *act_counts = nullptr, *chunk = nullptr, *pos_of_task = nullptr, *act_bits = nullptr;
     uint32_t* cell_sweep = nullptr;
+    uint2* cellpack = nullptr;
+    float* per_pos = nullptr;
     const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
     if (ok) ok = h->alloc(&chunk, chunks);
     if (ok && pull)
       ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
-           h->alloc(&act_bits, (nd + 31) / 32) && h->alloc(&cell_sweep, (size_t)h->Np);
+           h->alloc(&act_bits, (nd + 31) / 32) && h->alloc(&cell_sweep, (size_t)h->Np) &&
+           h->alloc(&cellpack, (size_t)h->Np) && h->alloc(&per_pos, (size_t)h->N * h->D + 4);
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
-              (pull ? 2 * rb + 33 : 4 * rb + 9) * nd >> 20);
+              (pull ? 2 * rb + 37 : 4 * rb + 9) * nd >> 20);
       return bail(SW_ERR_OOM);
     }
     cudaMemset(inc, 0, nd * rb);
@@ -865,6 +873,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (pull) {
       cudaMemset(qe, 0, nd * sizeof(unsigned long long));
       cudaMemset(cell_sweep, 0, (size_t)h->Np * sizeof(uint32_t));
+      cudaMemset(per_pos, 0, ((size_t)h->N * h->D + 4) * sizeof(float));
     } else {
       cudaMemset(outg, 0, nd * rb);
       cudaMemset(pend, 0, nd * rb);
@@ -877,6 +886,8 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     p.pos_of_task = pos_of_task;
     p.act_bits = act_bits;
     p.cell_sweep = cell_sweep;
+    p.cellpack = cellpack;
+    p.per_pos = per_pos;
     p.chunk = chunk;
     p.incoming = inc;
     p.outgoing = outg;
@@ -924,8 +935,9 @@ static bool pull_sparse(sw_handle* h, int level) {
   if (level <= 0) return false;
   const int v = p.pull_variant > 0 ? p.pull_variant : swh::kDefaultPullVariant;
   if (p.compact_mode == 1) return true;
-  if (p.compact_mode == 2 && v >= 80) return false;
-  return h->n_ge_host[level] * 2 < h->N || v < 80;
+  // the independent-cursor variants (below 70) cannot test levels themselves
+  if (p.compact_mode == 2 && v >= 70) return false;
+  return h->n_ge_host[level] * 2 < h->N || v < 70;
 }
 
 static sw_status ensure_act_list(sw_handle* h, int level) {
@@ -1466,6 +1478,10 @@ sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes) {
   h->ts.first_done = hd.ts_first_done != 0;
   h->p.epoch = hd.epoch;
   h->last_epoch = hd.last_epoch;
+  // pull path: the periodic sources by schedule position follow from the restored words
+  // (between steps the periodic array is the fold of the current words, so this
+  // rewrites it unchanged)
+  if (h->ops->pull) SW_CUDA(h, h->ops->fold_periodic(h->p, h->stream), "periodic fold kernel");
   // cells per level for the next step
   h->act_valid = 0;
   SW_CUDA(h, swh::launch_level_hist(h->p, h->stream), "level histogram");

@@ -62,7 +62,7 @@ cudaError_t occupancy(int* blocks_per_sm) {
 cudaError_t attenuation(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::k_attenuation<kCarry><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
       (uint32_t)p.num_cells, p.level, level, p.density, p.xhii, p.yneu, p.size, p.att, p.cell_sweep,
-      p.epoch_base, p.epoch);
+      p.epoch_base, p.epoch, static_cast<uint2*>(p.cellpack), p.cellpack ? static_cast<const float*>(p.src_dir) : nullptr);
   return cudaGetLastError();
 }
 
@@ -225,6 +225,11 @@ swk::PullArgs pull_args(const DevicePtrs& p, int level) {
   a.act = nullptr;
   a.act_count = nullptr;
   a.count = (uint32_t)(p.num_cells * p.D);
+  a.lvl = p.lvl;
+  a.num_sched = p.num_sched_levels;
+  a.cellpack = static_cast<const uint2*>(p.cellpack);
+  a.per_pos = p.per_pos;
+  a.pos_of_task = p.pos_of_task;
   return a;
 }
 
@@ -252,8 +257,9 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 }
 
 // Variants of the pull kernel: independent cursors (10 * cursors per group + target
-// blocks per SM), warp-lockstep blocks of four positions (90 + blocks per SM) and their
-// nested-loop form (80 + blocks per SM).  SUBSWEEP_PULL_VARIANT picks one.
+// blocks per SM), warp-lockstep blocks of four positions (90 + blocks per SM), their
+// nested-loop form (80 + blocks per SM) and the level-synchronous wavefront (70 +
+// blocks per SM).  SUBSWEEP_PULL_VARIANT picks one.
 
 const void* pull_kernel(int variant) {
   switch (variant) {
@@ -270,6 +276,8 @@ const void* pull_kernel(int variant) {
     case 84: return (const void*)swk::k_sweep_pull_lock2<4>;
     case 85: return (const void*)swk::k_sweep_pull_lock2<5>;
     case 86: return (const void*)swk::k_sweep_pull_lock2<6>;
+    case 72: return (const void*)swk::k_sweep_pull_wave<2>;
+    case 78: return (const void*)swk::k_sweep_pull_staged;
     default: return nullptr;
   }
 }
@@ -314,6 +322,30 @@ cudaError_t occupancy_pull(int* blocks_per_sm) {
 // schedule built at the level's first sweep of a step (three launches; the kernel reads
 // the count from the device).  Dense sweeps visit every position; the kernel stamps the
 // inactive tasks itself.
+// Shared memory of the staged wavefront kernel: the largest slot stages that fit the
+// device's per-block limit next to the record, periodic and level-offset buffers;
+// cudaErrorInvalidConfiguration when a stage would hold fewer than 9 slots per thread
+// (the level offsets of a very deep schedule take the room).
+cudaError_t staged_layout(const DevicePtrs& p, uint32_t* cap, size_t* smem) {
+  int optin = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0);
+  if (e != cudaSuccess) return e;
+  const size_t fixed = swk::stg_smem_bytes(0, p.lvl_words) + sizeof(swk::StgShared) + 1024;
+  if ((size_t)optin <= fixed) return cudaErrorInvalidConfiguration;
+  const uint32_t c = (uint32_t)(((size_t)optin - fixed) / 16) & ~1u;
+  if (c < 9u * swk::kStgThreads) return cudaErrorInvalidConfiguration;
+  *cap = c;
+  *smem = swk::stg_smem_bytes(c, p.lvl_words);
+  static size_t attr = 0;
+  if (attr != *smem) {
+    e = cudaFuncSetAttribute((const void*)swk::k_sweep_pull_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)*smem);
+    if (e != cudaSuccess) return e;
+    attr = *smem;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, level);
   const int variant = pull_variant(&p);
@@ -337,12 +369,25 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
     a.act = act;
     a.act_count = cnt;
   }
-  // sparse sweeps run the lockstep kernel, which tests the upwind cells' levels
-  const void* fn = pull_kernel(p.sparse_sweep ? kDefaultPullVariant : variant);
+  // sparse sweeps run the lockstep kernel, which tests the upwind cells' levels; the
+  // wavefront kernel needs the levelled schedule
+  const bool wave = variant >= 70 && variant < 80;
+  const void* fn = pull_kernel((p.sparse_sweep || (wave && p.num_sched_levels == 0)) ? kDefaultPullVariant : variant);
+  void* args[] = {&a};
+  uint32_t cap = 0;
+  size_t smem = 0;
+  if (fn == (const void*)swk::k_sweep_pull_staged && staged_layout(p, &cap, &smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    fn = pull_kernel(kDefaultPullVariant);  // no room for the stages: the lockstep kernel
+  }
+  if (fn == (const void*)swk::k_sweep_pull_staged) {  // one block of 1024 threads per SM
+    uint32_t words = p.lvl_words;
+    void* sargs[] = {&a, &cap, &words};
+    return cudaLaunchCooperativeKernel(fn, dim3(p.num_sms), dim3(swk::kStgThreads), sargs, smem, s);
+  }
   int grid = 0;
   cudaError_t e = coop_grid(p, fn, &grid);
   if (e != cudaSuccess) return e;
-  void* args[] = {&a};
   return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(swk::kPullThreads), args, 0, s);
 }
 

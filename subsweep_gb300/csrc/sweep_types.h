@@ -26,7 +26,7 @@ enum : uint32_t { kErrStall = 1u, kErrQueue = 2u, kErrClamp = 8u, kErrRecords = 
 
 // Control block of one handle (device memory).
 struct SweepCtl {
-  unsigned long long head;  // next ready-queue slot to claim (consumers)
+  unsigned long long head;  // next ready-queue slot to claim (consumers); pull wavefront: barrier arrivals
   unsigned long long tail;  // next ready-queue slot to fill (producers)
   uint32_t error;           // kErr* bits
   uint32_t pad;

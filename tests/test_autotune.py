@@ -38,3 +38,27 @@ def test_autotuned_equals_fixed(use_graphs, monkeypatch):
         assert 0 < st["graph_launches"] < steps  # replay starts once tuning is done
     tuned.close()
     fixed.close()
+
+
+@pytest.mark.parametrize("variant", [95, 84, 72, 78])
+def test_variant_equals_default(variant, monkeypatch):
+    """Each transport variant (lockstep at 5 blocks per SM, the nested-loop lockstep, the
+    level-synchronous wavefront, its fully TMA-staged form) against the default lockstep
+    kernel, bit for bit over steps with dense and sparse sweeps above level 0."""
+    monkeypatch.delenv("SUBSWEEP_AUTOTUNE", raising=False)
+    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2)
+    mk = lambda: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
+                       precision="mixed", autotune=False)
+    monkeypatch.setenv("SUBSWEEP_PULL_VARIANT", "94")
+    ref = mk()
+    monkeypatch.setenv("SUBSWEEP_PULL_VARIANT", str(variant))
+    var = mk()
+    for _ in range(6):
+        assert var.run_sweeps() == ref.run_sweeps()
+        np.testing.assert_array_equal(var.cell_state()["level"], ref.cell_state()["level"])
+    fv, fr = var.fields(), ref.fields()
+    for k in fr:
+        np.testing.assert_array_equal(fv[k], fr[k], err_msg=k)
+    assert var.stats()["pull_variant"] == variant
+    ref.close()
+    var.close()
