@@ -59,10 +59,23 @@ cudaError_t occupancy(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep<R>, swk::kSweepThreads, 0);
 }
 
+// Whether the handle runs the staged wavefront kernel (pull variant 78), whose per-cell
+// {attenuation, source} pack and per-position periodic sources the attenuation and the
+// fold then maintain.  The variant of a handle is fixed at creation (the autotuner's
+// candidates do not include it).
+bool staged_inputs(const DevicePtrs& p) {
+  if (!p.cellpack || !p.per_pos) return false;
+  int v = p.pull_variant;
+  if (v <= 0)
+    if (const char* env = std::getenv("SUBSWEEP_PULL_VARIANT")) v = std::atoi(env);
+  return v == 78;
+}
+
 cudaError_t attenuation(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::k_attenuation<kCarry><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
       (uint32_t)p.num_cells, p.level, level, p.density, p.xhii, p.yneu, p.size, p.att, p.cell_sweep,
-      p.epoch_base, p.epoch, static_cast<uint2*>(p.cellpack), p.cellpack ? static_cast<const float*>(p.src_dir) : nullptr);
+      p.epoch_base, p.epoch, staged_inputs(p) ? static_cast<uint2*>(p.cellpack) : nullptr,
+      static_cast<const float*>(p.src_dir));
   return cudaGetLastError();
 }
 
@@ -394,6 +407,7 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
 cudaError_t fold_pull(const DevicePtrs& p, cudaStream_t s) {
   if (p.n_periodic_cells == 0) return cudaSuccess;
   swk::PullArgs a = pull_args(p, 0);
+  if (!staged_inputs(p)) a.per_pos = nullptr;
   const dim3 grid((p.n_periodic_cells + 255) / 256, p.D);
   swk::k_fold_pull<<<grid, 256, 0, s>>>(a, static_cast<float*>(p.periodic), p.periodic_cells, p.n_periodic_cells,
                                         p.fold_cnt, static_cast<const uint2*>(p.fold_slots));
