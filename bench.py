@@ -152,6 +152,23 @@ MEASURED_DRAM_BYTES_PER_TASK = {"mixed": 102.4}
 TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 launch on C2 64^3, per task"
 
 
+# FP64 work of one try_timestep_update attempt of the chemistry kernel (mixed path),
+# counted by ncu on C2 64^3 (one attempt per cell): 535 DFMA, 128 DADD, 169 DMUL
+# thread instructions, i.e. 2 * 535 + 128 + 169 FP64 flops.
+CHEM_FP64_FLOPS_PER_ATTEMPT = 2 * 535 + 128 + 169
+
+
+def chemistry_figures(d: dict, res: dict) -> dict:
+    """Chemistry cells/s, attempts (substeps tried) per cell update and FP64 flop rate
+    over the chemistry launches' CUDA-event time."""
+    cells, attempts, ms = float(d["chem_cells"]), float(d["chem_attempts"]), float(d["chem_ms"])
+    return {"cells_per_s": res["chem_cells_per_s"],
+            "attempts_per_cell": attempts / cells if cells else None,
+            "fp64_flops_per_attempt": CHEM_FP64_FLOPS_PER_ATTEMPT,
+            "fp64_tflops": attempts * CHEM_FP64_FLOPS_PER_ATTEMPT / (ms * 1e-3) / 1e12 if ms else None,
+            "kernel_ms": ms}
+
+
 def bytes_per_task(f_dn: float, rate_bytes: int, counter_bytes: int = 1) -> float:
     """Algorithmic bytes of one cell-direction update: read incoming, periodic and the
     old outgoing rate, write the new one, and read-modify-write the incoming rate and
@@ -364,6 +381,7 @@ def run_ours(args, dist: Dist):
                           (n * ((w.params.num_directions() + 7) // 8 * 8) * 4 / 1e9),
                        grid_build_s=round(grid_s, 1)),
         "chem_cells_per_s": mixed["chem_cells_per_s"],
+        "chemistry": chemistry_figures(d, mixed),
         "fp64": ({k: results["fp64"][k] for k in ("cell_dir_updates_per_s", "chem_cells_per_s", "ms_per_step")}
                  if "fp64" in results else None),
         "speedup_mixed_vs_fp64": (results["fp64"]["ms_per_step"] / mixed["ms_per_step"]

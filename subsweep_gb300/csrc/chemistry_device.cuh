@@ -14,6 +14,10 @@
 // additionally carries y = 1 - x as its own FP64 state, updated by -dx, so the
 // neutral density keeps full relative precision near complete ionisation; the
 // smaller of x and y is the accurate one and the other is re-derived from it.
+//
+// Work per try_timestep_update attempt (counted by ncu on C2 64^3, one attempt per
+// cell, mixed path): 535 DFMA, 128 DADD and 169 DMUL thread instructions, 1367 FP64
+// flops; the kernel keeps the FP64 pipe 82 % busy.
 #pragma once
 
 #include <cfloat>
