@@ -59,12 +59,11 @@ cudaError_t occupancy(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, swk::k_sweep<R>, swk::kSweepThreads, 0);
 }
 
-// Whether the handle runs the staged wavefront kernel (pull variant 78), whose per-cell
-// {attenuation, source} pack and per-position periodic sources the attenuation and the
-// fold then maintain.  The variant of a handle is fixed at creation (the autotuner's
-// candidates do not include it).
+// Whether the handle runs the staged wavefront kernel (pull variant 78), whose
+// per-position periodic sources the fold then maintains.  The variant of a handle is
+// fixed at creation (the autotuner's candidates do not include it).
 bool staged_inputs(const DevicePtrs& p) {
-  if (!p.cellpack || !p.per_pos) return false;
+  if (!p.per_pos) return false;
   int v = p.pull_variant;
   if (v <= 0)
     if (const char* env = std::getenv("SUBSWEEP_PULL_VARIANT")) v = std::atoi(env);
@@ -74,8 +73,7 @@ bool staged_inputs(const DevicePtrs& p) {
 cudaError_t attenuation(const DevicePtrs& p, int level, cudaStream_t s) {
   swk::k_attenuation<kCarry><<<grid_for(p.num_cells, 256), 256, 0, s>>>(
       (uint32_t)p.num_cells, p.level, level, p.density, p.xhii, p.yneu, p.size, p.att, p.cell_sweep,
-      p.epoch_base, p.epoch, staged_inputs(p) ? static_cast<uint2*>(p.cellpack) : nullptr,
-      static_cast<const float*>(p.src_dir));
+      p.epoch_base, p.epoch, static_cast<uint2*>(p.cellpack), static_cast<const float*>(p.src_dir));
   return cudaGetLastError();
 }
 

@@ -132,17 +132,22 @@ __device__ __forceinline__ void split_task(uint32_t t, uint32_t Np, float inv_np
 }
 
 // record word w: upwind count (7 bits) | direction << 7 (7 bits) | slot offset >> 32 << 14
+// (17 bits) | 1 << 31 when an upwind face of the task is LOCAL_PERIODIC (its periodic
+// source can be non-zero; every other task's stays 0)
+constexpr uint32_t kRecPeriodic = 1u << 31;
 __device__ __forceinline__ unsigned long long rec_offset(const uint4& r) {
-  return (unsigned long long)r.z | ((unsigned long long)(r.w >> 14) << 32);
+  return (unsigned long long)r.z | ((unsigned long long)((r.w >> 14) & 0x1ffffu) << 32);
 }
 __device__ __forceinline__ uint32_t rec_count(const uint4& r) { return r.w & 0x7fu; }
 __device__ __forceinline__ uint32_t rec_dir(const uint4& r) { return (r.w >> 7) & 0x7fu; }
+__device__ __forceinline__ bool rec_periodic(const uint4& r) { return (r.w & kRecPeriodic) != 0u; }
 
 // ---------------------------------------------------------------------------------------
 // Task records and upwind slots, built once per grid from the schedule (geometry only).
 // Position p of the schedule (task t = order[p] = d * Np + c) gets
 //   rec[p]   = {c, bits of 1 / A_down (FP32; 0 when no face is downwind),
-//               slot offset (low 32 bits), upwind count | d << 7 | offset >> 32 << 14}
+//               slot offset (low 32 bits), upwind count | d << 7 | offset >> 32 << 14
+//               | kRecPeriodic}
 //   slots[offset + k] = {upwind task d * Np + n, |area n . d| in FP32}, k < count,
 // for the upwind LOCAL faces of c in face order (exact sign of n . d).  A_down is
 // summed in face order.  Counts, a chunked 64-bit exclusive scan, then the writes.
@@ -163,15 +168,16 @@ __global__ void k_pull_rec_count(PullArgs a, const uint32_t* order, uint32_t tot
     const float fx = a.dir32[3 * d], fy = a.dir32[3 * d + 1], fz = a.dir32[3 * d + 2];
     const double dx = a.dir64[3 * d], dy = a.dir64[3 * d + 1], dz = a.dir64[3 * d + 2];
     float area_down = 0.f;
-    uint32_t n_up = 0;
+    uint32_t n_up = 0, periodic_up = 0;
     for (uint32_t j = 0; j < nf; ++j) {
       const uint4 g = a.geo16[beg + j];
       const float sj = face_eff(g, fx, fy, fz, a.geo64 + beg + j, dx, dy, dz);
       if (sj > 0.f) area_down += sj;
       else if (sj < 0.f && (g.w >> kKindShift) == kKindLocal) ++n_up;
+      else if (sj < 0.f && (g.w >> kKindShift) == kKindPeriodic) periodic_up = kRecPeriodic;
     }
     const float inv = area_down > 0.f ? 1.0f / area_down : 0.f;
-    rec[p] = make_uint4(c, __float_as_uint(inv), 0u, n_up | (d << 7));
+    rec[p] = make_uint4(c, __float_as_uint(inv), 0u, n_up | (d << 7) | periodic_up);
   }
 }
 
@@ -252,7 +258,7 @@ __global__ void __launch_bounds__(kCompactThreads) k_pull_slots(PullArgs a, uint
     const uint32_t n_up = rec_count(r);
     const uint32_t c = r.x, d = rec_dir(r);
     r.z = (uint32_t)o;
-    r.w = n_up | (d << 7) | ((uint32_t)(o >> 32) << 14);
+    r.w = n_up | (d << 7) | ((uint32_t)(o >> 32) << 14) | (r.w & kRecPeriodic);
     rec[p] = r;
     const uint32_t beg = a.off[c], nf = a.off[c + 1] - beg;
     const uint32_t dnp = d * a.Np;
@@ -570,15 +576,17 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   const bool sparse = a.act != nullptr && a.current_level > 0;
   float src = 0.f, per = 0.f, att = 0.f;
   bool active = true;
+  // One 8-byte load per cell gives {(float) attenuation or the inactive mark, source}
+  // (written by the attenuation kernel); the periodic source only for tasks with an
+  // upwind periodic face.
   auto load_cell = [&]() {
     active = true;
-    if (have) {
-      if (check_level) active = a.level[cur.x] >= a.current_level;
-      if (gl == 0) {
-        src = a.src_dir[cur.x];
-        per = __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x);
-        att = (float)a.att[cur.x];
-      }
+    if (have && (check_level || gl == 0)) {
+      const uint2 cp = __ldg(a.cellpack + cur.x);
+      active = cp.x != kInactiveCell;
+      att = __uint_as_float(cp.x);
+      src = __uint_as_float(cp.y);
+      per = (gl == 0 && rec_periodic(cur)) ? __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x) : 0.f;
     }
   };
   load_cell();
@@ -715,17 +723,18 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
     bool have = idx(b) < count;
     const uint32_t t = rec_dir(cur) * a.Np + cur.x;
     float src = 0.f, per = 0.f, att = 0.f;
-    if (have) {
-      if (check_level && a.level[cur.x] < a.current_level) {  // inactive: keep q, stamp the word
+    if (have && (check_level || gl == 0)) {
+      const uint2 cp = __ldg(a.cellpack + cur.x);  // {(float) attenuation or inactive mark, source}
+      if (cp.x == kInactiveCell) {  // inactive: keep q, stamp the word
         if (gl == 0) {
           const unsigned long long own = ld_relaxed_u64(a.qe + t);
           st_relaxed_u64(a.qe + t, (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
         }
         have = false;
       } else if (gl == 0) {
-        src = a.src_dir[cur.x];
-        per = __ldcg(a.periodic + t);
-        att = (float)a.att[cur.x];
+        src = __uint_as_float(cp.y);
+        per = rec_periodic(cur) ? __ldcg(a.periodic + t) : 0.f;
+        att = __uint_as_float(cp.x);
       }
     }
     const uint32_t n_up = have ? rec_count(cur) : 0u;
@@ -854,17 +863,16 @@ struct WaveTask {
 __device__ __forceinline__ void wave_fetch(const PullArgs& a, uint32_t i, bool check_level, WaveTask& w) {
   w.r = __ldg(a.rec + i);
   const uint32_t c = w.r.x;
-  w.live = !check_level || __ldg(a.level + c) >= (uint32_t)a.current_level;
+  const uint2 cp = __ldg(a.cellpack + c);  // {(float) attenuation or inactive mark, source}
+  w.live = cp.x != kInactiveCell;
   const uint32_t n = w.live ? rec_count(w.r) : 0u;
   const uint2* base = a.slots + rec_offset(w.r);
 #pragma unroll
   for (int j = 0; j < kWaveSlots; ++j)
     if ((uint32_t)j < n) w.s[j] = __ldg(base + j);
-  if (w.live) {
-    w.src = __ldg(a.src_dir + c);
-    w.per = __ldcg(a.periodic + rec_dir(w.r) * a.Np + c);
-    w.att = (float)__ldg(a.att + c);
-  }
+  w.src = __uint_as_float(cp.y);
+  w.att = __uint_as_float(cp.x);
+  w.per = (w.live && rec_periodic(w.r)) ? __ldcg(a.periodic + rec_dir(w.r) * a.Np + c) : 0.f;
 }
 
 __device__ __forceinline__ void wave_solve(const PullArgs& a, const WaveTask& w, uint32_t sweep,
