@@ -745,10 +745,16 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
     const bool big = n_up > (uint32_t)(kPullRounds * kPullGroup);
     unsigned long long w0 = 0;
     uint32_t wait_ns = 32;
+    // a word that carries the current sweep number is final for the sweep: a retry
+    // reloads only the words that did not
+    unsigned long long x0 = 0, x1 = 0;
+    bool need0 = p0, need1 = p1;
     while (true) {
-      const unsigned long long x0 = ld_relaxed_u64_if(p0, q0);
-      const unsigned long long x1 = ld_relaxed_u64_if(p1, q1);
-      bool bad = (p0 && !word_current(x0, sweep)) || (p1 && !word_current(x1, sweep));
+      if (need0) x0 = ld_relaxed_u64(q0);
+      if (need1) x1 = ld_relaxed_u64(q1);
+      need0 = p0 && !word_current(x0, sweep);
+      need1 = p1 && !word_current(x1, sweep);
+      bool bad = need0 || need1;
       float in = p0 ? fmaf(wt0, __uint_as_float((uint32_t)x0), 0.f) : 0.f;
       if (p1) in = fmaf(wt1, __uint_as_float((uint32_t)x1), in);
       if (big) {
