@@ -78,6 +78,7 @@ struct DevicePtrs {
   uint32_t* pos_of_task;     // pull path: schedule position of every task (inverse order)
   uint8_t* fold_cnt;         // pull path: upwind periodic faces per (periodic cell, direction)
   void* fold_slots;          // pull path: their uint2 {upwind task, weight}, 4 per entry
+  uint8_t* fold_changed;     // pull path: per periodic cell, a periodic neighbour was active
   uint32_t* act_bits;        // pull path: one bit per schedule position (sparse compaction)
   int sparse_sweep;          // pull path: this launch runs over the compacted list of its level
   int compact_now;           // pull path: ... and builds that list first

@@ -758,15 +758,16 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     p.periodic_cells = d_pc;
     p.n_periodic_cells = (uint32_t)pcells.size();
     if (h->ops->pull && !pcells.empty()) {  // the fold's precomputed upwind periodic faces
-      uint8_t* fcnt = nullptr;
+      uint8_t *fcnt = nullptr, *fchanged = nullptr;
       uint2* fslots = nullptr;
       const size_t entries = pcells.size() * (size_t)D;
-      if (!h->alloc(&fcnt, entries) || !h->alloc(&fslots, entries * 4)) {
+      if (!h->alloc(&fcnt, entries) || !h->alloc(&fslots, entries * 4) || !h->alloc(&fchanged, pcells.size())) {
         h->fail(SW_ERR_OOM, "device allocation of the periodic fold slots failed");
         return bail(SW_ERR_OOM);
       }
       p.fold_cnt = fcnt;
       p.fold_slots = fslots;
+      p.fold_changed = fchanged;
     }
   }
   // directions
@@ -1006,6 +1007,8 @@ static sw_status step_graph(sw_handle* h, double* time_elapsed_out) {
       // attenuation, transport, chemistry, the periodic fold, and the counts (push) or
       // the compaction at a sparse level's first sweep (pull)
       kernels += 3 + (p.n_periodic_cells > 0 ? 1 : 0);
+      // the fold's mark pass after a sweep that leaves cells inactive (pull path)
+      if (ops.pull && p.n_periodic_cells > 0 && h->n_ge_host[levels[k]] < h->N) kernels += 1;
       if (!ops.pull) {
         kernels += 1;
       } else if (variants[k] && !((compacted >> levels[k]) & 1u)) {
@@ -1213,6 +1216,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     SW_CUDA(h, cudaEventRecord(h->ev[7], h->stream), "event");
     SW_CUDA(h, ops.fold_periodic(h->p, h->stream), "periodic fold kernel");
     launches += 3 + (h->p.n_periodic_cells > 0 ? 1 : 0);
+    if (ops.pull && h->p.n_periodic_cells > 0 && h->p.active_cells < h->N) launches += 1;  // fold marks
     SW_CUDA(h, cudaEventRecord(h->ev[1], h->stream), "event");
     SW_CUDA(h, ops.chemistry(h->p, level, h->stream), "chemistry kernel");
     SW_CUDA(h, cudaEventRecord(h->ev[2], h->stream), "event");
@@ -1481,7 +1485,11 @@ sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes) {
   // pull path: the periodic sources by schedule position follow from the restored words
   // (between steps the periodic array is the fold of the current words, so this
   // rewrites it unchanged)
-  if (h->ops->pull) SW_CUDA(h, h->ops->fold_periodic(h->p, h->stream), "periodic fold kernel");
+  if (h->ops->pull) {
+    swh::DevicePtrs q = h->p;
+    q.active_cells = h->N;  // every entry
+    SW_CUDA(h, h->ops->fold_periodic(q, h->stream), "periodic fold kernel");
+  }
   // cells per level for the next step
   h->act_valid = 0;
   SW_CUDA(h, swh::launch_level_hist(h->p, h->stream), "level histogram");

@@ -407,8 +407,15 @@ cudaError_t fold_pull(const DevicePtrs& p, cudaStream_t s) {
   swk::PullArgs a = pull_args(p, 0);
   if (!staged_inputs(p)) a.per_pos = nullptr;
   const dim3 grid((p.n_periodic_cells + 255) / 256, p.D);
+  // after a sweep that left cells inactive, only entries next to an active cell
+  uint8_t* changed = nullptr;
+  if (p.active_cells < p.num_cells && p.fold_changed) {
+    changed = p.fold_changed;
+    swk::k_fold_mark<<<grid_for(p.n_periodic_cells, 256), 256, 0, s>>>(a, p.periodic_cells, p.n_periodic_cells,
+                                                                        changed);
+  }
   swk::k_fold_pull<<<grid, 256, 0, s>>>(a, static_cast<float*>(p.periodic), p.periodic_cells, p.n_periodic_cells,
-                                        p.fold_cnt, static_cast<const uint2*>(p.fold_slots));
+                                        p.fold_cnt, static_cast<const uint2*>(p.fold_slots), changed);
   return cudaGetLastError();
 }
 

@@ -1282,11 +1282,27 @@ __global__ void k_fold_build(PullArgs a, const uint32_t* cells, uint32_t n_cells
 }
 
 // grid: (periodic cells / blockDim.x, D)
+// After a sweep that left cells inactive: marks the periodic cells with a periodic
+// neighbour that was active (attenuation's inactive mark in `cellpack`).  Only their
+// entries can change; every other entry is the same sum of the same words.
+__global__ void k_fold_mark(PullArgs a, const uint32_t* cells, uint32_t n_cells, uint8_t* changed) {
+  for (uint32_t pc = blockIdx.x * blockDim.x + threadIdx.x; pc < n_cells; pc += gridDim.x * blockDim.x) {
+    const uint32_t c = cells[pc];
+    uint8_t ch = 0;
+    for (uint32_t f = a.off[c]; f < a.off[c + 1] && !ch; ++f) {
+      const uint32_t w = a.geo16[f].w;
+      if ((w >> kKindShift) == kKindPeriodic && a.cellpack[w & kNbrMask].x != kInactiveCell) ch = 1;
+    }
+    changed[pc] = ch;
+  }
+}
+
+// changed: null after a sweep of every cell, else the marks of k_fold_mark
 __global__ void k_fold_pull(PullArgs a, float* periodic, const uint32_t* cells, uint32_t n_cells,
-                            const uint8_t* cnt, const uint2* slots) {
+                            const uint8_t* cnt, const uint2* slots, const uint8_t* changed) {
   const uint32_t d = blockIdx.y;
   const uint32_t pc = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pc < n_cells) {
+  if (pc < n_cells && (!changed || changed[pc])) {
     const size_t e = (size_t)d * n_cells + pc;
     const uint32_t c = cells[pc];
     const uint32_t n = cnt[e];
