@@ -153,9 +153,9 @@ TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 
 
 
 # FP64 work of one try_timestep_update attempt of the chemistry kernel (mixed path),
-# counted by ncu on C2 64^3 (one attempt per cell): 535 DFMA, 128 DADD, 169 DMUL
-# thread instructions, i.e. 2 * 535 + 128 + 169 FP64 flops.
-CHEM_FP64_FLOPS_PER_ATTEMPT = 2 * 535 + 128 + 169
+# counted by ncu on a level-0 launch of C2 64^3 (about one attempt per cell): 366 DFMA,
+# 63 DADD, 156 DMUL thread instructions, i.e. 2 * 366 + 63 + 156 FP64 flops.
+CHEM_FP64_FLOPS_PER_ATTEMPT = 2 * 366 + 63 + 156
 
 
 def chemistry_figures(d: dict, res: dict) -> dict:

@@ -15,9 +15,10 @@
 // neutral density keeps full relative precision near complete ionisation; the
 // smaller of x and y is the accurate one and the other is re-derived from it.
 //
-// Work per try_timestep_update attempt (counted by ncu on C2 64^3, one attempt per
-// cell, mixed path): 535 DFMA, 128 DADD and 169 DMUL thread instructions, 1367 FP64
-// flops; the kernel keeps the FP64 pipe 82 % busy.
+// Work per try_timestep_update attempt (counted by ncu on a level-0 launch of C2 64^3,
+// about one attempt per cell, mixed path): 366 DFMA, 63 DADD and 156 DMUL thread
+// instructions, 951 FP64 flops (the reference's expressions, as on the FP64 path:
+// 535 / 128 / 169, 1367 flops); the kernel keeps the FP64 pipe 78 % busy.
 #pragma once
 
 #include <cfloat>
@@ -89,6 +90,69 @@ struct ChemSolver {
     fitd = (e * (c1 * c2 * t + 0.5 * s5 * (2.0 * c2 + t))) / ((t * sqrt_t) * s5 * ((s5 + 1.0) * (s5 + 1.0)));
   }
 
+  // Mixed path (kCarryNeutral): the same fits with one reciprocal of T, rsqrt for both
+  // square roots and exp / log1p for the powers ((1 + q)^-c = exp(-c log1p(q)) gives the
+  // reciprocal power directly), FP64 throughout.  Each value agrees with the reference's
+  // expression to a few ulps; the FP64 drop-in keeps the reference's expressions.
+  struct TFits {
+    double inv_t, rsq, sq, s5, inv_s5, inv_1s5;
+  };
+  __device__ static TFits t_fits(double t) {
+    TFits f;
+    f.inv_t = 1.0 / t;
+    f.rsq = rsqrt(t);
+    f.sq = t * f.rsq;                         // sqrt(t)
+    f.s5 = f.sq * 0.003162277660168379;       // sqrt(t / 1e5)
+    f.inv_s5 = f.rsq * 316.22776601683796;    // 1 / sqrt(t / 1e5)
+    f.inv_1s5 = 1.0 / (1.0 + f.s5);
+    return f;
+  }
+  __device__ static void collision_fits_fast(double t, const TFits& g, double& fit, double& fitd) {
+    const double c1 = 1.0 / 1e5, c2 = 157809.1;
+    const double e = exp(-c2 * g.inv_t);
+    fit = g.sq * g.inv_1s5 * e;
+    fitd = (e * (c1 * c2 * t + 0.5 * g.s5 * (2.0 * c2 + t))) * (g.inv_t * g.rsq) * g.inv_s5 *
+           (g.inv_1s5 * g.inv_1s5);
+  }
+
+  __device__ void cooling_fast(double& lambda_c, double& dlambda_c) const {
+    const double t = temperature;
+    const double ne = n_ionized();
+    const double nhn = n_neutral();
+    const double nhi = n_ionized();
+    const TFits g = t_fits(t);
+    double fit, fitd;
+    collision_fits_fast(t, g, fit, fitd);
+    const double e_exc = exp(-118348.0 * g.inv_t);
+    const double exc = (7.5e-19 * g.inv_1s5 * e_exc) * Units::kErgsCentimetersCubedPerS;
+    const double c3 = 1.0 / 1e5, c2e = 118348.0;
+    const double dexc = ((7.5e-19 * e_exc * (c2e * c3 * t - 0.5 * c3 * (t * t) + c2e * g.s5)) *
+                         (g.inv_t * g.inv_t) * g.inv_s5 * (g.inv_1s5 * g.inv_1s5)) *
+                        Units::kErgsCentimetersCubedPerS;
+    const double lambda = 315614.0 * g.inv_t;
+    const double ln_lambda = log(lambda);
+    const double l197 = exp(1.97 * ln_lambda);
+    const double q = exp(0.376 * (ln_lambda - 0.8109302162163288));  // ln 2.25
+    const double inv_a = exp(-3.72 * log1p(q));                      // (1 + q)^-3.72
+    const double recomb_rate = (3.435e-30 * t * l197 * inv_a) * Units::kErgsCentimetersCubedPerS;
+    const double c2r = 1.97, c3r = 0.376, c4r = 3.72;
+    const double drecomb_rate = (3.435e-30 * ((inv_a / (1.0 + q)) *
+                                             (1.0 - 1.0 * c2r + (1.0 - 1.0 * c2r + c3r * c4r) * q) * l197)) *
+                                Units::kErgsCentimetersCubedPerS;
+    const double xx = 2.727 / scale_factor;
+    const double x2 = xx * xx;
+    const double compton = (1.017e-37 * (x2 * x2) * (t - xx)) * Units::kErgsPerS;
+    const double dcompton = (1.017e-37 * (x2 * x2)) * Units::kErgsPerS;
+    const double coll = (exc + (1.27e-21 * fit) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
+    const double recomb = recomb_rate * ne * nhi;
+    const double brems = ((1.42e-27 * g.sq) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
+    lambda_c = coll + recomb + brems + compton * ne;
+    const double dcoll = (dexc + (1.27e-21 * fitd) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
+    const double drecomb = drecomb_rate * ne * nhi;
+    const double dbrems = ((1.42e-27 * 0.5 * g.rsq) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
+    dlambda_c = dcoll + drecomb + dbrems + dcompton * ne;
+  }
+
   // cooling_rate 275-287 and cooling_rate_derivative 289-302 at the current temperature:
   // collisional ionization / excitation cooling (237-253), case B recombination cooling
   // (196-216), bremsstrahlung and Compton cooling (265-273).
@@ -143,10 +207,14 @@ struct ChemSolver {
   // 304-310 (+ photoheating_rate 321-325)
   __device__ double temperature_change(double timestep, double absorbed) const {
     double k = (Units::kGamma - 1.0) * Units::kProtonMass / (density * Units::kBoltzmann);
-    double heating = ((timestep * rate * absorbed) / volume) *
-                     (Units::kPhotonAverageEnergy - Units::kRydberg) / timestep;
-    double lc, dlc;
-    cooling(lc, dlc);
+    double heating, lc, dlc;
+    if (kCarryNeutral) {
+      heating = ((rate * absorbed) / volume) * (Units::kPhotonAverageEnergy - Units::kRydberg);
+      cooling_fast(lc, dlc);
+    } else {
+      heating = ((timestep * rate * absorbed) / volume) * (Units::kPhotonAverageEnergy - Units::kRydberg) / timestep;
+      cooling(lc, dlc);
+    }
     double lambda = heating - lc;
     double dlambdadt = -dlc;
     double m = mu();
@@ -158,22 +226,36 @@ struct ChemSolver {
     const double t = temperature;
     double n_h = nh();
     double ne = n_ionized();
-    const double lambda = 315614.0 / t;
-    const double dlambda_dt = -315614.0 / (t * t);
-    const double sl = sqrt(lambda);
-    const double p = pow(lambda / 2.74, 0.407);
-    const double b = pow(1.0 + p, 2.242);
-    const double alpha = (2.753e-14 * (lambda * sl) / b) * Units::kCentimetersCubedPerS;
+    double alpha, dalpha, fit, fitd, photo;
     const double c2a = 0.407, c3a = 2.242;
-    const double da = -sl * (1.0 / (b * (p + 1.0))) * (c2a * c3a * p - 1.5 * p - 1.5);
-    const double dalpha = ((2.753e-14 * da) * Units::kCentimetersCubedPerS) * dlambda_dt;
-    const double sq = sqrt(t);
-    const double s5 = sqrt(t / 1e5);
-    double fit, fitd;
-    collision_fits(t, sq, s5, fit, fitd);
+    if (kCarryNeutral) {
+      const TFits g = t_fits(t);
+      const double lambda = 315614.0 * g.inv_t;
+      const double dlambda_dt = -lambda * g.inv_t;
+      const double sl = 561.7953363992976 * g.rsq;                            // sqrt(lambda)
+      const double p = exp(0.407 * (log(lambda) - 1.007957920399979));         // (lambda / 2.74)^0.407
+      const double inv_b = exp(-2.242 * log1p(p));                             // (1 + p)^-2.242
+      alpha = (2.753e-14 * (lambda * sl) * inv_b) * Units::kCentimetersCubedPerS;
+      const double da = -sl * (inv_b / (p + 1.0)) * (c2a * c3a * p - 1.5 * p - 1.5);
+      dalpha = ((2.753e-14 * da) * Units::kCentimetersCubedPerS) * dlambda_dt;
+      collision_fits_fast(t, g, fit, fitd);
+      photo = (rate * absorbed) / (n_neutral() * volume);
+    } else {
+      const double lambda = 315614.0 / t;
+      const double dlambda_dt = -315614.0 / (t * t);
+      const double sl = sqrt(lambda);
+      const double p = pow(lambda / 2.74, 0.407);
+      const double b = pow(1.0 + p, 2.242);
+      alpha = (2.753e-14 * (lambda * sl) / b) * Units::kCentimetersCubedPerS;
+      const double da = -sl * (1.0 / (b * (p + 1.0))) * (c2a * c3a * p - 1.5 * p - 1.5);
+      dalpha = ((2.753e-14 * da) * Units::kCentimetersCubedPerS) * dlambda_dt;
+      const double sq = sqrt(t);
+      const double s5 = sqrt(t / 1e5);
+      collision_fits(t, sq, s5, fit, fitd);
+      photo = (((timestep * rate) * absorbed) / (n_neutral() * volume)) / timestep;
+    }
     double beta = (5.85e-11 * fit) * Units::kCentimetersCubedPerS;
     double dbeta = (5.85e-11 * fitd) * Units::kCentimetersCubedPerS;
-    double photo = (((timestep * rate) * absorbed) / (n_neutral() * volume)) / timestep;
     double c = beta * ne + photo;
     double m = mu();
     double d = alpha * ne;
