@@ -668,7 +668,8 @@ struct ChemArgs {
   int current_level;
   int D;
   uint32_t Np;
-  const R* incoming;
+  const R* incoming;          // incoming rate of task t at incoming[t * incoming_stride]
+  uint32_t incoming_stride;
   const R* periodic;
   double rate_scale;
   const double* source;
@@ -704,14 +705,14 @@ __global__ void k_chemistry(ChemArgs<R> a) {
       rate = 0.0;  // sum over directions of Site::get_rate, in direction order
       for (int d = 0; d < a.D; ++d) {
         const size_t t = (size_t)d * a.Np + c;
-        rate += ((double)a.incoming[t] + src) + (double)a.periodic[t];
+        rate += ((double)a.incoming[t * a.incoming_stride] + src) + (double)a.periodic[t];
       }
     } else {
       // compensated FP32 sum of the scaled transported rates, the source added in FP64
       float s = 0.f, comp = 0.f;
       for (int d = 0; d < a.D; ++d) {
         const size_t t = (size_t)d * a.Np + c;
-        const float v = (float)a.incoming[t] + (float)a.periodic[t];
+        const float v = (float)a.incoming[t * a.incoming_stride] + (float)a.periodic[t];
         const float yv = v - comp;
         const float tt = s + yv;
         comp = (tt - s) - yv;

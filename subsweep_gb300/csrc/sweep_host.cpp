@@ -849,7 +849,8 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     uint32_t *cnt = nullptr, *queue = nullptr, *order = nullptr;
     unsigned long long* qe = nullptr;
     swk::SweepCtl* ctl = nullptr;
-    bool ok = h->alloc(&inc, nd * rb) && h->alloc(&per, nd * rb) && h->alloc(&cnt, nd / 4) &&
+    // the pull path keeps each task's incoming rate beside its word (16 bytes per task)
+    bool ok = (pull || h->alloc(&inc, nd * rb)) && h->alloc(&per, nd * rb) && h->alloc(&cnt, nd / 4) &&
               h->alloc(&order, nd) && h->alloc(&ctl, 1);
     uint4* rec = nullptr;
     uint32_t *act_counts = nullptr, *chunk = nullptr, *pos_of_task = nullptr, *act_bits = nullptr;
@@ -859,20 +860,21 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
     if (ok) ok = h->alloc(&chunk, chunks);
     if (ok && pull)
-      ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
+      ok = h->alloc(&qe, 2 * nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
            h->alloc(&act_bits, (nd + 31) / 32) && h->alloc(&cell_sweep, (size_t)h->Np) &&
            h->alloc(&cellpack, (size_t)h->Np) && h->alloc(&per_pos, (size_t)h->N * h->D + 4);
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
-              (pull ? 2 * rb + 37 : 4 * rb + 9) * nd >> 20);
+              (pull ? rb + 49 : 4 * rb + 9) * nd >> 20);
       return bail(SW_ERR_OOM);
     }
-    cudaMemset(inc, 0, nd * rb);
+    if (!pull) cudaMemset(inc, 0, nd * rb);
     cudaMemset(per, 0, nd * rb);
     cudaMemset(cnt, 0, nd);
     if (pull) {
-      cudaMemset(qe, 0, nd * sizeof(unsigned long long));
+      cudaMemset(qe, 0, 2 * nd * sizeof(unsigned long long));
+      inc = reinterpret_cast<char*>(qe) + 8;  // task 0's incoming rate; stride 16 bytes
       cudaMemset(cell_sweep, 0, (size_t)h->Np * sizeof(uint32_t));
       cudaMemset(per_pos, 0, ((size_t)h->N * h->D + 4) * sizeof(float));
     } else {
@@ -1401,12 +1403,13 @@ static std::vector<CheckpointSection> checkpoint_sections(sw_handle* h) {
   std::vector<CheckpointSection> v = {
       {p.xhii, n * 8},           {p.yneu, n * 8},          {p.temperature, n * 8}, {p.previous_rate, n * 8},
       {p.change_timescale, n * 8}, {p.species_timestep, n * 8}, {p.ionization_time, n * 8}, {p.level, n},
-      {p.incoming, nd * rb},     {p.periodic, nd * rb},
+      {p.periodic, nd * rb},
   };
   if (h->ops->pull) {
-    v.push_back({p.qe, nd * 8});
+    v.push_back({p.qe, nd * 16});  // words and incoming rates
     v.push_back({p.cell_sweep, n * 4});
   } else {
+    v.push_back({p.incoming, nd * rb});
     v.push_back({p.outgoing, nd * rb});
     v.push_back({p.pending, nd * rb});
   }

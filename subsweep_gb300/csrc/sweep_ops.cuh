@@ -181,6 +181,7 @@ cudaError_t chemistry(const DevicePtrs& p, int level, cudaStream_t s) {
   a.D = p.D;
   a.Np = p.Np;
   a.incoming = static_cast<const R*>(p.incoming);
+  a.incoming_stride = SWK_PULL ? 4u : 1u;  // pull path: beside each task's word, 16 bytes apart
   a.periodic = static_cast<const R*>(p.periodic);
   a.rate_scale = p.rate_scale;
   a.source = p.source;
@@ -222,7 +223,6 @@ swk::PullArgs pull_args(const DevicePtrs& p, int level) {
   a.src_dir = static_cast<const float*>(p.src_dir);
   a.att = p.att;
   a.threshold = (float)(p.threshold / p.rate_scale);
-  a.incoming = static_cast<float*>(p.incoming);
   a.periodic = static_cast<const float*>(p.periodic);
   a.qe = p.qe;
   a.ctl = p.ctl;

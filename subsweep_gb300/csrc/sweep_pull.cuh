@@ -43,9 +43,10 @@ struct PullArgs {
   const float* src_dir;     // source / D per cell, stored rate units
   const double* att;
   float threshold;
-  float* incoming;
   const float* periodic;
-  unsigned long long* qe;   // {q (float bits) low, sweep number high}
+  // per task t, 16 bytes at qe + 2 t: the word {q (float bits) low, sweep number high}
+  // and the task's incoming rate (float bits, low half of the second 8 bytes)
+  unsigned long long* qe;
   SweepCtl* ctl;
   int current_level;
   uint32_t epoch;
@@ -89,6 +90,22 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64_if(bool pred, const
 
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
   WordRef(*p).store(v, cuda::memory_order_relaxed);
+}
+
+// Task t's slot: its word, and beside it its incoming rate.  A commit writes both with
+// one 16-byte store; each 8-byte element of a vector access is single-copy atomic, so
+// readers of the word see either the old or the new word whole.
+__device__ __forceinline__ unsigned long long* word_ptr(unsigned long long* qe, size_t t) { return qe + 2 * t; }
+__device__ __forceinline__ const unsigned long long* word_ptr(const unsigned long long* qe, size_t t) {
+  return qe + 2 * t;
+}
+__device__ __forceinline__ float stored_incoming(const unsigned long long* qe, size_t t) {
+  return __uint_as_float((uint32_t)qe[2 * t + 1]);
+}
+__device__ __forceinline__ void commit_slot(unsigned long long* qe, size_t t, unsigned long long word, float in) {
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(qe + 2 * t), "l"(word),
+               "l"((unsigned long long)__float_as_uint(in))
+               : "memory");
 }
 
 // {q, sweep << 1}: solved in `sweep`; {q, sweep << 1 | 1}: stamped (inactive in `sweep`)
@@ -445,7 +462,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArg
       const uint32_t n_up = q.have[k] ? rec_count(q.cur[k]) : 0u;
 #pragma unroll
       for (int r = 0; r < kPullRounds; ++r)
-        w[k][r] = ld_relaxed_u64_if(gl + r * kPullGroup < n_up, a.qe + q.s[k][r].x);
+        w[k][r] = ld_relaxed_u64_if(gl + r * kPullGroup < n_up, word_ptr(a.qe, q.s[k][r].x));
       src[k] = per[k] = att[k] = 0.f;
       if (q.have[k] && gl == 0) {
         const uint32_t c = q.cur[k].x;
@@ -470,7 +487,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArg
       // tasks with more than kPullGroup * kPullRounds upwind faces: the rest from memory
       for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
         const uint2 sl = a.slots[rec_offset(q.cur[k]) + j];
-        const unsigned long long wn = ld_relaxed_u64(a.qe + sl.x);
+        const unsigned long long wn = ld_relaxed_u64(word_ptr(a.qe, sl.x));
         bad = bad || !word_current(wn, sweep);
         in = fmaf(__uint_as_float(sl.y), __uint_as_float((uint32_t)wn), in);
       }
@@ -484,8 +501,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArg
         const float rt = (in + src[k]) + per[k];                   // Site::get_rate, site.rs:53-56
         const float out = (rt < a.threshold) ? 0.f : rt * att[k];  // get_outgoing_rate
         const float qv = out * __uint_as_float(q.cur[k].y);
-        a.incoming[t] = in;
-        st_relaxed_u64(a.qe + t, pack_qe(qv, sweep));
+        commit_slot(a.qe, t, pack_qe(qv, sweep), in);
         ++solved;
       }
       if (commit) {  // advance the cursor and its pipeline by one position
@@ -596,8 +612,8 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
     if (have && !active) {  // inactive cell: keep its q, stamp the word with this sweep
       if (gl == 0) {
         const uint32_t t = rec_dir(cur) * a.Np + cur.x;
-        const unsigned long long own = ld_relaxed_u64(a.qe + t);
-        st_relaxed_u64(a.qe + t, (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
+        const unsigned long long own = ld_relaxed_u64(word_ptr(a.qe, t));
+        st_relaxed_u64(word_ptr(a.qe, t), (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
       }
       have = false;
     }
@@ -608,7 +624,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
       const bool pr = gl + r * G < n_up;
-      w[r] = ld_relaxed_u64_if(pr, a.qe + s[r].x);
+      w[r] = ld_relaxed_u64_if(pr, word_ptr(a.qe, s[r].x));
       lv[r] = (sparse && pr) ? a.level[s[r].x - dnp] : 0xffu;
     }
     float in = 0.f;
@@ -623,7 +639,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
     }
     for (uint32_t j = gl + RR * G; j < n_up; j += G) {
       const uint2 sj = a.slots[rec_offset(cur) + j];
-      const unsigned long long wn = ld_relaxed_u64(a.qe + sj.x);
+      const unsigned long long wn = ld_relaxed_u64(word_ptr(a.qe, sj.x));
       const uint32_t lj = sparse ? a.level[sj.x - dnp] : 0xffu;
       bad = bad || (!word_current(wn, sweep) && lj >= (uint32_t)a.current_level);
       in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
@@ -637,8 +653,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
       const uint32_t t = rec_dir(cur) * a.Np + cur.x;
       const float rt = (in + src) + per;                   // Site::get_rate, site.rs:53-56
       const float out = (rt < a.threshold) ? 0.f : rt * att;  // get_outgoing_rate
-      a.incoming[t] = in;
-      st_relaxed_u64(a.qe + t, pack_qe(out * __uint_as_float(cur.y), sweep));
+      commit_slot(a.qe, t, pack_qe(out * __uint_as_float(cur.y), sweep), in);
       ++solved;
     }
     have = have && !commit;
@@ -727,8 +742,8 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
       const uint2 cp = __ldg(a.cellpack + cur.x);  // {(float) attenuation or inactive mark, source}
       if (cp.x == kInactiveCell) {  // inactive: keep q, stamp the word
         if (gl == 0) {
-          const unsigned long long own = ld_relaxed_u64(a.qe + t);
-          st_relaxed_u64(a.qe + t, (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
+          const unsigned long long own = ld_relaxed_u64(word_ptr(a.qe, t));
+          st_relaxed_u64(word_ptr(a.qe, t), (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
         }
         have = false;
       } else if (gl == 0) {
@@ -739,8 +754,8 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
     }
     const uint32_t n_up = have ? rec_count(cur) : 0u;
     const bool p0 = gl < n_up, p1 = gl + kPullGroup < n_up;
-    const unsigned long long* q0 = a.qe + s[0].x;
-    const unsigned long long* q1 = a.qe + s[1].x;
+    const unsigned long long* q0 = word_ptr(a.qe, s[0].x);
+    const unsigned long long* q1 = word_ptr(a.qe, s[1].x);
     const float wt0 = __uint_as_float(s[0].y), wt1 = __uint_as_float(s[1].y);
     const bool big = n_up > (uint32_t)(kPullRounds * kPullGroup);
     unsigned long long w0 = 0;
@@ -760,7 +775,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
       if (big) {
         for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
           const uint2 sj = a.slots[rec_offset(cur) + j];
-          const unsigned long long wn = ld_relaxed_u64(a.qe + sj.x);
+          const unsigned long long wn = ld_relaxed_u64(word_ptr(a.qe, sj.x));
           bad = bad || !word_current(wn, sweep);
           in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
         }
@@ -773,8 +788,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
       if (commit && gl == 0) {
         const float rt = (in + src) + per;                      // Site::get_rate, site.rs:53-56
         const float out = (rt < a.threshold) ? 0.f : rt * att;  // get_outgoing_rate
-        a.incoming[t] = in;
-        st_relaxed_u64(a.qe + t, pack_qe(out * __uint_as_float(cur.y), sweep));
+        commit_slot(a.qe, t, pack_qe(out * __uint_as_float(cur.y), sweep), in);
         ++solved;
       }
       have = have && !commit;
@@ -888,7 +902,7 @@ __device__ __forceinline__ void wave_solve(const PullArgs& a, const WaveTask& w,
   uint32_t q[kWaveSlots];
 #pragma unroll
   for (int j = 0; j < kWaveSlots; ++j)
-    q[j] = (uint32_t)j < n ? ld_relaxed(reinterpret_cast<const uint32_t*>(a.qe + w.s[j].x)) : 0u;
+    q[j] = (uint32_t)j < n ? ld_relaxed(reinterpret_cast<const uint32_t*>(word_ptr(a.qe, w.s[j].x))) : 0u;
   float p[8];
 #pragma unroll
   for (int l = 0; l < 8; ++l) p[l] = 0.f;
@@ -902,7 +916,7 @@ __device__ __forceinline__ void wave_solve(const PullArgs& a, const WaveTask& w,
       for (int l = 0; l < 8; ++l)
         if (j0 + l < n) {
           const uint2 sl = __ldg(base + j0 + l);
-          const float qv = __uint_as_float(ld_relaxed(reinterpret_cast<const uint32_t*>(a.qe + sl.x)));
+          const float qv = __uint_as_float(ld_relaxed(reinterpret_cast<const uint32_t*>(word_ptr(a.qe, sl.x))));
           p[l] = fmaf(__uint_as_float(sl.y), qv, p[l]);
         }
     }
@@ -911,8 +925,7 @@ __device__ __forceinline__ void wave_solve(const PullArgs& a, const WaveTask& w,
   const uint32_t t = rec_dir(w.r) * a.Np + w.r.x;
   const float rt = (in + w.src) + w.per;                    // Site::get_rate, site.rs:53-56
   const float out = (rt < a.threshold) ? 0.f : rt * w.att;  // get_outgoing_rate
-  a.incoming[t] = in;
-  st_relaxed_u64(a.qe + t, pack_qe(out * __uint_as_float(w.r.y), sweep));
+  commit_slot(a.qe, t, pack_qe(out * __uint_as_float(w.r.y), sweep), in);
   ++solved;
 }
 
@@ -1007,8 +1020,7 @@ __device__ __forceinline__ void stg_commit(const PullArgs& a, const uint4& r, co
   const uint32_t t = rec_dir(r) * a.Np + r.x;
   const float rt = (in + c.src) + c.per;                    // Site::get_rate, site.rs:53-56
   const float out = (rt < a.threshold) ? 0.f : rt * c.att;  // get_outgoing_rate
-  a.incoming[t] = in;
-  st_relaxed_u64(a.qe + t, pack_qe(out * __uint_as_float(r.y), sweep));
+  commit_slot(a.qe, t, pack_qe(out * __uint_as_float(r.y), sweep), in);
 }
 
 // Fully staged wavefront kernel (one block of 1024 threads per SM).  A plain load still
@@ -1053,7 +1065,7 @@ __host__ __device__ constexpr size_t stg_smem_bytes(uint32_t cap, uint32_t lvl_w
 // written during a level, and the barrier's acquire fence leaves no stale line in L1, so
 // the load may be served by L1: neighbouring tasks of a block share many upwind words.
 __device__ __forceinline__ uint32_t stg_word(const PullArgs& a, uint32_t t) {
-  return *reinterpret_cast<const unsigned int*>(a.qe + t);
+  return *reinterpret_cast<const unsigned int*>(word_ptr(a.qe, t));
 }
 
 // incoming rate of one task (the lockstep kernels' sum): the first 16 neighbours' words
@@ -1246,7 +1258,7 @@ __device__ __forceinline__ float gather_in(const PullArgs& a, uint32_t c, uint32
     const uint4 g = a.geo16[f];
     if ((g.w >> kKindShift) != want) continue;
     const float s = face_eff(g, fx, fy, fz, a.geo64 + f, dx, dy, dz);
-    if (s < 0.f) in = fmaf(-s, __uint_as_float((uint32_t)a.qe[(size_t)d * a.Np + (g.w & kNbrMask)]), in);
+    if (s < 0.f) in = fmaf(-s, __uint_as_float((uint32_t)*word_ptr(a.qe, (size_t)d * a.Np + (g.w & kNbrMask))), in);
   }
   return in;
 }
@@ -1312,7 +1324,7 @@ __global__ void k_fold_pull(PullArgs a, float* periodic, const uint32_t* cells, 
     } else {
       for (uint32_t k = 0; k < n; ++k) {
         const uint2 sl = slots[e * kFoldSlots + k];
-        in = fmaf(__uint_as_float(sl.y), __uint_as_float((uint32_t)a.qe[sl.x]), in);
+        in = fmaf(__uint_as_float(sl.y), __uint_as_float((uint32_t)*word_ptr(a.qe, sl.x)), in);
       }
     }
     periodic[(size_t)d * a.Np + c] = in;
@@ -1339,8 +1351,8 @@ __device__ __forceinline__ bool cell_current(const PullArgs& a, uint32_t c) {
 __device__ __forceinline__ float current_incoming(const PullArgs& a, uint32_t c, uint32_t d, uint32_t last_epoch,
                                                   bool cell_is_current) {
   const size_t t = (size_t)d * a.Np + c;
-  if (cell_is_current) return a.incoming[t];
-  if ((uint32_t)(a.qe[t] >> 32) == (last_epoch << 1)) return a.incoming[t];  // solved, not stamped
+  if (cell_is_current) return stored_incoming(a.qe, t);
+  if ((uint32_t)(*word_ptr(a.qe, t) >> 32) == (last_epoch << 1)) return stored_incoming(a.qe, t);  // solved, not stamped
   return gather_in(a, c, d, false);
 }
 
@@ -1386,7 +1398,7 @@ __global__ void k_export_pull(PullArgs a, uint32_t last_epoch, int which, double
         const float s = face_eff(a.geo16[f], fx, fy, fz, a.geo64 + f, dx, dy, dz);
         if (s > 0.f) area_down += s;
       }
-      v = __uint_as_float((uint32_t)a.qe[t]) * area_down;
+      v = __uint_as_float((uint32_t)*word_ptr(a.qe, t)) * area_down;
     }
     out[i] = (double)v * rate_scale;
   }
