@@ -178,14 +178,14 @@ def bytes_per_task(f_dn: float, rate_bytes: int, counter_bytes: int = 1) -> floa
     return rate_bytes * (4 + 2 * f_dn) + 2 * counter_bytes * f_dn
 
 
-def build_workload(name: str, n_per_side, nthreads: int):
+def build_workload(name: str, n_per_side, nthreads: int, grid_device: str = "host"):
     from subsweep_gb300 import workloads
     if name == "c2":
-        return workloads.c2_lognormal(n_per_side=n_per_side or 128, nthreads=nthreads)
+        return workloads.c2_lognormal(n_per_side=n_per_side or 128, nthreads=nthreads, grid_device=grid_device)
     if name == "c1":
-        return workloads.c1_small_periodic(n_per_side=n_per_side or 32, nthreads=nthreads)
+        return workloads.c1_small_periodic(n_per_side=n_per_side or 32, nthreads=nthreads, grid_device=grid_device)
     if name == "c4":
-        return workloads.c4_grf(n_per_side=n_per_side or 256, nthreads=nthreads)
+        return workloads.c4_grf(n_per_side=n_per_side or 256, nthreads=nthreads, grid_device=grid_device)
     if name == "c3":
         return workloads.c3_batched(num_boxes=n_per_side or 256, nthreads=nthreads)
     raise SystemExit(f"unknown workload {name}")
@@ -291,7 +291,8 @@ def run_ours(args, dist: Dist):
 
     device = dist.local
     t0 = time.perf_counter()
-    w = build_workload(args.workload, args.n_per_side, nthreads=os.cpu_count() or 1)
+    # the grids of the GPU arm are built on the GPU (csrc/voronoi_gpu.cu)
+    w = build_workload(args.workload, args.n_per_side, nthreads=os.cpu_count() or 1, grid_device="gpu")
     grid_s = time.perf_counter() - t0
     directions = directions_from_num(w.params.num_directions())
     f_dn = mean_downwind_faces(w.grid, directions)
@@ -381,7 +382,7 @@ def run_ours(args, dist: Dist):
         "config": dict(w.describe(), precision=head, replicas=args.gpus, cuda_graph_steps=bool(args.graphs),
                        l2="per-(cell,dir) state of %.1f GB per array > 129 MB L2; no flush needed" %
                           (n * ((w.params.num_directions() + 7) // 8 * 8) * 4 / 1e9),
-                       grid_build_s=round(grid_s, 1)),
+                       grid_build_s=round(grid_s, 1), grid_builder="gpu"),
         "chem_cells_per_s": mixed["chem_cells_per_s"],
         "chemistry": chemistry_figures(d, mixed),
         "fp64": ({k: results["fp64"][k] for k in ("cell_dir_updates_per_s", "chem_cells_per_s", "ms_per_step")}

@@ -154,6 +154,18 @@ def load_gpu() -> ctypes.CDLL:
     lib.sw_last_error.restype = ctypes.c_char_p
     lib.sw_destroy.argtypes = [c_void_p]
     lib.sw_destroy.restype = None
+    # GPU Voronoi producer (csrc/voronoi_gpu.h)
+    lib.sw_gpu_grid_voronoi.restype = c_void_p
+    lib.sw_gpu_grid_voronoi.argtypes = [c_void_p, c_int64, c_void_p, c_int32]
+    lib.sw_gpu_grid_status.restype = c_int32
+    lib.sw_gpu_grid_status.argtypes = [c_void_p]
+    for f in ("sw_gpu_grid_num_faces", "sw_gpu_grid_failed_cells", "sw_gpu_grid_dropped_faces"):
+        getattr(lib, f).restype = c_int64
+        getattr(lib, f).argtypes = [c_void_p]
+    lib.sw_gpu_grid_copy.argtypes = [c_void_p] + [c_void_p] * 7
+    lib.sw_gpu_grid_copy.restype = None
+    lib.sw_gpu_grid_free.argtypes = [c_void_p]
+    lib.sw_gpu_grid_free.restype = None
     for name in ABI_SYMBOLS:
         fn = getattr(lib, name)
         if fn.restype is ctypes.c_int:  # default restype: sw_status

@@ -2,7 +2,8 @@
 
 * ``_build/libsubsweep_gpu.so``  — the sweep library behind include/subsweep_gpu.h:
   sweep_fp64.cu (compiled with -fmad=false so FP64 expressions round as the Rust
-  reference's do), sweep_mixed.cu (FMA allowed) and the C++ host runtime.
+  reference's do), sweep_mixed.cu (FMA allowed) and the C++ host runtime, plus the GPU
+  Voronoi producer voronoi_gpu.cu (-fmad=false, as the host producer).
 * ``_build/libsubsweep_grid.so`` — host grid producers (Voronoi / cartesian CSR).
 
 Both are compiled for sm_103a only.  Sources are rebuilt when newer than the output.
@@ -67,6 +68,7 @@ def build(verbose: bool = False) -> dict:
         (CSRC / "sweep_mixed.cu", True),
         (CSRC / "sweep_host.cpp", True),
         (CSRC / "sweep_noalloc.cu", True),
+        (CSRC / "voronoi_gpu.cu", False),
     ]
     with cf.ThreadPoolExecutor(max_workers=4) as ex:
         futs = [ex.submit(_nvcc_obj, src, fmad, verbose) for src, fmad in jobs]

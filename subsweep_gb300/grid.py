@@ -70,6 +70,36 @@ def voronoi(points: np.ndarray, box_size, periodic: bool = True, nthreads: int =
     return _from_handle(lib, h, box, periodic)
 
 
+def voronoi_gpu(points: np.ndarray, box_size, periodic: bool = True) -> Grid:
+    """Voronoi grid of `points` built on the GPU (csrc/voronoi_gpu.cu), one thread per
+    cell: the CSR conventions of `voronoi`, the same faces and neighbours; areas and
+    volumes equal to rounding (the clipping order can differ in its last bits)."""
+    lib = _native.load_gpu()
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    box = np.ascontiguousarray(np.broadcast_to(np.asarray(box_size, np.float64), (3,)))
+    n = pts.shape[0]
+    h = lib.sw_gpu_grid_voronoi(pts.ctypes.data, n, box.ctypes.data, int(periodic))
+    if not h:
+        raise RuntimeError("GPU grid construction rejected its arguments")
+    try:
+        st = lib.sw_gpu_grid_status(h)
+        if st:
+            raise RuntimeError(f"GPU grid construction failed with CUDA error {st}")
+        failed = lib.sw_gpu_grid_failed_cells(h)
+        if failed:
+            raise RuntimeError(f"Voronoi construction failed for {failed} cells")
+        e = lib.sw_gpu_grid_num_faces(h)
+        g = Grid(
+            row_ptr=np.zeros(n + 1, np.int64), nbr=np.zeros(e, np.int32), kind=np.zeros(e, np.uint8),
+            area=np.zeros(e), normal=np.zeros((e, 3)), volume=np.zeros(n), size=np.zeros(n),
+            position=pts.copy(), box_size=box.copy(), periodic=bool(periodic))
+        lib.sw_gpu_grid_copy(h, g.row_ptr.ctypes.data, g.nbr.ctypes.data, g.kind.ctypes.data, g.area.ctypes.data,
+                             g.normal.ctypes.data, g.volume.ctypes.data, g.size.ctypes.data)
+        return g
+    finally:
+        lib.sw_gpu_grid_free(h)
+
+
 def cartesian(nx: int, ny: int, nz: int, cell_size: float, periodic: bool) -> Grid:
     """The reference's cartesian grid (cartesian.rs:220-395) for one rank."""
     lib = _native.load_grid()

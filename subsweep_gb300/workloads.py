@@ -52,15 +52,23 @@ class Workload:
         }
 
 
+def _voronoi(pts: np.ndarray, box: float, nthreads: int, grid_device: str) -> gridmod.Grid:
+    """Periodic Voronoi grid of the generators on the host (`nthreads` threads) or on
+    the GPU (`grid_device="gpu"`, same topology, geometry equal to rounding)."""
+    if grid_device == "gpu":
+        return gridmod.voronoi_gpu(pts, box, periodic=True)
+    return gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
+
+
 def _box_for(n_per_side: int) -> float:
     return MEGAPARSEC * n_per_side / 32.0
 
 
 def c1_small_periodic(n_per_side: int = 32, seed: int = 1, num_directions: int = 84,
-                      nthreads: int = 0) -> Workload:
+                      nthreads: int = 0, grid_device: str = "host") -> Workload:
     box = _box_for(n_per_side)
     pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
-    g = gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
+    g = _voronoi(pts, box, nthreads, grid_device)
     n = g.num_cells
     src = gridmod.place_sources(g, np.array([[box / 2, box / 2, box / 2]]), np.array([5e48]))
     params = SweepParameters(directions=num_directions, num_timestep_levels=1, periodic=True,
@@ -71,11 +79,11 @@ def c1_small_periodic(n_per_side: int = 32, seed: int = 1, num_directions: int =
 
 
 def c2_lognormal(n_per_side: int = 128, seed: int = 2, num_directions: int = 84, num_levels: int = 4,
-                 nthreads: int = 0) -> Workload:
+                 nthreads: int = 0, grid_device: str = "host") -> Workload:
     box = _box_for(n_per_side)
     rng = np.random.default_rng(seed)
     pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
-    g = gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
+    g = _voronoi(pts, box, nthreads, grid_device)
     n = g.num_cells
     sigma = 1.0
     n_h = 1e-3 * np.exp(sigma * rng.standard_normal(n) - 0.5 * sigma * sigma)
@@ -135,10 +143,10 @@ def gaussian_random_field(m: int, ln_sigma: float, seed: int) -> np.ndarray:
 
 
 def c4_grf(n_per_side: int = 256, seed: int = 4, ln_sigma: float = 1.5, num_sources: int = 1000,
-           num_directions: int = 84, num_levels: int = 4, nthreads: int = 0) -> Workload:
+           num_directions: int = 84, num_levels: int = 4, nthreads: int = 0, grid_device: str = "host") -> Workload:
     box = _box_for(n_per_side)
     pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
-    g = gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
+    g = _voronoi(pts, box, nthreads, grid_device)
     n = g.num_cells
     field = gaussian_random_field(n_per_side, ln_sigma, seed)
     ijk = np.minimum((g.position / box * n_per_side).astype(np.int64), n_per_side - 1)
