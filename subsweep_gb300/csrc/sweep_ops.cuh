@@ -280,10 +280,12 @@ const void* pull_kernel(int variant) {
     case 24: return (const void*)swk::k_sweep_pull<2, 4>;
     case 32: return (const void*)swk::k_sweep_pull<3, 2>;
     case 23: return (const void*)swk::k_sweep_pull<2, 3>;
+    case 93: return (const void*)swk::k_sweep_pull_lock<3>;
     case 94: return (const void*)swk::k_sweep_pull_lock<4>;
     case 95: return (const void*)swk::k_sweep_pull_lock<5>;
     case 96: return (const void*)swk::k_sweep_pull_lock<6>;
     case 14: return (const void*)swk::k_sweep_pull<1, 4>;
+    case 83: return (const void*)swk::k_sweep_pull_lock2<3>;
     case 84: return (const void*)swk::k_sweep_pull_lock2<4>;
     case 85: return (const void*)swk::k_sweep_pull_lock2<5>;
     case 86: return (const void*)swk::k_sweep_pull_lock2<6>;
@@ -305,11 +307,13 @@ int pull_variant(const DevicePtrs* p = nullptr) {
   return pull_kernel(v) ? v : kDefaultPullVariant;
 }
 
-// candidates of the autotuner: lockstep blocks of four positions at 4, 5 and 6 target
-// blocks per SM and the nested-loop lockstep form at 4 (the independent-cursor variants
-// measured slower everywhere and would cost trial sweeps: a sweep of a tiny active set
-// is not a trial, so a step may offer a single dense sweep)
-constexpr int kTuneVariants[] = {94, 95, 96, 84};
+// candidates of the autotuner: the nested-loop lockstep form at 4 target blocks per SM
+// and the lockstep blocks of four positions at 3, 4 and 5 (measured on C2 128^3: the
+// nested-loop form at 5 or 6 blocks and the lockstep at 6 keep too many warps ahead of
+// the dependency front and retry up to twice per task; the independent-cursor variants
+// measured slower everywhere; a sweep of a tiny active set is not a trial, so a step
+// may offer a single dense sweep)
+constexpr int kTuneVariants[] = {84, 93, 94, 95};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM
