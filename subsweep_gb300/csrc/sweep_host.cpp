@@ -930,17 +930,14 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
 // ends the remaining sweeps at once, and is read when the step has finished.  Event
 // nodes around each sweep's transport give the transport kernel time.
 // Pull path: whether the sweep of `level` runs over the compacted list of its active
-// positions (above level 0, fewer than half of the cells active, or a transport
-// variant that cannot test levels itself; SUBSWEEP_COMPACT overrides), and that list's
-// buffer, allocated on first use.
+// positions (above level 0 with fewer than half of the cells active; SUBSWEEP_COMPACT
+// overrides), and that list's buffer, allocated on first use.
 static bool pull_sparse(sw_handle* h, int level) {
   const swh::DevicePtrs& p = h->p;
   if (level <= 0) return false;
-  const int v = p.pull_variant > 0 ? p.pull_variant : swh::kDefaultPullVariant;
   if (p.compact_mode == 1) return true;
-  // the independent-cursor variants (below 70) cannot test levels themselves
-  if (p.compact_mode == 2 && v >= 70) return false;
-  return h->n_ge_host[level] * 2 < h->N || v < 70;
+  if (p.compact_mode == 2) return false;
+  return h->n_ge_host[level] * 2 < h->N;
 }
 
 static sw_status ensure_act_list(sw_handle* h, int level) {

@@ -267,28 +267,17 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
   return cudaGetLastError();
 }
 
-// Variants of the pull kernel: independent cursors (10 * cursors per group + target
-// blocks per SM), warp-lockstep blocks of four positions (90 + blocks per SM), their
-// nested-loop form (80 + blocks per SM) and the level-synchronous wavefront (70 +
-// blocks per SM).  SUBSWEEP_PULL_VARIANT picks one.
+// Variants of the pull kernel: warp-lockstep blocks of four positions (90 + target
+// blocks per SM), their nested-loop form (80 + blocks per SM) and the level-synchronous
+// wavefronts (72: registers, 78: TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
 
 const void* pull_kernel(int variant) {
   switch (variant) {
-    case 13: return (const void*)swk::k_sweep_pull<1, 3>;
-    case 15: return (const void*)swk::k_sweep_pull<1, 5>;
-    case 22: return (const void*)swk::k_sweep_pull<2, 2>;
-    case 24: return (const void*)swk::k_sweep_pull<2, 4>;
-    case 32: return (const void*)swk::k_sweep_pull<3, 2>;
-    case 23: return (const void*)swk::k_sweep_pull<2, 3>;
     case 93: return (const void*)swk::k_sweep_pull_lock<3>;
     case 94: return (const void*)swk::k_sweep_pull_lock<4>;
     case 95: return (const void*)swk::k_sweep_pull_lock<5>;
-    case 96: return (const void*)swk::k_sweep_pull_lock<6>;
-    case 14: return (const void*)swk::k_sweep_pull<1, 4>;
     case 83: return (const void*)swk::k_sweep_pull_lock2<3>;
     case 84: return (const void*)swk::k_sweep_pull_lock2<4>;
-    case 85: return (const void*)swk::k_sweep_pull_lock2<5>;
-    case 86: return (const void*)swk::k_sweep_pull_lock2<6>;
     case 72: return (const void*)swk::k_sweep_pull_wave<2>;
     case 78: return (const void*)swk::k_sweep_pull_staged;
     default: return nullptr;

@@ -391,26 +391,15 @@ __global__ void __launch_bounds__(kBitsThreads) k_bits_scatter(const uint32_t* b
 // ---------------------------------------------------------------------------------------
 // Scheduled pull sweep (cooperative launch; every block resident).
 //
-// A group of kPullGroup lanes runs K cursors; cursor v (of V = groups * K) visits the
-// active positions v, v + V, v + 2V, ... in schedule order.  For its current task a
-// cursor gathers the upwind tasks' words through the task's slots (lane l: slots l,
-// l + 8, ...) and commits
+// Groups of kPullGroup lanes visit the active positions in schedule order.  For its
+// current task a group gathers the upwind tasks' words through the task's slots (lane
+// l: slots l, l + 8, ...) and commits
 //   in = sum_slots |area n . d| q(n, d),   out = (in + source/D + periodic) * attenuation
 // (zero below the threshold), q = out / A_down, once every word carries the current
-// sweep number; otherwise it retries.  Each cursor keeps a pipeline of its next
-// positions (position index, record, slots), every stage loaded one task before it is
-// used, so a task waits only for its neighbours' words.  The warp sleeps with
-// exponential backoff only when none of its cursors committed.  Every dependency lies
-// at an earlier position and every cursor walks its positions in order, so the
-// earliest unsolved task can always commit.
-template <int K>
-struct PullCursor {
-  uint32_t i[K];                       // current position index
-  uint4 cur[K], n1[K], n2[K];          // records of positions i, i + V, i + 2V
-  uint32_t p3[K];                      // schedule position of i + 3V
-  uint2 s[K][kPullRounds], ns[K][kPullRounds];  // slots of i and i + V
-  bool have[K];
-};
+// sweep number; otherwise it retries.  The next positions' records and slots are
+// loaded one block ahead, so a task waits only for its neighbours' words.  Every
+// dependency lies at an earlier position and every warp walks its positions in order,
+// so the earliest unsolved task can always commit.
 
 __device__ __forceinline__ uint32_t pull_pos(const PullArgs& a, uint32_t j) { return a.act ? a.act[j] : j; }
 
@@ -420,128 +409,6 @@ __device__ __forceinline__ void load_slots(const PullArgs& a, const uint4& r, ui
 #pragma unroll
   for (int k = 0; k < kPullRounds; ++k)
     if (gl + k * kPullGroup < n) s[k] = __ldg(base + gl + k * kPullGroup);
-}
-
-template <int K, int kMinBlocks>
-__global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull(PullArgs a) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t gl = lane & (kPullGroup - 1);
-  const uint32_t gfirst = lane & ~(uint32_t)(kPullGroup - 1);
-  const uint32_t V = gridDim.x * (kPullThreads / kPullGroup) * K;
-  const uint32_t v0 = (blockIdx.x * (kPullThreads / kPullGroup) + (threadIdx.x / kPullGroup)) * K;
-  const uint32_t count = a.act ? *a.act_count : a.count;
-  const uint32_t sweep = sweep_number(a);
-  PullCursor<K> q;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const uint32_t i = v0 + k;
-    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-    q.i[k] = i;
-    q.cur[k] = q.n1[k] = q.n2[k] = z;
-    q.p3[k] = 0;
-    if (i < count) q.cur[k] = a.rec[pull_pos(a, i)];
-    if (i + V < count) q.n1[k] = a.rec[pull_pos(a, i + V)];
-    if (i + 2 * V < count) q.n2[k] = a.rec[pull_pos(a, i + 2 * V)];
-    if (i + 3 * V < count) q.p3[k] = pull_pos(a, i + 3 * V);
-    q.have[k] = i < count;
-    load_slots(a, q.cur[k], gl, q.s[k]);
-    if (i + V < count) load_slots(a, q.n1[k], gl, q.ns[k]);
-  }
-  unsigned long long solved = 0, attempts = 0, w0 = 0;
-  uint32_t wait_ns = 32;
-  while (true) {
-    bool any_have = false;
-#pragma unroll
-    for (int k = 0; k < K; ++k) any_have = any_have || q.have[k];
-    if (!__any_sync(0xffffffffu, any_have)) break;
-    // the upwind words of the current tasks, and the leaders' cell data
-    unsigned long long w[K][kPullRounds];
-    float src[K], per[K], att[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const uint32_t n_up = q.have[k] ? rec_count(q.cur[k]) : 0u;
-#pragma unroll
-      for (int r = 0; r < kPullRounds; ++r)
-        w[k][r] = ld_relaxed_u64_if(gl + r * kPullGroup < n_up, word_ptr(a.qe, q.s[k][r].x));
-      src[k] = per[k] = att[k] = 0.f;
-      if (q.have[k] && gl == 0) {
-        const uint32_t c = q.cur[k].x;
-        src[k] = a.src_dir[c];
-        per[k] = __ldcg(a.periodic + rec_dir(q.cur[k]) * a.Np + c);
-        att[k] = (float)a.att[c];
-      }
-    }
-    bool progress = false;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const uint32_t n_up = q.have[k] ? rec_count(q.cur[k]) : 0u;
-      float in = 0.f;
-      bool bad = false;
-#pragma unroll
-      for (int r = 0; r < kPullRounds; ++r) {
-        if (gl + r * kPullGroup < n_up) {
-          bad = bad || !word_current(w[k][r], sweep);
-          in = fmaf(__uint_as_float(q.s[k][r].y), __uint_as_float((uint32_t)w[k][r]), in);
-        }
-      }
-      // tasks with more than kPullGroup * kPullRounds upwind faces: the rest from memory
-      for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
-        const uint2 sl = a.slots[rec_offset(q.cur[k]) + j];
-        const unsigned long long wn = ld_relaxed_u64(word_ptr(a.qe, sl.x));
-        bad = bad || !word_current(wn, sweep);
-        in = fmaf(__uint_as_float(sl.y), __uint_as_float((uint32_t)wn), in);
-      }
-      const bool ok = ((__ballot_sync(0xffffffffu, bad) >> gfirst) & ((1u << kPullGroup) - 1u)) == 0u;
-#pragma unroll
-      for (int o = 1; o < kPullGroup; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, kPullGroup);
-      const bool commit = q.have[k] && ok;
-      if (q.have[k] && gl == 0) ++attempts;
-      if (commit && gl == 0) {
-        const uint32_t t = rec_dir(q.cur[k]) * a.Np + q.cur[k].x;
-        const float rt = (in + src[k]) + per[k];                   // Site::get_rate, site.rs:53-56
-        const float out = (rt < a.threshold) ? 0.f : rt * att[k];  // get_outgoing_rate
-        const float qv = out * __uint_as_float(q.cur[k].y);
-        commit_slot(a.qe, t, pack_qe(qv, sweep), in);
-        ++solved;
-      }
-      if (commit) {  // advance the cursor and its pipeline by one position
-        const uint32_t i = q.i[k] + V;
-        q.i[k] = i;
-        q.cur[k] = q.n1[k];
-#pragma unroll
-        for (int r = 0; r < kPullRounds; ++r) q.s[k][r] = q.ns[k][r];
-        q.have[k] = i < count;
-        q.n1[k] = q.n2[k];
-        if (i + V < count) load_slots(a, q.n1[k], gl, q.ns[k]);
-        if (i + 2 * V < count) q.n2[k] = a.rec[q.p3[k]];
-        if (i + 3 * V < count) q.p3[k] = pull_pos(a, i + 3 * V);
-        progress = true;
-      }
-    }
-    if (__any_sync(0xffffffffu, progress)) {
-      w0 = 0;
-      wait_ns = 32;
-    } else {
-      int expired = 0;
-      if (lane == 0) {
-        const unsigned long long now = globaltimer_ns();
-        if (w0 == 0) w0 = now;
-        expired = (now - w0 > a.timeout_ns) || (*(volatile uint32_t*)&a.ctl->error != 0);
-      }
-      if (__shfl_sync(0xffffffffu, expired, 0)) {
-        if (lane == 0) atomicOr(&a.ctl->error, kErrStall);
-        break;
-      }
-      __nanosleep(wait_ns);
-      wait_ns = min(wait_ns * 2, 256u);
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    solved += __shfl_xor_sync(0xffffffffu, solved, o);
-    attempts += __shfl_xor_sync(0xffffffffu, attempts, o);
-  }
-  if (lane == 0 && solved) atomicAdd(&a.ctl->tasks, solved);
-  if (lane == 0 && attempts) atomicAdd(&a.ctl->attempts, attempts);
 }
 
 // Warp-lockstep variant of the pull sweep: warp w owns the blocks of four consecutive
