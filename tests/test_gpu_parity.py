@@ -216,3 +216,47 @@ def test_mixed_precision_cycle_reports_stalled():
         s.run_sweeps()
     assert e.value.status == _native.SW_ERR_STALLED
     s.close()
+
+
+REFERENCE_SWEEP_CASES = [
+    # src/sweep/tests.rs:89-114 (`simple_sweep`): 10^3 cartesian cells of 0.1 m, direction
+    # (1, 1, 1), 1-2 timestep levels, walled or periodic
+    (10, (1.0, 1.0, 1.0), 1, False, 0.0), (10, (1.0, 1.0, 1.0), 2, False, 0.0),
+    (10, (1.0, 1.0, 1.0), 1, True, 0.0), (10, (1.0, 1.0, 1.0), 2, True, 0.0),
+    # src/sweep/tests.rs:116-133: 5^3 cells swept along +x (faces parallel to the direction)
+    (5, (1.0, 0.0, 0.0), 1, False, 0.0),
+    # the same set-ups with a source in one cell, so that the transport is not trivial
+    (10, (1.0, 1.0, 1.0), 2, True, 1e30), (5, (1.0, 0.0, 0.0), 1, False, 1e30),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("n,direction,levels,periodic,source", REFERENCE_SWEEP_CASES)
+def test_reference_sweep_setups(precision, n, direction, levels, periodic, source):
+    """The reference's own sweep tests (ignored there; they assert only that the sweep
+    neither deadlocks nor crashes): the same grids, parameters and initial conditions
+    (`initialize_sweep_test_components_system`, src/sweep/mod.rs:783-797: 1e-10 kg/cm^3,
+    x = 1e-10, T = 1000 K; safety factors 0, max timestep 1 ms, no cooling floor), run
+    through the C ABI against the oracle."""
+    g = gridmod.cartesian(n, n, n, 0.1, periodic)
+    cells = g.num_cells
+    p = SweepParameters(directions=[list(direction)], num_timestep_levels=levels, periodic=periodic,
+                        max_timestep=1e-3, timestep_safety_factor=0.0, chemistry_timestep_safety_factor=0.0,
+                        prevent_cooling=False, significant_rate_threshold=0.0)
+    density = np.full(cells, 1e-10 / 1e-6)
+    src = np.zeros(cells)
+    src[0] = source
+    args = (p, g, density, np.full(cells, 1e-10), np.full(cells, 1000.0), src)
+    gpu = Sweep(*args, precision=precision)
+    orc = binding.OracleSweep(*args, oracle_dirs(p))
+    for _ in range(2):
+        assert gpu.run_sweeps() == orc.run_sweeps()
+    if precision == "fp64":
+        compare_fp64(gpu, orc)
+    else:
+        fg, fo = gpu.fields(), orc.fields()
+        np.testing.assert_array_equal(gpu.cell_state()["level"], fo["level"])
+        assert np.abs(fg["ionized_hydrogen_fraction"] - fo["ionized_hydrogen_fraction"]).max() <= 1e-4
+        assert (np.abs(fg["temperature"] - fo["temperature"]) / fo["temperature"]).max() <= 1e-4
+    gpu.close()
