@@ -396,6 +396,9 @@ def run_ours(args, dist: Dist):
                      "frac": (achieved_gbs / peaks["hbm_gbs"]) if achieved_gbs else None,
                      "traffic": traffic, "traffic_unit": "bytes per launch",
                      "traffic_source": TRAFFIC_SOURCE if traffic else None,
+                     # the measured DRAM bytes over the same CUDA-event time
+                     "traffic_gbs": (traffic * launches / (d["transport_kernel_ms"] / 1e3) / 1e9
+                                     if traffic and d["transport_kernel_ms"] else None),
                      "kernel": "k_sweep_pull" if head == "mixed" else "k_sweep_sched<double>",
                      "bytes_per_task": b_task, "f_dn": f_dn, "launches": launches,
                      "peak_source": peaks["source"]},
