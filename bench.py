@@ -292,7 +292,7 @@ def run_ours(args, dist: Dist):
     device = dist.local
     t0 = time.perf_counter()
     # the grids of the GPU arm are built on the GPU (csrc/voronoi_gpu.cu)
-    w = build_workload(args.workload, args.n_per_side, nthreads=os.cpu_count() or 1, grid_device="gpu")
+    w = build_workload(args.workload, args.n_per_side, nthreads=os.cpu_count() or 1, grid_device=f"gpu:{device}")
     grid_s = time.perf_counter() - t0
     directions = directions_from_num(w.params.num_directions())
     f_dn = mean_downwind_faces(w.grid, directions)

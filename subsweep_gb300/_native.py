@@ -156,7 +156,7 @@ def load_gpu() -> ctypes.CDLL:
     lib.sw_destroy.restype = None
     # GPU Voronoi producer (csrc/voronoi_gpu.h)
     lib.sw_gpu_grid_voronoi.restype = c_void_p
-    lib.sw_gpu_grid_voronoi.argtypes = [c_void_p, c_int64, c_void_p, c_int32]
+    lib.sw_gpu_grid_voronoi.argtypes = [c_void_p, c_int64, c_void_p, c_int32, c_int32]
     lib.sw_gpu_grid_status.restype = c_int32
     lib.sw_gpu_grid_status.argtypes = [c_void_p]
     for f in ("sw_gpu_grid_num_faces", "sw_gpu_grid_failed_cells", "sw_gpu_grid_dropped_faces"):

@@ -560,10 +560,18 @@ struct DeviceBuffers {
 
 extern "C" {
 
-sw_gpu_grid* sw_gpu_grid_voronoi(const double* points, int64_t n, const double box_size[3], int32_t periodic) {
+sw_gpu_grid* sw_gpu_grid_voronoi(const double* points, int64_t n, const double box_size[3], int32_t periodic,
+                                  int32_t device) {
   if (n <= 0 || !points || n >= (int64_t)INT32_MAX) return nullptr;
   sw_gpu_grid* g = new sw_gpu_grid();
   g->n = n;
+  {
+    const cudaError_t de = cudaSetDevice(device);
+    if (de != cudaSuccess) {
+      g->status = (int)de;
+      return g;
+    }
+  }
   vgpu::Params p{};
   p.n = n;
   for (int a = 0; a < 3; ++a) p.L[a] = box_size[a];

@@ -9,10 +9,11 @@ extern "C" {
 
 typedef struct sw_gpu_grid sw_gpu_grid;
 
-/* Voronoi tessellation of `n` generators (xyz interleaved) in [0, box)^3 on device 0's
- * current device; null for invalid arguments.  sw_gpu_grid_status() is the CUDA error
- * of the construction (0: the arrays are valid). */
-sw_gpu_grid* sw_gpu_grid_voronoi(const double* points, int64_t n, const double box_size[3], int32_t periodic);
+/* Voronoi tessellation of `n` generators (xyz interleaved) in [0, box)^3 on `device`
+ * (made the calling thread's current device); null for invalid arguments.
+ * sw_gpu_grid_status() is the CUDA error of the construction (0: the arrays are valid). */
+sw_gpu_grid* sw_gpu_grid_voronoi(const double* points, int64_t n, const double box_size[3], int32_t periodic,
+                                 int32_t device);
 int32_t sw_gpu_grid_status(const sw_gpu_grid* g);
 int64_t sw_gpu_grid_num_faces(const sw_gpu_grid* g);
 int64_t sw_gpu_grid_failed_cells(const sw_gpu_grid* g);

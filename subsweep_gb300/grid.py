@@ -70,7 +70,7 @@ def voronoi(points: np.ndarray, box_size, periodic: bool = True, nthreads: int =
     return _from_handle(lib, h, box, periodic)
 
 
-def voronoi_gpu(points: np.ndarray, box_size, periodic: bool = True) -> Grid:
+def voronoi_gpu(points: np.ndarray, box_size, periodic: bool = True, device: int = 0) -> Grid:
     """Voronoi grid of `points` built on the GPU (csrc/voronoi_gpu.cu), one thread per
     cell: the CSR conventions of `voronoi`, the same faces and neighbours; areas and
     volumes equal to rounding (the clipping order can differ in its last bits)."""
@@ -78,7 +78,7 @@ def voronoi_gpu(points: np.ndarray, box_size, periodic: bool = True) -> Grid:
     pts = np.ascontiguousarray(points, dtype=np.float64)
     box = np.ascontiguousarray(np.broadcast_to(np.asarray(box_size, np.float64), (3,)))
     n = pts.shape[0]
-    h = lib.sw_gpu_grid_voronoi(pts.ctypes.data, n, box.ctypes.data, int(periodic))
+    h = lib.sw_gpu_grid_voronoi(pts.ctypes.data, n, box.ctypes.data, int(periodic), int(device))
     if not h:
         raise RuntimeError("GPU grid construction rejected its arguments")
     try:

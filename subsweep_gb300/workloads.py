@@ -54,9 +54,11 @@ class Workload:
 
 def _voronoi(pts: np.ndarray, box: float, nthreads: int, grid_device: str) -> gridmod.Grid:
     """Periodic Voronoi grid of the generators on the host (`nthreads` threads) or on
-    the GPU (`grid_device="gpu"`, same topology, geometry equal to rounding)."""
-    if grid_device == "gpu":
-        return gridmod.voronoi_gpu(pts, box, periodic=True)
+    a GPU (`grid_device="gpu"` or `"gpu:<index>"`, same topology, geometry equal to
+    rounding)."""
+    if grid_device.startswith("gpu"):
+        index = int(grid_device.split(":")[1]) if ":" in grid_device else 0
+        return gridmod.voronoi_gpu(pts, box, periodic=True, device=index)
     return gridmod.voronoi(pts, box, periodic=True, nthreads=nthreads)
 
 
