@@ -862,7 +862,9 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (ok && pull)
       ok = h->alloc(&qe, 2 * nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
            h->alloc(&act_bits, (nd + 31) / 32) && h->alloc(&cell_sweep, (size_t)h->Np) &&
-           h->alloc(&cellpack, (size_t)h->Np) && h->alloc(&per_pos, (size_t)h->N * h->D + 4);
+           h->alloc(&cellpack, (size_t)h->Np) &&
+           // per-position periodic sources: only for the staged wavefront kernel (78)
+           (p.pull_variant != 78 || h->alloc(&per_pos, (size_t)h->N * h->D + 4));
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
@@ -876,7 +878,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
       cudaMemset(qe, 0, 2 * nd * sizeof(unsigned long long));
       inc = reinterpret_cast<char*>(qe) + 8;  // task 0's incoming rate; stride 16 bytes
       cudaMemset(cell_sweep, 0, (size_t)h->Np * sizeof(uint32_t));
-      cudaMemset(per_pos, 0, ((size_t)h->N * h->D + 4) * sizeof(float));
+      if (per_pos) cudaMemset(per_pos, 0, ((size_t)h->N * h->D + 4) * sizeof(float));
     } else {
       cudaMemset(outg, 0, nd * rb);
       cudaMemset(pend, 0, nd * rb);

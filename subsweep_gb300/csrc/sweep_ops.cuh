@@ -380,7 +380,7 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   void* args[] = {&a};
   uint32_t cap = 0;
   size_t smem = 0;
-  if (fn == (const void*)swk::k_sweep_pull_staged && staged_layout(p, &cap, &smem) != cudaSuccess) {
+  if (fn == (const void*)swk::k_sweep_pull_staged && (!p.per_pos || staged_layout(p, &cap, &smem) != cudaSuccess)) {
     (void)cudaGetLastError();
     fn = pull_kernel(kDefaultPullVariant);  // no room for the stages: the lockstep kernel
   }
