@@ -147,3 +147,22 @@ def test_stats_fields_used_by_smoke_and_bench():
               "kernel_launches", "levelled_sweeps", "schedule_levels", "transport_attempts", "chem_attempts",
               "sweep_ms", "chem_ms", "level_ms", "pull_variant", "graph_launches"):
         assert k in names, k
+
+
+def test_c5_size_rejected_before_any_allocation():
+    """The C5 stress configuration (384^3 cells x 84 directions = 4.76 G tasks) exceeds the
+    32-bit task ids: sw_create rejects it from the sizes alone, before reading an array
+    or touching the device."""
+    lib = _native.load_gpu()
+    p = _native.SwParams()
+    assert lib.sw_default_params(ctypes.byref(p)) == 0
+    p.num_directions = 84
+    p.precision = _native.SW_PRECISION_MIXED
+    g = _native.SwGridCsr()
+    g.num_cells = 384 ** 3  # arrays left NULL: never read
+    init = _native.SwCellInit()
+    h = ctypes.c_void_p()
+    st = lib.sw_create(ctypes.byref(p), ctypes.byref(g), ctypes.byref(init), ctypes.byref(h))
+    assert st == _native.SW_ERR_UNSUPPORTED
+    assert not h.value
+    assert b"2^32" in lib.sw_last_error(None)
