@@ -373,10 +373,11 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
     a.act = act;
     a.act_count = cnt;
   }
-  // sparse sweeps run the lockstep kernel, which tests the upwind cells' levels; the
-  // wavefront kernel needs the levelled schedule
+  // the wavefront kernels run dense sweeps over a levelled schedule only; sparse sweeps
+  // run the handle's lockstep variant (which tests the upwind cells' levels) or the
+  // default one
   const bool wave = variant >= 70 && variant < 80;
-  const void* fn = pull_kernel((p.sparse_sweep || (wave && p.num_sched_levels == 0)) ? kDefaultPullVariant : variant);
+  const void* fn = pull_kernel((wave && (p.sparse_sweep || p.num_sched_levels == 0)) ? kDefaultPullVariant : variant);
   void* args[] = {&a};
   uint32_t cap = 0;
   size_t smem = 0;

@@ -580,6 +580,9 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
   const uint32_t count = a.act ? *a.act_count : a.count;
   const uint32_t sweep = sweep_number(a);
   const bool check_level = a.act == nullptr && a.current_level > 0;
+  // over a compacted list of active positions: an upwind cell below the sweep's level is
+  // inactive and keeps the q of its last solve, its word is accepted as it is
+  const bool sparse = a.act != nullptr && a.current_level > 0;
   uint32_t b = blockIdx.x * (kPullThreads / 32) + threadIdx.x / 32;
   auto idx = [&](uint32_t bb) { return bb * kGroups + g; };
   // pipeline: record + slots of block b, record of b + W, position of b + 2W
@@ -625,17 +628,20 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
     const unsigned long long* q1 = word_ptr(a.qe, s[1].x);
     const float wt0 = __uint_as_float(s[0].y), wt1 = __uint_as_float(s[1].y);
     const bool big = n_up > (uint32_t)(kPullRounds * kPullGroup);
+    const uint32_t dnp = rec_dir(cur) * a.Np;
+    const bool keep0 = sparse && p0 && a.level[s[0].x - dnp] < (uint32_t)a.current_level;
+    const bool keep1 = sparse && p1 && a.level[s[1].x - dnp] < (uint32_t)a.current_level;
     unsigned long long w0 = 0;
     uint32_t wait_ns = 32;
-    // a word that carries the current sweep number is final for the sweep: a retry
-    // reloads only the words that did not
+    // a word that carries the current sweep number (or of an inactive upwind cell) is
+    // final for the sweep: a retry reloads only the words that were not
     unsigned long long x0 = 0, x1 = 0;
     bool need0 = p0, need1 = p1;
     while (true) {
       if (need0) x0 = ld_relaxed_u64(q0);
       if (need1) x1 = ld_relaxed_u64(q1);
-      need0 = p0 && !word_current(x0, sweep);
-      need1 = p1 && !word_current(x1, sweep);
+      need0 = p0 && !keep0 && !word_current(x0, sweep);
+      need1 = p1 && !keep1 && !word_current(x1, sweep);
       bool bad = need0 || need1;
       float in = p0 ? fmaf(wt0, __uint_as_float((uint32_t)x0), 0.f) : 0.f;
       if (p1) in = fmaf(wt1, __uint_as_float((uint32_t)x1), in);
@@ -643,7 +649,8 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
         for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
           const uint2 sj = a.slots[rec_offset(cur) + j];
           const unsigned long long wn = ld_relaxed_u64(word_ptr(a.qe, sj.x));
-          bad = bad || !word_current(wn, sweep);
+          bad = bad || (!word_current(wn, sweep) &&
+                        !(sparse && a.level[sj.x - dnp] < (uint32_t)a.current_level));
           in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
         }
       }
