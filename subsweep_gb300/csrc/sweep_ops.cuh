@@ -10,6 +10,10 @@
 #include "sweep_device.cuh"
 #if SWK_PULL
 #include "sweep_pull.cuh"
+#include "sweep_pull_setup.cuh"
+#include "sweep_pull_lockstep.cuh"
+#include "sweep_pull_wavefront.cuh"
+#include "sweep_pull_fold.cuh"
 #else
 #include "sweep_push_records.cuh"
 #endif

@@ -1,0 +1,325 @@
+// The warp-lockstep pull sweep kernels (pull path).
+// Part of the pull-form transport of the mixed path; the shared definitions
+// (PullArgs, words, records) are in sweep_pull.cuh.
+#pragma once
+
+#include "sweep_pull.cuh"
+
+namespace swk {
+
+// ---------------------------------------------------------------------------------------
+// Scheduled pull sweep (cooperative launch; every block resident).
+//
+// Groups of kPullGroup lanes visit the active positions in schedule order.  For its
+// current task a group gathers the upwind tasks' words through the task's slots (lane
+// l: slots l, l + 8, ...) and commits
+//   in = sum_slots |area n . d| q(n, d),   out = (in + source/D + periodic) * attenuation
+// (zero below the threshold), q = out / A_down, once every word carries the current
+// sweep number; otherwise it retries.  The next positions' records and slots are
+// loaded one block ahead, so a task waits only for its neighbours' words.  Every
+// dependency lies at an earlier position and every warp walks its positions in order,
+// so the earliest unsolved task can always commit.
+
+__device__ __forceinline__ uint32_t pull_pos(const PullArgs& a, uint32_t j) { return a.act ? a.act[j] : j; }
+
+__device__ __forceinline__ void load_slots(const PullArgs& a, const uint4& r, uint32_t gl, uint2 (&s)[kPullRounds]) {
+  const uint32_t n = rec_count(r);
+  const uint2* base = a.slots + rec_offset(r);
+#pragma unroll
+  for (int k = 0; k < kPullRounds; ++k)
+    if (gl + k * kPullGroup < n) s[k] = __ldg(base + gl + k * kPullGroup);
+}
+
+// Warp-lockstep variant of the pull sweep: warp w owns the blocks of four consecutive
+// positions b = w, w + W, ... (group g of the warp takes position 4b + g) and advances
+// all four together once every one has committed, so the pipeline shift is a
+// warp-uniform branch and the four groups' records and slots are contiguous.
+// this lane's slots l, l + G, ... (RR of them) of the task whose record is r
+template <int G, int RR>
+__device__ __forceinline__ void load_slots_g(const PullArgs& a, const uint4& r, uint32_t gl, uint2 (&s)[RR]) {
+  const uint32_t n = rec_count(r);
+  const uint2* base = a.slots + rec_offset(r);
+#pragma unroll
+  for (int k = 0; k < RR; ++k)
+    if (gl + k * G < n) s[k] = __ldg(base + gl + k * G);
+}
+
+template <int kMinBlocks, int G = kPullGroup>
+__global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(PullArgs a) {
+  constexpr int RR = kPullGroup * kPullRounds / G;  // slot rounds per lane (16 slots in registers)
+  constexpr uint32_t kGroups = 32 / G;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = lane & (G - 1);
+  const uint32_t g = lane / G;
+  const uint32_t gfirst = g * G;
+  const uint32_t gmask = ((1u << G) - 1u) << gfirst;
+  const uint32_t W = gridDim.x * (kPullThreads / 32);
+  const uint32_t count = a.act ? *a.act_count : a.count;
+  const uint32_t sweep = sweep_number(a);
+  uint32_t b = blockIdx.x * (kPullThreads / 32) + threadIdx.x / 32;
+  // this group's position index in block bb
+  auto idx = [&](uint32_t bb) { return bb * kGroups + g; };
+  const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+  uint4 cur = z, n1 = z, n2 = z;
+  uint2 s[RR], ns[RR];
+  uint32_t p3 = 0;
+  if (idx(b) < count) cur = a.rec[pull_pos(a, idx(b))];
+  if (idx(b + W) < count) n1 = a.rec[pull_pos(a, idx(b + W))];
+  if (idx(b + 2 * W) < count) n2 = a.rec[pull_pos(a, idx(b + 2 * W))];
+  if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
+  load_slots_g<G, RR>(a, cur, gl, s);
+  if (idx(b + W) < count) load_slots_g<G, RR>(a, n1, gl, ns);
+  bool have = idx(b) < count;
+  // the leader's cell data of the current task, loaded once per block.  Above level 0,
+  // a sweep over every position tests each task's cell level here and stamps the
+  // words of inactive tasks; a sweep over a compacted list of active positions
+  // (`sparse`) instead tests the upwind cells' levels when their words are not current.
+  const bool check_level = a.act == nullptr && a.current_level > 0;
+  const bool sparse = a.act != nullptr && a.current_level > 0;
+  float src = 0.f, per = 0.f, att = 0.f;
+  bool active = true;
+  // One 8-byte load per cell gives {(float) attenuation or the inactive mark, source}
+  // (written by the attenuation kernel); the periodic source only for tasks with an
+  // upwind periodic face.
+  auto load_cell = [&]() {
+    active = true;
+    if (have && (check_level || gl == 0)) {
+      const uint2 cp = __ldg(a.cellpack + cur.x);
+      active = cp.x != kInactiveCell;
+      att = __uint_as_float(cp.x);
+      src = __uint_as_float(cp.y);
+      per = (gl == 0 && rec_periodic(cur)) ? __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x) : 0.f;
+    }
+  };
+  load_cell();
+  unsigned long long solved = 0, attempts = 0, w0 = 0;
+  uint32_t wait_ns = 32;
+  while (b * kGroups < count) {
+    if (have && !active) {  // inactive cell: keep its q, stamp the word with this sweep
+      if (gl == 0) {
+        const uint32_t t = rec_dir(cur) * a.Np + cur.x;
+        const unsigned long long own = ld_relaxed_u64(word_ptr(a.qe, t));
+        st_relaxed_u64(word_ptr(a.qe, t), (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
+      }
+      have = false;
+    }
+    const uint32_t n_up = have ? rec_count(cur) : 0u;
+    const uint32_t dnp = rec_dir(cur) * a.Np;
+    unsigned long long w[RR];
+    uint32_t lv[RR];
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      const bool pr = gl + r * G < n_up;
+      w[r] = ld_relaxed_u64_if(pr, word_ptr(a.qe, s[r].x));
+      lv[r] = (sparse && pr) ? a.level[s[r].x - dnp] : 0xffu;
+    }
+    float in = 0.f;
+    bool bad = false;
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      if (gl + r * G < n_up) {
+        // an upwind cell inactive in this sweep keeps the q of its last solve
+        bad = bad || (!word_current(w[r], sweep) && lv[r] >= (uint32_t)a.current_level);
+        in = fmaf(__uint_as_float(s[r].y), __uint_as_float((uint32_t)w[r]), in);
+      }
+    }
+    for (uint32_t j = gl + RR * G; j < n_up; j += G) {
+      const uint2 sj = a.slots[rec_offset(cur) + j];
+      const unsigned long long wn = ld_relaxed_u64(word_ptr(a.qe, sj.x));
+      const uint32_t lj = sparse ? a.level[sj.x - dnp] : 0xffu;
+      bad = bad || (!word_current(wn, sweep) && lj >= (uint32_t)a.current_level);
+      in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
+    }
+    const uint32_t badmask = __ballot_sync(0xffffffffu, bad);
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, G);
+    const bool commit = have && (badmask & gmask) == 0u;
+    if (have && gl == 0) ++attempts;
+    if (commit && gl == 0) {
+      const uint32_t t = rec_dir(cur) * a.Np + cur.x;
+      const float rt = (in + src) + per;                   // Site::get_rate, site.rs:53-56
+      const float out = (rt < a.threshold) ? 0.f : rt * att;  // get_outgoing_rate
+      commit_slot(a.qe, t, pack_qe(out * __uint_as_float(cur.y), sweep), in);
+      ++solved;
+    }
+    have = have && !commit;
+    const bool any_commit = __any_sync(0xffffffffu, commit);
+    if (!__any_sync(0xffffffffu, have)) {  // every group of the block done: advance the warp
+      b += W;
+      cur = n1;
+#pragma unroll
+      for (int r = 0; r < RR; ++r) s[r] = ns[r];
+      n1 = n2;
+      have = idx(b) < count;
+      if (idx(b + W) < count) load_slots_g<G, RR>(a, n1, gl, ns);
+      if (idx(b + 2 * W) < count) n2 = a.rec[p3];
+      if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
+      load_cell();
+    }
+    if (any_commit) {
+      w0 = 0;
+      wait_ns = 32;
+    } else {
+      int expired = 0;
+      if (lane == 0) {
+        const unsigned long long now = globaltimer_ns();
+        if (w0 == 0) w0 = now;
+        expired = (now - w0 > a.timeout_ns) || (*(volatile uint32_t*)&a.ctl->error != 0);
+      }
+      if (__shfl_sync(0xffffffffu, expired, 0)) {
+        if (lane == 0) atomicOr(&a.ctl->error, kErrStall);
+        break;
+      }
+      __nanosleep(wait_ns);
+      wait_ns = min(wait_ns * 2, 256u);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    solved += __shfl_xor_sync(0xffffffffu, solved, o);
+    attempts += __shfl_xor_sync(0xffffffffu, attempts, o);
+  }
+  if (lane == 0 && solved) atomicAdd(&a.ctl->tasks, solved);
+  if (lane == 0 && attempts) atomicAdd(&a.ctl->attempts, attempts);
+}
+
+// Lockstep variant with an outer loop over blocks and an inner retry loop: everything
+// a retry does not change (word addresses, predicates, weights, commit address, cell
+// data) is set up once per block, and the next block's record and slot loads are issued
+// when a block starts, so they overlap its waits.  Same additions in the same order as
+// the other variants.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(PullArgs a) {
+  constexpr uint32_t kGroups = 32 / kPullGroup;
+  static_assert(kPullRounds == 2, "two slot rounds per lane");
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = lane & (kPullGroup - 1);
+  const uint32_t g = lane / kPullGroup;
+  const uint32_t gmask = ((1u << kPullGroup) - 1u) << (g * kPullGroup);
+  const uint32_t W = gridDim.x * (kPullThreads / 32);
+  const uint32_t count = a.act ? *a.act_count : a.count;
+  const uint32_t sweep = sweep_number(a);
+  const bool check_level = a.act == nullptr && a.current_level > 0;
+  // over a compacted list of active positions: an upwind cell below the sweep's level is
+  // inactive and keeps the q of its last solve, its word is accepted as it is
+  const bool sparse = a.act != nullptr && a.current_level > 0;
+  uint32_t b = blockIdx.x * (kPullThreads / 32) + threadIdx.x / 32;
+  auto idx = [&](uint32_t bb) { return bb * kGroups + g; };
+  // pipeline: record + slots of block b, record of b + W, position of b + 2W
+  const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+  uint4 cur = z, n1 = z;
+  uint2 s[kPullRounds];
+  uint32_t p2 = 0;
+  if (idx(b) < count) cur = a.rec[pull_pos(a, idx(b))];
+  if (idx(b + W) < count) n1 = a.rec[pull_pos(a, idx(b + W))];
+  if (idx(b + 2 * W) < count) p2 = pull_pos(a, idx(b + 2 * W));
+  load_slots(a, cur, gl, s);
+  uint32_t solved = 0, attempts = 0;
+  bool stop = false;
+  while (!stop && b * kGroups < count) {
+    // next block's pipeline stages, issued now
+    uint2 ns[kPullRounds];
+    uint4 n2 = z;
+    uint32_t p3 = 0;
+    if (idx(b + W) < count) load_slots(a, n1, gl, ns);
+    if (idx(b + 2 * W) < count) n2 = a.rec[p2];
+    if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
+    // this block's task
+    bool have = idx(b) < count;
+    const uint32_t t = rec_dir(cur) * a.Np + cur.x;
+    float src = 0.f, per = 0.f, att = 0.f;
+    if (have && (check_level || gl == 0)) {
+      const uint2 cp = __ldg(a.cellpack + cur.x);  // {(float) attenuation or inactive mark, source}
+      if (cp.x == kInactiveCell) {  // inactive: keep q, stamp the word
+        if (gl == 0) {
+          const unsigned long long own = ld_relaxed_u64(word_ptr(a.qe, t));
+          st_relaxed_u64(word_ptr(a.qe, t), (own & 0xffffffffull) | ((unsigned long long)((sweep << 1) | 1u) << 32));
+        }
+        have = false;
+      } else if (gl == 0) {
+        src = __uint_as_float(cp.y);
+        per = rec_periodic(cur) ? __ldcg(a.periodic + t) : 0.f;
+        att = __uint_as_float(cp.x);
+      }
+    }
+    const uint32_t n_up = have ? rec_count(cur) : 0u;
+    const bool p0 = gl < n_up, p1 = gl + kPullGroup < n_up;
+    const unsigned long long* q0 = word_ptr(a.qe, s[0].x);
+    const unsigned long long* q1 = word_ptr(a.qe, s[1].x);
+    const float wt0 = __uint_as_float(s[0].y), wt1 = __uint_as_float(s[1].y);
+    const bool big = n_up > (uint32_t)(kPullRounds * kPullGroup);
+    const uint32_t dnp = rec_dir(cur) * a.Np;
+    const bool keep0 = sparse && p0 && a.level[s[0].x - dnp] < (uint32_t)a.current_level;
+    const bool keep1 = sparse && p1 && a.level[s[1].x - dnp] < (uint32_t)a.current_level;
+    unsigned long long w0 = 0;
+    uint32_t wait_ns = 32;
+    // a word that carries the current sweep number (or of an inactive upwind cell) is
+    // final for the sweep: a retry reloads only the words that were not
+    unsigned long long x0 = 0, x1 = 0;
+    bool need0 = p0, need1 = p1;
+    while (true) {
+      if (need0) x0 = ld_relaxed_u64(q0);
+      if (need1) x1 = ld_relaxed_u64(q1);
+      need0 = p0 && !keep0 && !word_current(x0, sweep);
+      need1 = p1 && !keep1 && !word_current(x1, sweep);
+      bool bad = need0 || need1;
+      float in = p0 ? fmaf(wt0, __uint_as_float((uint32_t)x0), 0.f) : 0.f;
+      if (p1) in = fmaf(wt1, __uint_as_float((uint32_t)x1), in);
+      if (big) {
+        for (uint32_t j = gl + kPullRounds * kPullGroup; j < n_up; j += kPullGroup) {
+          const uint2 sj = a.slots[rec_offset(cur) + j];
+          const unsigned long long wn = ld_relaxed_u64(word_ptr(a.qe, sj.x));
+          bad = bad || (!word_current(wn, sweep) &&
+                        !(sparse && a.level[sj.x - dnp] < (uint32_t)a.current_level));
+          in = fmaf(__uint_as_float(sj.y), __uint_as_float((uint32_t)wn), in);
+        }
+      }
+      const uint32_t badmask = __ballot_sync(0xffffffffu, bad);
+#pragma unroll
+      for (int o = 1; o < kPullGroup; o <<= 1) in += __shfl_xor_sync(0xffffffffu, in, o, kPullGroup);
+      const bool commit = have && (badmask & gmask) == 0u;
+      if (have && gl == 0) ++attempts;
+      if (commit && gl == 0) {
+        const float rt = (in + src) + per;                      // Site::get_rate, site.rs:53-56
+        const float out = (rt < a.threshold) ? 0.f : rt * att;  // get_outgoing_rate
+        commit_slot(a.qe, t, pack_qe(out * __uint_as_float(cur.y), sweep), in);
+        ++solved;
+      }
+      have = have && !commit;
+      if (!__any_sync(0xffffffffu, have)) break;
+      if (__any_sync(0xffffffffu, commit)) {
+        w0 = 0;
+        wait_ns = 32;
+        continue;
+      }
+      int expired = 0;
+      if (lane == 0) {
+        const unsigned long long now = globaltimer_ns();
+        if (w0 == 0) w0 = now;
+        expired = (now - w0 > a.timeout_ns) || (*(volatile uint32_t*)&a.ctl->error != 0);
+      }
+      if (__shfl_sync(0xffffffffu, expired, 0)) {
+        if (lane == 0) atomicOr(&a.ctl->error, kErrStall);
+        stop = true;
+        break;
+      }
+      __nanosleep(wait_ns);
+      wait_ns = min(wait_ns * 2, 256u);
+    }
+    // advance the pipeline by one block
+    b += W;
+    cur = n1;
+#pragma unroll
+    for (int r = 0; r < kPullRounds; ++r) s[r] = ns[r];
+    n1 = n2;
+    p2 = p3;
+  }
+  unsigned long long ts = solved, ta = attempts;
+  for (int o = 16; o > 0; o >>= 1) {
+    ts += __shfl_xor_sync(0xffffffffu, ts, o);
+    ta += __shfl_xor_sync(0xffffffffu, ta, o);
+  }
+  if (lane == 0 && ts) atomicAdd(&a.ctl->tasks, ts);
+  if (lane == 0 && ta) atomicAdd(&a.ctl->attempts, ta);
+}
+
+}  // namespace swk
