@@ -15,8 +15,8 @@ namespace swk {
 // l: slots l, l + 8, ...) and commits
 //   in = sum_slots |area n . d| q(n, d),   out = (in + source/D + periodic) * attenuation
 // (zero below the threshold), q = out / A_down, once every word carries the current
-// sweep number; otherwise it retries.  The next positions' records and slots are
-// loaded one block ahead, so a task waits only for its neighbours' words.  Every
+// sweep number; otherwise it retries.  The next positions' records, slots and cell data
+// are loaded one block ahead, so a task waits only for its neighbours' words.  Every
 // dependency lies at an earlier position and every warp walks its positions in order,
 // so the earliest unsolved task can always commit.
 
@@ -80,18 +80,27 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
   bool active = true;
   // One 8-byte load per cell gives {(float) attenuation or the inactive mark, source}
   // (written by the attenuation kernel); the periodic source only for tasks with an
-  // upwind periodic face.
-  auto load_cell = [&]() {
+  // upwind periodic face.  Both are loaded one block ahead, with the slots: whether the
+  // cell is active decides which lanes load words, so a pack loaded in the block itself
+  // would hold back its word loads.
+  const bool cell_lane = check_level || gl == 0;
+  uint2 cp = make_uint2(0u, 0u), ncp = make_uint2(0u, 0u);
+  float nper = 0.f;
+  auto fetch_cell = [&](const uint4& r, uint2& pk, float& pr) {
+    pk = __ldg(a.cellpack + r.x);
+    pr = (gl == 0 && rec_periodic(r)) ? __ldcg(a.periodic + rec_dir(r) * a.Np + r.x) : 0.f;
+  };
+  auto take_cell = [&]() {
     active = true;
-    if (have && (check_level || gl == 0)) {
-      const uint2 cp = __ldg(a.cellpack + cur.x);
+    if (have && cell_lane) {
       active = cp.x != kInactiveCell;
       att = __uint_as_float(cp.x);
       src = __uint_as_float(cp.y);
-      per = (gl == 0 && rec_periodic(cur)) ? __ldcg(a.periodic + rec_dir(cur) * a.Np + cur.x) : 0.f;
     }
   };
-  load_cell();
+  if (have && cell_lane) fetch_cell(cur, cp, per);
+  if (idx(b + W) < count && cell_lane) fetch_cell(n1, ncp, nper);
+  take_cell();
   unsigned long long solved = 0, attempts = 0, w0 = 0;
   uint32_t wait_ns = 32;
   while (b * kGroups < count) {
@@ -150,11 +159,16 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
 #pragma unroll
       for (int r = 0; r < RR; ++r) s[r] = ns[r];
       n1 = n2;
+      cp = ncp;
+      per = nper;
       have = idx(b) < count;
-      if (idx(b + W) < count) load_slots_g<G, RR>(a, n1, gl, ns);
+      if (idx(b + W) < count) {
+        load_slots_g<G, RR>(a, n1, gl, ns);
+        if (cell_lane) fetch_cell(n1, ncp, nper);
+      }
       if (idx(b + 2 * W) < count) n2 = a.rec[p3];
       if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
-      load_cell();
+      take_cell();
     }
     if (any_commit) {
       w0 = 0;
@@ -184,9 +198,11 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock(Pu
 
 // Lockstep variant with an outer loop over blocks and an inner retry loop: everything
 // a retry does not change (word addresses, predicates, weights, commit address, cell
-// data) is set up once per block, and the next block's record and slot loads are issued
-// when a block starts, so they overlap its waits.  Same additions in the same order as
-// the other variants.
+// data) is set up once per block, and the next block's record, slots, cell pack and
+// periodic source are loaded when a block starts, so they overlap its waits and a block
+// waits only for its neighbours' words (a cell pack loaded in the block itself would
+// hold back the word loads: whether the cell is active decides which lanes load).  Same
+// additions in the same order as the other variants.
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(PullArgs a) {
   constexpr uint32_t kGroups = 32 / kPullGroup;
@@ -213,6 +229,16 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
   if (idx(b + W) < count) n1 = a.rec[pull_pos(a, idx(b + W))];
   if (idx(b + 2 * W) < count) p2 = pull_pos(a, idx(b + 2 * W));
   load_slots(a, cur, gl, s);
+  // the cell pack {(float) attenuation or inactive mark, source} of a block's task (every
+  // lane above level 0, else the leader) and its periodic source (leader, periodic tasks)
+  const bool cell_lane = check_level || gl == 0;
+  uint2 cp = make_uint2(0u, 0u);
+  float per = 0.f;
+  auto load_cell = [&](const uint4& r, uint2& pk, float& pr) {
+    pk = __ldg(a.cellpack + r.x);
+    pr = (gl == 0 && rec_periodic(r)) ? __ldcg(a.periodic + rec_dir(r) * a.Np + r.x) : 0.f;
+  };
+  if (idx(b) < count && cell_lane) load_cell(cur, cp, per);
   uint32_t solved = 0, attempts = 0;
   bool stop = false;
   while (!stop && b * kGroups < count) {
@@ -220,15 +246,19 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
     uint2 ns[kPullRounds];
     uint4 n2 = z;
     uint32_t p3 = 0;
-    if (idx(b + W) < count) load_slots(a, n1, gl, ns);
+    uint2 ncp = make_uint2(0u, 0u);
+    float nper = 0.f;
+    if (idx(b + W) < count) {
+      load_slots(a, n1, gl, ns);
+      if (cell_lane) load_cell(n1, ncp, nper);
+    }
     if (idx(b + 2 * W) < count) n2 = a.rec[p2];
     if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
     // this block's task
     bool have = idx(b) < count;
     const uint32_t t = rec_dir(cur) * a.Np + cur.x;
-    float src = 0.f, per = 0.f, att = 0.f;
-    if (have && (check_level || gl == 0)) {
-      const uint2 cp = __ldg(a.cellpack + cur.x);  // {(float) attenuation or inactive mark, source}
+    float src = 0.f, att = 0.f;
+    if (have && cell_lane) {
       if (cp.x == kInactiveCell) {  // inactive: keep q, stamp the word
         if (gl == 0) {
           const unsigned long long own = ld_relaxed_u64(word_ptr(a.qe, t));
@@ -237,7 +267,6 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
         have = false;
       } else if (gl == 0) {
         src = __uint_as_float(cp.y);
-        per = rec_periodic(cur) ? __ldcg(a.periodic + t) : 0.f;
         att = __uint_as_float(cp.x);
       }
     }
@@ -310,6 +339,8 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lock2(P
     cur = n1;
 #pragma unroll
     for (int r = 0; r < kPullRounds; ++r) s[r] = ns[r];
+    cp = ncp;
+    per = nper;
     n1 = n2;
     p2 = p3;
   }
