@@ -135,7 +135,7 @@ struct PrecisionOps {
 
 // pull path: transport kernel variant used without autotuning (lockstep blocks of four
 // positions, 4 target blocks per SM)
-constexpr int kDefaultPullVariant = 94;
+constexpr int kDefaultPullVariant = 84;
 
 extern const PrecisionOps kOpsFP64;
 extern const PrecisionOps kOpsMixed;
