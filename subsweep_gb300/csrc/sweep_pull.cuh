@@ -21,7 +21,12 @@
 // Geometry is one 16-byte load per face: {area * n (FP32, area scaled by 2^-k),
 // neighbour | kind << 30}.  The sign of n . d decides up/downwind exactly: the FP32 dot
 // decides when it exceeds its rounding bound, else the FP64 normal does.  The sweep
-// itself reads precomputed per-position records and upwind slots (below).
+// itself reads precomputed per-position records and upwind slots.
+//
+// The path's kernels: records, upwind slots and the compaction of active positions in
+// sweep_pull_setup.cuh; the warp-lockstep sweep kernels in sweep_pull_lockstep.cuh; the
+// level-synchronous (wavefront) ones in sweep_pull_wavefront.cuh; the periodic fold and
+// the field export in sweep_pull_fold.cuh.
 #pragma once
 
 #include <cuda/atomic>
