@@ -197,12 +197,8 @@ def _cpu_worker(args):
     name, n_per_side, warmup, steps, seed_offset = args
     sys.path.insert(0, str(ROOT))
     from oracle import binding
-    from subsweep_gb300 import workloads
     from subsweep_gb300.sweep import directions_from_num
-    if name == "c1":
-        w = workloads.c1_small_periodic(n_per_side=n_per_side, nthreads=1)
-    else:
-        w = workloads.c2_lognormal(n_per_side=n_per_side, seed=2 + seed_offset, nthreads=1)
+    w = sample_workload(name, n_per_side, seed_offset)
     o = binding.OracleSweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
                             directions_from_num(w.params.num_directions()))
     for _ in range(warmup):
@@ -214,6 +210,26 @@ def _cpu_worker(args):
     dt = time.perf_counter() - t0
     t1_tasks, t1_chem = o.work()
     return t1_tasks - t0_tasks, t1_chem - t0_chem, dt
+
+
+def sample_workload(name: str, n_per_side: int, seed_offset: int):
+    """A bounded CPU sample of a workload: the same generator at n_per_side^3 cells (C4
+    with its sources scaled to the sample's cells), or one C3 box."""
+    from subsweep_gb300 import workloads
+    if name == "c1":
+        return workloads.c1_small_periodic(n_per_side=n_per_side, nthreads=1)
+    if name == "c4":
+        sources = max(1, round(1000 * (n_per_side / 256) ** 3))
+        return workloads.c4_grf(n_per_side=n_per_side, seed=4 + seed_offset, num_sources=sources, nthreads=1)
+    if name == "c3":
+        return workloads.c3_batched(num_boxes=1, seed=3 + seed_offset, nthreads=1)
+    return workloads.c2_lognormal(n_per_side=n_per_side, seed=2 + seed_offset, nthreads=1)
+
+
+def sample_label(name: str, n_per_side: int) -> str:
+    if name == "c3":
+        return "one C3 box (512..64000 cells, 32 dirs, 2 levels) per process"
+    return f"{name.upper()} generator at {n_per_side}^3 cells"
 
 
 def cpu_sample(workload: str, n_per_side: int, warmup: int, steps: int, procs: int):
@@ -246,17 +262,18 @@ def cpu_model() -> str:
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return
+    from subsweep_gb300 import workloads
     procs = os.cpu_count() or 1
     n_side = args.cpu_sample_side
     tasks, chem, wall = cpu_sample(args.workload, n_side, 1, max(1, args.steps), procs)
     value = tasks / wall
-    sample = (f"{args.workload.upper()} generator at {n_side}^3 cells, one oracle process per host core "
+    sample = (f"{sample_label(args.workload, n_side)}, one oracle process per host core "
               f"({procs}), each 1 warm-up + {max(1, args.steps)} timed steps")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": sample, "cpu": cpu_model()},
+        "config": {"workload": workloads.label(args.workload, args.n_per_side), "cpu": cpu_model()},
         "chem_cells_per_s": chem / wall,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -361,7 +378,7 @@ def run_ours(args, dist: Dist):
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         c_tasks, c_chem, c_wall = cpu_sample(args.workload, args.cpu_sample_side, 1, 1, 1)
         cpu = {"value": c_tasks / c_wall, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{args.workload.upper()} generator at {args.cpu_sample_side}^3 cells, oracle, "
+               "sample": f"{sample_label(args.workload, args.cpu_sample_side)}, oracle, "
                          f"1 warm-up + 1 timed step ({c_tasks} tasks, {c_wall:.1f} s)",
                "chem_cells_per_s": c_chem / c_wall}
     if dist.rank != 0:

@@ -66,6 +66,31 @@ def _box_for(n_per_side: int) -> float:
     return MEGAPARSEC * n_per_side / 32.0
 
 
+def label(name: str, n_per_side: int | None = None, num_directions: int | None = None,
+          num_levels: int | None = None) -> str:
+    """The name a workload carries (`Workload.name`), from its parameters alone: the
+    CPU reference arm of the benchmark names the full-size workload it samples without
+    building it.  `n_per_side` is the cells per side (C1, C2, C4) or the number of boxes
+    (C3); None takes the workload's default."""
+    if name == "c1":
+        n, d = n_per_side or 32, num_directions or 84
+        return f"C1 periodic jittered-lattice Voronoi {n}^3, {d} dirs, 1 level"
+    if name == "c2":
+        n, d, lv = n_per_side or 128, num_directions or 84, num_levels or 4
+        return f"C2 periodic jittered-lattice Voronoi {n}^3 lognormal, {d} dirs, {lv} levels"
+    if name == "c3":
+        return _c3_label(n_per_side or 256, 512, 64000, num_directions or 32, num_levels or 2)
+    if name == "c4":
+        n, d, lv = n_per_side or 256, num_directions or 84, num_levels or 4
+        return f"C4 periodic jittered-lattice Voronoi {n}^3 GRF, {d} dirs, {lv} levels"
+    raise ValueError(f"unknown workload {name}")
+
+
+def _c3_label(num_boxes: int, min_cells: int, max_cells: int, num_directions: int, num_levels: int) -> str:
+    return (f"C3 {num_boxes} periodic Poisson Voronoi boxes of {min_cells}..{max_cells} cells, "
+            f"{num_directions} dirs, {num_levels} levels")
+
+
 def c1_small_periodic(n_per_side: int = 32, seed: int = 1, num_directions: int = 84,
                       nthreads: int = 0, grid_device: str = "host") -> Workload:
     box = _box_for(n_per_side)
@@ -75,8 +100,8 @@ def c1_small_periodic(n_per_side: int = 32, seed: int = 1, num_directions: int =
     src = gridmod.place_sources(g, np.array([[box / 2, box / 2, box / 2]]), np.array([5e48]))
     params = SweepParameters(directions=num_directions, num_timestep_levels=1, periodic=True,
                              max_timestep=1.0 * MEGAYEAR, significant_rate_threshold=1e-5)
-    return Workload(f"C1 periodic jittered-lattice Voronoi {n_per_side}^3, {num_directions} dirs, 1 level",
-                    params, g, np.full(n, float(mass_density_from_number_density(1e-3))), np.full(n, 1e-10),
+    return Workload(label("c1", n_per_side, num_directions), params, g,
+                    np.full(n, float(mass_density_from_number_density(1e-3))), np.full(n, 1e-10),
                     np.full(n, 1e4), src, steps=10)
 
 
@@ -94,8 +119,8 @@ def c2_lognormal(n_per_side: int = 128, seed: int = 2, num_directions: int = 84,
     src = gridmod.place_sources(g, pos, rates)
     params = SweepParameters(directions=num_directions, num_timestep_levels=num_levels, periodic=True,
                              max_timestep=1.0 * MEGAYEAR, timestep_safety_factor=0.1)
-    return Workload(f"C2 periodic jittered-lattice Voronoi {n_per_side}^3 lognormal, {num_directions} dirs, "
-                    f"{num_levels} levels", params, g, mass_density_from_number_density(n_h), np.full(n, 1e-10),
+    return Workload(label("c2", n_per_side, num_directions, num_levels), params, g,
+                    mass_density_from_number_density(n_h), np.full(n, 1e-10),
                     np.full(n, 1e4), src, steps=4)
 
 
@@ -124,8 +149,7 @@ def c3_batched(num_boxes: int = 256, seed: int = 3, min_cells: int = 512, max_ce
     n = g.num_cells
     params = SweepParameters(directions=num_directions, num_timestep_levels=num_levels, periodic=True,
                              max_timestep=1.0 * MEGAYEAR, timestep_safety_factor=0.1)
-    return Workload(f"C3 {len(boxes)} periodic Poisson Voronoi boxes of {min_cells}..{max_cells} cells "
-                    f"({n} total), {num_directions} dirs, {num_levels} levels", params, g,
+    return Workload(_c3_label(len(boxes), min_cells, max_cells, num_directions, num_levels), params, g,
                     mass_density_from_number_density(n_h), np.full(n, 1e-10), np.full(n, 1e4), src, steps=4)
 
 
@@ -139,7 +163,7 @@ def gaussian_random_field(m: int, ln_sigma: float, seed: int) -> np.ndarray:
     k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
     amp = np.zeros_like(k2)
     amp[k2 > 0] = 1.0 / np.sqrt(k2[k2 > 0])  # sqrt(P) with P ~ k^-2
-    field = np.fft.irfftn(np.fft.rfftn(white) * amp, s=(m, m, m))
+    field = np.fft.irfftn(np.fft.rfftn(white) * amp, s=(m, m, m), axes=(0, 1, 2))
     field -= field.mean()
     return field * (ln_sigma / field.std())
 
@@ -160,8 +184,8 @@ def c4_grf(n_per_side: int = 256, seed: int = 4, ln_sigma: float = 1.5, num_sour
     src[peaks] = n_h[peaks] / n_h[peaks].sum() * 1e52
     params = SweepParameters(directions=num_directions, num_timestep_levels=num_levels, periodic=True,
                              max_timestep=1.0 * MEGAYEAR)
-    return Workload(f"C4 periodic jittered-lattice Voronoi {n_per_side}^3 GRF, {num_directions} dirs, "
-                    f"{num_levels} levels", params, g, mass_density_from_number_density(n_h), np.full(n, 1e-10),
+    return Workload(label("c4", n_per_side, num_directions, num_levels), params, g,
+                    mass_density_from_number_density(n_h), np.full(n, 1e-10),
                     np.full(n, 1e4), src, steps=4)
 
 

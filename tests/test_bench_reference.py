@@ -1,0 +1,46 @@
+"""bench.py's CPU reference arm (the oracle timed on the host cores) and the workload
+names it reports.  CPU only: `--impl reference` runs no GPU code."""
+import json
+import pathlib
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from subsweep_gb300 import workloads
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+@pytest.mark.parametrize("name,n", [("c1", 6), ("c2", 6), ("c4", 8)])
+def test_label_is_the_constructors_name(name, n):
+    make = {"c1": workloads.c1_small_periodic, "c2": workloads.c2_lognormal, "c4": workloads.c4_grf}[name]
+    kw = {"num_sources": 4} if name == "c4" else {}
+    assert make(n_per_side=n, nthreads=2, **kw).name == workloads.label(name, n)
+
+
+def test_label_of_c3_boxes():
+    box = workloads.c3_box(np.random.default_rng(0), 7, 512, 600, nthreads=2)
+    assert workloads.c3_batched(boxes=[box] * 2).name == workloads.label("c3", 2)
+
+
+def test_reference_arm_json_line():
+    """One JSON line with the GPU arm's metric, unit and full-size workload, the bounded
+    sample described in cpu_baseline, and an e2e block without device copies."""
+    import bench
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--cpu-sample-side", "6",
+                          "--steps", "3", "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert (d["metric"], d["unit"], d["higher_is_better"]) == (bench.METRIC, bench.UNIT, True)
+    assert (d["steps"], d["warmup"], d["n_gpus"]) == (3, 3, 1)
+    assert d["value"] > 0
+    assert d["config"]["workload"] == workloads.label("c2")
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert "6^3" in cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
