@@ -377,7 +377,7 @@ def run_ours(args, dist: Dist):
     cpu = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         c_tasks, c_chem, c_wall = cpu_sample(args.workload, args.cpu_sample_side, 1, 1, 1)
-        cpu = {"value": c_tasks / c_wall, "unit": UNIT, "cores": 1, "kind": "port",
+        cpu = {"value": c_tasks / c_wall, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_model(),
                "sample": f"{sample_label(args.workload, args.cpu_sample_side)}, oracle, "
                          f"1 warm-up + 1 timed step ({c_tasks} tasks, {c_wall:.1f} s)",
                "chem_cells_per_s": c_chem / c_wall}
@@ -418,6 +418,9 @@ def run_ours(args, dist: Dist):
                                      if traffic and d["transport_kernel_ms"] else None),
                      "kernel": "k_sweep_pull" if head == "mixed" else "k_sweep_sched<double>",
                      "bytes_per_task": b_task, "f_dn": f_dn, "launches": launches,
+                     # face geometry, 16 B per face, reported beside B_task and not in it
+                     # (the mixed sweep reads its precomputed records and slots instead)
+                     "geometry_bytes_per_cell": 16.0 * w.grid.num_faces / w.grid.num_cells,
                      "peak_source": peaks["source"]},
         "gpu_launches": int(d["kernel_launches"]),
         "clocks": mixed["clocks"],
