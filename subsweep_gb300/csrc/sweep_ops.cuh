@@ -301,12 +301,12 @@ int pull_variant(const DevicePtrs* p = nullptr) {
 }
 
 // candidates of the autotuner: the nested-loop lockstep form at 4 target blocks per SM
-// and the lockstep blocks of four positions at 3, 4 and 5 (measured on C2 128^3: the
-// nested-loop form at 5 or 6 blocks and the lockstep at 6 keep too many warps ahead of
-// the dependency front and retry up to twice per task; the independent-cursor variants
-// measured slower everywhere; a sweep of a tiny active set is not a trial, so a step
-// may offer a single dense sweep)
-constexpr int kTuneVariants[] = {84, 93, 94, 95};
+// and the lockstep blocks of four positions at 3 and 4 (measured on C2 128^3: the
+// nested-loop form at 5 or 6 blocks and the lockstep at 5 or 6 keep too many warps ahead
+// of the dependency front and retry up to twice per task; the independent-cursor
+// variants measured slower everywhere).  Only dense sweeps are trials and a step may
+// offer a single one (its first), so three candidates finish within three steps.
+constexpr int kTuneVariants[] = {84, 93, 94};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM

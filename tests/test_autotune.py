@@ -14,7 +14,7 @@ from subsweep_gb300.sweep import Sweep
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = {84, 93, 94, 95}
+CANDIDATES = {84, 93, 94}
 
 
 @pytest.mark.parametrize("use_graphs", [False, True])
@@ -25,7 +25,10 @@ def test_autotuned_equals_fixed(use_graphs, monkeypatch):
     mk = lambda tune, graphs: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature,
                                     w.source, precision="mixed", autotune=tune, use_graphs=graphs)
     tuned, fixed = mk(True, use_graphs), mk(False, False)
-    steps = 8  # the first steps have 1, 1, 2, 4 and 8 sweeps; tuning needs one per candidate
+    # the first steps have 1, 1, 2, 4 and 8 sweeps; tuning needs one dense sweep per
+    # candidate and every step opens with one, so it ends within the three warm-up steps
+    # a benchmark runs
+    steps = 8
     for _ in range(steps):
         assert tuned.run_sweeps() == fixed.run_sweeps()
     ft, ff = tuned.fields(), fixed.fields()
@@ -35,7 +38,7 @@ def test_autotuned_equals_fixed(use_graphs, monkeypatch):
     assert st["pull_variant"] in CANDIDATES
     assert fixed.stats()["pull_variant"] == 84  # the nested-loop lockstep kernel
     if use_graphs:
-        assert 0 < st["graph_launches"] < steps  # replay starts once tuning is done
+        assert steps - 3 <= st["graph_launches"] < steps  # replay starts once tuning is done
     tuned.close()
     fixed.close()
 
