@@ -1,6 +1,7 @@
 """Self-validation of the oracle's transport (no reference golden vectors exist for it):
-the analytic attenuation of a 1-D column (examples/sweep_1d.rs setting) and flux
-conservation of the push-form corrections."""
+the analytic attenuation of a 1-D column (examples/sweep_1d.rs setting), flux
+conservation of the push-form corrections, and push-form against pull-form
+agreement."""
 import math
 
 import numpy as np
@@ -65,3 +66,44 @@ def test_periodic_snapshot_vs_immediate_deviation_is_bounded():
         outs.append(o.fields())
     dx = np.abs(outs[0]["ionized_hydrogen_fraction"] - outs[1]["ionized_hydrogen_fraction"]).max()
     assert dx < 0.05
+
+
+def pull_form_incoming(g, dirs, outgoing):
+    """The pull form of the incoming rates: for every upwind LOCAL face of c (neighbour
+    n), |area n.d| * out(n, d) / A_down(n, d), A_down the total effective downwind area
+    of n (boundary and periodic faces included), summed in face order."""
+    n = g.num_cells
+    owner = np.repeat(np.arange(n), np.diff(g.row_ptr))
+    dots = g.normal @ dirs.T                       # faces x directions
+    eff = g.area[:, None] * dots
+    a_down = np.zeros((n, dirs.shape[0]))
+    np.add.at(a_down, owner, np.where(dots > 0.0, eff, 0.0))
+    q = np.divide(outgoing, a_down, out=np.zeros_like(outgoing), where=a_down > 0.0)
+    local = (g.kind == 0)[:, None] & (dots < 0.0)
+    nb = np.where(g.kind == 0, g.nbr, 0)
+    contrib = np.where(local, g.area[:, None] * -dots * q[nb], 0.0)
+    inc = np.zeros_like(outgoing)
+    np.add.at(inc, owner, contrib)
+    return inc
+
+
+def test_push_form_equals_pull_form():
+    """One timestep level, every cell active in every sweep: each sweep's corrections
+    telescope, so after any number of steps the incoming rates the push form
+    accumulated equal the pull form of the final outgoing rates, to rounding."""
+    box = 1.0 * 3.0857e22 / 4
+    pts = gridmod.jittered_lattice(7, box, 0.25, 5)
+    g = gridmod.voronoi(pts, box, periodic=True, nthreads=1)
+    n = g.num_cells
+    src = gridmod.place_sources(g, np.array([[box / 3] * 3, [box * 0.7] * 3]), np.array([1e50, 3e49]))
+    params = SweepParameters(directions=16, num_timestep_levels=1, periodic=True, max_timestep=MEGAYEAR)
+    dirs = np.array(__import__("subsweep_gb300").directions_from_num(16))
+    o = binding.OracleSweep(params, g, np.full(n, float(mass_density_from_number_density(3e-4))),
+                            np.full(n, 1e-10), np.full(n, 1e4), src, dirs)
+    for step in range(3):
+        o.run_sweeps()
+        r = o.rates()
+        pull = pull_form_incoming(g, dirs, r["outgoing"])
+        scale = np.abs(r["incoming"]).max()
+        np.testing.assert_allclose(r["incoming"], pull, rtol=1e-12, atol=1e-12 * scale, err_msg=f"step {step}")
+        assert (pull > 0.0).mean() > 0.5
