@@ -166,3 +166,17 @@ def test_c5_size_rejected_before_any_allocation():
     assert st == _native.SW_ERR_UNSUPPORTED
     assert not h.value
     assert b"2^32" in lib.sw_last_error(None)
+
+
+def test_no_device_fails_loudly():
+    """Without a usable CUDA device a valid handle cannot be created: SW_ERR_CUDA with the
+    runtime's message, never a CPU fallback (on a GPU machine there is nothing to test)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    g, init = _small()
+    p = SweepParameters(directions=16, num_timestep_levels=1, periodic=False, max_timestep=1.0)
+    with pytest.raises(SweepError) as e:
+        Sweep(p, g, **init, precision="mixed")
+    assert e.value.status == _native.SW_ERR_CUDA
+    assert str(e.value)
