@@ -1,0 +1,35 @@
+"""The C ABI from plain C: tests/abi_consumer.c compiles as strict C99 against
+include/subsweep_gpu.h alone, links against the sweep library and runs.  Without a
+device its handle creation must fail with SW_ERR_CUDA and a message (no fallback);
+with one, the consumer steps a small column and reads the fields back."""
+import pathlib
+import shutil
+import subprocess
+
+import pytest
+
+from subsweep_gb300 import _native
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def test_c99_consumer_links_and_runs(tmp_path):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = pathlib.Path(_native.load_gpu()._name)
+    exe = tmp_path / "abi_consumer"
+    build = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", str(ROOT / "include"),
+                            str(ROOT / "tests" / "abi_consumer.c"), "-o", str(exe), str(lib),
+                            f"-Wl,-rpath,{lib.parent}", "-lm"], capture_output=True, text=True)
+    assert build.returncode == 0, build.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
+    first = run.stdout.splitlines()[0].split(" ", 2)
+    assert first[0] == "create"
+    status = int(first[1])
+    if status == _native.SW_OK:
+        x0, t0 = map(float, run.stdout.splitlines()[1].split()[1:])
+        assert 0.0 < x0 <= 1.0 and t0 > 0.0
+    else:
+        assert status == _native.SW_ERR_CUDA and first[2].strip()
