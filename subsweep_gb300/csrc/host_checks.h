@@ -1,0 +1,23 @@
+// Host-side checks exported by libsubsweep_gpu.so beside the C ABI: the runtime's own
+// timestep scheduling (TimestepState in sweep_host.cpp), callable without a device so
+// the CPU tests can hold it against the reference's known answers
+// (src/sweep/timestep_state.rs:98-137).  Not part of the drop-in interface.
+#pragma once
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The levels of one step's sweeps in order after `advances` calls of
+ * advance_allowed_levels, for `num_levels` levels (1..16).  Writes at most `cap`
+ * entries; returns the number of sweeps, or -1 on an invalid argument. */
+int32_t sw_host_sweep_order(int32_t num_levels, int32_t advances, int32_t* out, int32_t cap);
+
+/* The lowest allowed level after `advances` calls; -1 on an invalid argument. */
+int32_t sw_host_lowest_allowed(int32_t num_levels, int32_t advances);
+
+#ifdef __cplusplus
+}
+#endif

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/subsweep_gpu.h"
+#include "host_checks.h"
 #include "launch.h"
 #include "sweep_types.h"
 
@@ -68,6 +69,24 @@ cudaError_t dalloc(T** p, size_t count) {
 }
 
 }  // namespace
+
+int32_t sw_host_sweep_order(int32_t num_levels, int32_t advances, int32_t* out, int32_t cap) {
+  if (num_levels < 1 || num_levels > 16 || advances < 0 || cap < 0 || (cap > 0 && !out)) return -1;
+  TimestepState ts;
+  ts.init(1.0, num_levels);
+  for (int32_t i = 0; i < advances; ++i) ts.advance();
+  const std::vector<int> order = ts.sweep_order();
+  for (size_t i = 0; i < order.size() && (int32_t)i < cap; ++i) out[i] = order[i];
+  return (int32_t)order.size();
+}
+
+int32_t sw_host_lowest_allowed(int32_t num_levels, int32_t advances) {
+  if (num_levels < 1 || num_levels > 16 || advances < 0) return -1;
+  TimestepState ts;
+  ts.init(1.0, num_levels);
+  for (int32_t i = 0; i < advances; ++i) ts.advance();
+  return ts.lowest;
+}
 
 struct sw_handle {
   sw_params params{};
