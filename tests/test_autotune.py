@@ -1,7 +1,7 @@
 """Autotuning of the mixed path's transport kernel.
 
 The first dense sweeps of a handle try each candidate variant (the nested-loop lockstep
-form at 4 target blocks per SM, lockstep blocks of four positions at 3, 4 and 5) and
+form at 4 target blocks per SM, lockstep blocks of four positions at 3 and 4) and
 keep the fastest per task.  Every variant sums in the same order, so a tuned
 handle, with or without graph replay after tuning, matches a handle fixed on the
 default variant bit for bit.
