@@ -70,10 +70,11 @@ typedef struct {
                                   when the step's set of sweeps changes); the transport kernel
                                   time is still recorded, the sweep / chemistry split is not.
                                   Default 0. */
-  int32_t autotune;            /* mixed path: the first sweeps try each transport kernel variant
-                                  (cells per warp, resident blocks per SM) and keep the fastest
-                                  per task; every variant computes identical results.
-                                  Default 1. */
+  int32_t autotune;            /* mixed path: the first dense sweeps (each step opens with one)
+                                  try each transport kernel variant (loop form, resident blocks
+                                  per SM; three candidates, so tuning ends within three steps)
+                                  and keep the fastest per task; every variant computes
+                                  identical results.  Default 1. */
 } sw_params;
 
 /* Face-neighbour CSR uploaded once (replaces the Cell component, grid/cell.rs:92-97).
