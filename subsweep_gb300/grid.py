@@ -8,7 +8,6 @@ sources on their nearest cell as src/source_systems.rs:48-80 does.
 """
 from __future__ import annotations
 
-import ctypes
 import dataclasses
 
 import numpy as np

@@ -5,7 +5,6 @@ agreement."""
 import math
 
 import numpy as np
-import pytest
 
 from oracle import binding
 from subsweep_gb300 import workloads, grid as gridmod

@@ -3,7 +3,6 @@ timing is the slowest rank's and the work is summed) on a world-size-2 gloo grou
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 

@@ -7,7 +7,6 @@ exactly what sw_get_dependency_counts returns, through the C ABI, on consecutive
 that share its fixed scratch array.  This file sorts last so that a run stopping at
 the first failure has already run every other test.
 """
-import ctypes
 
 import numpy as np
 import pytest
