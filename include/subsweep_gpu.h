@@ -12,7 +12,9 @@
  * Plain pointers and sizes only; no CUDA or torch types cross the boundary.  The
  * library owns all device memory.  One host thread per handle; calls on a handle
  * are not re-entrant.  All quantities are SI doubles (m, kg, s, K), as the
- * reference's diman quantities store them.
+ * reference's diman quantities store them.  Every entry point makes the handle's
+ * device current while it runs and makes the caller's current device current again
+ * before it returns.
  */
 #ifndef SUBSWEEP_GPU_H
 #define SUBSWEEP_GPU_H
@@ -210,6 +212,9 @@ sw_status sw_get_time_series(sw_handle* h, sw_time_series* out);
  * part of the state.  sw_checkpoint_size gives the buffer size in bytes. */
 sw_status sw_checkpoint_size(sw_handle* h, size_t* bytes);
 sw_status sw_save_state(sw_handle* h, void* buffer, size_t bytes);
+/* Rejects (SW_ERR_INVALID_ARG) a buffer whose header does not match the handle, that
+ * is shorter than the checkpoint, or that holds a timestep level >= num_timestep_levels,
+ * before any of it reaches the device. */
 sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes);
 
 /* Same result as sw_get_dependency_counts, for callers that cannot allocate device
@@ -218,8 +223,10 @@ sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes);
  * a fixed 16 MiB __device__ array of the library instead of a cudaMalloc'd buffer and
  * allocates nothing.  num_cells * directions must not exceed 16 MiB (SW_ERR_INVALID_ARG
  * otherwise).  The first call on a device looks up the array's device address; make it
- * before any stream capture.  Calls share the array, so calls that overlap on the GPU
- * race.  This entry point has no counterpart in the reference. */
+ * before any stream capture.  That address is kept for the life of the device's primary
+ * context: do not call this again after a cudaDeviceReset in the same process.  Calls
+ * share the array, so calls that overlap on the GPU race.  This entry point has no
+ * counterpart in the reference. */
 sw_status sw_get_dependency_counts_noalloc(sw_handle* h, int32_t level, uint8_t* counts);
 
 /* Message of the last error on this handle ("" if none); with h == NULL, the last

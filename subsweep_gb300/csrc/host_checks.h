@@ -1,9 +1,11 @@
 // Host-side checks exported by libsubsweep_gpu.so beside the C ABI: the runtime's own
 // timestep scheduling (TimestepState in sweep_host.cpp), callable without a device so
 // the CPU tests can hold it against the reference's known answers
-// (src/sweep/timestep_state.rs:98-137).  Not part of the drop-in interface.
+// (src/sweep/timestep_state.rs:98-137), and the checkpoint validation of
+// sw_load_state.  Not part of the drop-in interface.
 #pragma once
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -17,6 +19,13 @@ int32_t sw_host_sweep_order(int32_t num_levels, int32_t advances, int32_t* out, 
 
 /* The lowest allowed level after `advances` calls; -1 on an invalid argument. */
 int32_t sw_host_lowest_allowed(int32_t num_levels, int32_t advances);
+
+/* The validation sw_load_state applies to a checkpoint buffer before anything reaches
+ * the device: the header's magic, version and timestep state, the buffer's length,
+ * and every cell's timestep level below the header's level count.  Returns 0 for a
+ * buffer that passes, 1 for a bad header, 2 for a short buffer, 3 for a level out of
+ * range. */
+int32_t sw_host_check_checkpoint(const void* buffer, size_t bytes);
 
 #ifdef __cplusplus
 }

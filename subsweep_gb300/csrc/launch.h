@@ -154,6 +154,29 @@ struct HandleView {
 bool handle_view(sw_handle* h, HandleView* out);
 // Record an error message on the handle (returned by sw_last_error) and return `st`.
 sw_status handle_fail(sw_handle* h, sw_status st, const char* message);
+// Forget the handle's last error (every entry point starts with this).
+void handle_clear_error(sw_handle* h);
+
+// Makes a handle's device current for the duration of an entry point and makes the
+// caller's device current again on return, so a host that drives other GPU work on
+// another device keeps its own selection.  `status` is the result of the selection.
+struct DeviceScope {
+  int previous = -1;
+  cudaError_t status = cudaSuccess;
+  explicit DeviceScope(int device) {
+    int current = -1;
+    status = cudaGetDevice(&current);
+    if (status == cudaSuccess && current != device) {
+      status = cudaSetDevice(device);
+      if (status == cudaSuccess) previous = current;
+    }
+  }
+  ~DeviceScope() {
+    if (previous >= 0) cudaSetDevice(previous);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
 
 // Precision-independent kernels (compiled in sweep_fp64.cu).
 cudaError_t launch_update_levels(const DevicePtrs&, int lowest_allowed, cudaStream_t);

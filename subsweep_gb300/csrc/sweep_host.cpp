@@ -173,6 +173,12 @@ namespace {
     if (_e != cudaSuccess) return (h)->cuda_fail(_e, where); \
   } while (0)
 
+// The handle's device is current until the entry point returns; the caller's device
+// is current again afterwards.
+#define SW_DEVICE_SCOPE(h)                                    \
+  swh::DeviceScope _device_scope((h)->device);                \
+  if (_device_scope.status != cudaSuccess) return (h)->cuda_fail(_device_scope.status, "select device")
+
 sw_status create_fail(sw_status st, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -470,6 +476,10 @@ sw_status handle_fail(sw_handle* h, sw_status st, const char* message) {
   return st;
 }
 
+void handle_clear_error(sw_handle* h) {
+  if (h) h->last_error.clear();
+}
+
 }  // namespace swh
 
 extern "C" {
@@ -598,10 +608,19 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     delete h;
     return st;
   };
-  cudaError_t ce = (P.device >= 0) ? cudaSetDevice(P.device) : cudaGetDevice(&h->device);
-  if (ce == cudaSuccess && P.device >= 0) h->device = P.device;
+  cudaError_t ce = cudaSuccess;
+  if (P.device >= 0)
+    h->device = P.device;
+  else
+    ce = cudaGetDevice(&h->device);
   if (ce != cudaSuccess) {
     h->cuda_fail(ce, "select device");
+    return bail(SW_ERR_CUDA);
+  }
+  // the handle's device is current while the handle is built (and freed on failure)
+  swh::DeviceScope device_scope(h->device);
+  if (device_scope.status != cudaSuccess) {
+    h->cuda_fail(device_scope.status, "select device");
     return bail(SW_ERR_CUDA);
   }
   int coop = 0, sms = 0;
@@ -1181,7 +1200,7 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
   if (!h) return SW_ERR_INVALID_ARG;
   h->last_error.clear();
   const swh::PrecisionOps& ops = *h->ops;
-  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  SW_DEVICE_SCOPE(h);
   if (h->graph_mode && (h->tuned || !h->autotune)) return step_graph(h, time_elapsed_out);
   uint64_t expected = 0;
   std::vector<int> order = h->ts.sweep_order();
@@ -1321,6 +1340,8 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
 
 sw_status sw_get_fields(sw_handle* h, double* x, double* T, double* dt, double* rate) {
   if (!h) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  SW_DEVICE_SCOPE(h);
   size_t nb = (size_t)h->N * sizeof(double);
   if (x) SW_CUDA(h, cudaMemcpyAsync(x, h->p.xhii, nb, cudaMemcpyDeviceToHost, h->stream), "copy x");
   if (T) SW_CUDA(h, cudaMemcpyAsync(T, h->p.temperature, nb, cudaMemcpyDeviceToHost, h->stream), "copy T");
@@ -1335,6 +1356,8 @@ sw_status sw_get_fields(sw_handle* h, double* x, double* T, double* dt, double* 
 
 sw_status sw_get_cell_state(sw_handle* h, double* change_timescale, uint8_t* level, double* ionization_time) {
   if (!h) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  SW_DEVICE_SCOPE(h);
   size_t nb = (size_t)h->N * sizeof(double);
   if (change_timescale)
     SW_CUDA(h, cudaMemcpyAsync(change_timescale, h->p.change_timescale, nb, cudaMemcpyDeviceToHost, h->stream), "copy");
@@ -1347,6 +1370,8 @@ sw_status sw_get_cell_state(sw_handle* h, double* change_timescale, uint8_t* lev
 
 sw_status sw_set_fields(sw_handle* h, const double* x, const double* T) {
   if (!h) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  SW_DEVICE_SCOPE(h);
   size_t nb = (size_t)h->N * sizeof(double);
   if (x) {
     std::vector<double> y(h->N);
@@ -1366,12 +1391,14 @@ sw_status sw_get_level_counts(sw_handle* h, int64_t* per_level) {
 
 sw_status sw_get_dependency_counts(sw_handle* h, int32_t level, uint8_t* counts) {
   if (!h || !counts || level < 0 || level >= h->L) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  SW_DEVICE_SCOPE(h);
   uint8_t* d_counts = nullptr;
   size_t nb = (size_t)h->N * h->D;
   SW_CUDA(h, cudaMalloc(&d_counts, nb), "alloc");
-  cudaMemsetAsync(d_counts, 0, nb, h->stream);
-  cudaMemsetAsync(h->p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream);
-  cudaError_t e = h->ops->init_counts(h->p, level, d_counts, false, h->stream);
+  // inactive cells' entries are not written by the counting kernel: start from zero
+  cudaError_t e = cudaMemsetAsync(d_counts, 0, nb, h->stream);
+  if (e == cudaSuccess) e = h->ops->init_counts(h->p, level, d_counts, false, h->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_counts, nb, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   cudaFree(d_counts);
@@ -1381,6 +1408,8 @@ sw_status sw_get_dependency_counts(sw_handle* h, int32_t level, uint8_t* counts)
 
 sw_status sw_get_rates(sw_handle* h, double* incoming, double* outgoing, double* periodic) {
   if (!h) return SW_ERR_INVALID_ARG;
+  h->last_error.clear();
+  SW_DEVICE_SCOPE(h);
   size_t nb = (size_t)h->N * h->D * sizeof(double);
   double* d_out = nullptr;
   SW_CUDA(h, cudaMalloc(&d_out, nb), "alloc");
@@ -1440,6 +1469,47 @@ static size_t checkpoint_bytes(sw_handle* h) {
   return total;
 }
 
+// The per-cell level bytes follow seven per-cell double arrays (checkpoint_sections).
+static size_t checkpoint_level_offset(int64_t num_cells) {
+  return sizeof(CheckpointHeader) + 7 * (size_t)num_cells * sizeof(double);
+}
+
+// Checkpoint length implied by a header's counts, in the order of checkpoint_sections;
+// 0 for counts no handle can have.
+static size_t checkpoint_bytes_for(const CheckpointHeader& hd) {
+  if (hd.num_cells < 1 || hd.num_cells >= ((int64_t)1 << 30) || hd.num_directions < 1 ||
+      hd.num_directions > swk::kMaxDirections || hd.num_levels < 1 || hd.num_levels > 16 ||
+      (int64_t)hd.np < hd.num_cells || (hd.rate_bytes != 4 && hd.rate_bytes != 8) ||
+      (hd.precision != SW_PRECISION_FP64 && hd.precision != SW_PRECISION_MIXED))
+    return 0;
+  const size_t n = (size_t)hd.num_cells, nd = (size_t)hd.np * (size_t)hd.num_directions, rb = hd.rate_bytes;
+  size_t total = checkpoint_level_offset(hd.num_cells) + n + nd * rb;
+  total += hd.precision == SW_PRECISION_MIXED ? nd * 16 + n * 4 : 3 * nd * rb;
+  return total;
+}
+
+// Header, length and level checks of a checkpoint buffer, before any byte of it reaches
+// the device: a level >= num_levels would index past the per-level histograms.
+static int32_t check_checkpoint(const void* buffer, size_t bytes, CheckpointHeader* hd_out) {
+  if (bytes < sizeof(CheckpointHeader)) return 2;
+  CheckpointHeader hd;
+  std::memcpy(&hd, buffer, sizeof(hd));
+  if (hd_out) *hd_out = hd;
+  if (hd.magic != kCheckpointMagic || hd.version != 1) return 1;
+  const size_t need = checkpoint_bytes_for(hd);
+  if (need == 0 || hd.ts_lowest < 0 || hd.ts_lowest >= hd.num_levels) return 1;
+  if (bytes < need) return 2;
+  const uint8_t* level = static_cast<const uint8_t*>(buffer) + checkpoint_level_offset(hd.num_cells);
+  for (int64_t c = 0; c < hd.num_cells; ++c)
+    if (level[c] >= hd.num_levels) return 3;
+  return 0;
+}
+
+int32_t sw_host_check_checkpoint(const void* buffer, size_t bytes) {
+  if (!buffer) return 1;
+  return check_checkpoint(buffer, bytes, nullptr);
+}
+
 sw_status sw_checkpoint_size(sw_handle* h, size_t* bytes) {
   if (!h || !bytes) return SW_ERR_INVALID_ARG;
   *bytes = checkpoint_bytes(h);
@@ -1450,7 +1520,7 @@ sw_status sw_save_state(sw_handle* h, void* buffer, size_t bytes) {
   if (!h || !buffer) return SW_ERR_INVALID_ARG;
   h->last_error.clear();
   if (bytes < checkpoint_bytes(h)) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
-  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  SW_DEVICE_SCOPE(h);
   CheckpointHeader hd{};
   hd.magic = kCheckpointMagic;
   hd.version = 1;
@@ -1480,17 +1550,21 @@ sw_status sw_save_state(sw_handle* h, void* buffer, size_t bytes) {
 sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes) {
   if (!h || !buffer) return SW_ERR_INVALID_ARG;
   h->last_error.clear();
-  if (bytes < sizeof(CheckpointHeader)) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
-  CheckpointHeader hd;
-  std::memcpy(&hd, buffer, sizeof(hd));
+  CheckpointHeader hd{};
+  const int32_t check = check_checkpoint(buffer, bytes, &hd);
+  if (check == 2 && bytes < sizeof(CheckpointHeader))
+    return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
   if (hd.magic != kCheckpointMagic || hd.version != 1) return h->fail(SW_ERR_INVALID_ARG, "not a checkpoint");
   if (hd.precision != (uint32_t)h->params.precision || hd.num_cells != h->N || hd.num_faces != h->E ||
       hd.num_directions != h->D || hd.num_levels != h->L || hd.np != h->Np ||
       hd.rate_bytes != (uint32_t)h->ops->rate_bytes)
     return h->fail(SW_ERR_INVALID_ARG, "checkpoint was written by a handle with another grid, parameters or precision");
-  if (bytes < checkpoint_bytes(h)) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
-  if (hd.ts_lowest < 0 || hd.ts_lowest >= h->L) return h->fail(SW_ERR_INVALID_ARG, "corrupt checkpoint header");
-  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  if (checkpoint_bytes_for(hd) != checkpoint_bytes(h))
+    return h->fail(SW_ERR_INVALID_ARG, "checkpoint layout does not match this handle");
+  if (check == 1) return h->fail(SW_ERR_INVALID_ARG, "corrupt checkpoint header");
+  if (check == 2) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
+  if (check == 3) return h->fail(SW_ERR_INVALID_ARG, "corrupt checkpoint: a cell's timestep level is out of range");
+  SW_DEVICE_SCOPE(h);
   const char* in = static_cast<const char*>(buffer);
   size_t off = sizeof(hd);
   for (const CheckpointSection& s : checkpoint_sections(h)) {
@@ -1520,7 +1594,7 @@ sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes) {
 sw_status sw_get_time_series(sw_handle* h, sw_time_series* out) {
   if (!h || !out) return SW_ERR_INVALID_ARG;
   h->last_error.clear();
-  SW_CUDA(h, cudaSetDevice(h->device), "select device");
+  SW_DEVICE_SCOPE(h);
   if (!h->series_dev && !h->alloc(&h->series_dev, swh::kTimeSeriesPartials + 8))
     return h->fail(SW_ERR_OOM, "device allocation of the time-series buffer failed");
   double* partial = h->series_dev;
@@ -1556,6 +1630,7 @@ const char* sw_last_error(const sw_handle* h) {
 
 void sw_destroy(sw_handle* h) {
   if (!h) return;
+  swh::DeviceScope device_scope(h->device);  // frees on the handle's device
   cudaStreamSynchronize(h->stream);
   delete h;
 }

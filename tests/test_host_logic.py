@@ -62,3 +62,41 @@ def test_invalid_arguments(lib):
     assert lib.sw_host_lowest_allowed(0, 0) == -1
     # a short buffer gets the first entries and the full count
     assert lib.sw_host_sweep_order(3, 5, out.ctypes.data, 2) == 4
+
+
+def _checkpoint(num_cells=10, directions=4, levels=3, np_=32, precision=1, rate_bytes=4, level_fill=1):
+    """A checkpoint buffer laid out as sw_save_state writes it: the header, seven
+    per-cell double arrays, the per-cell levels, then the per-task sections."""
+    import struct
+    header = struct.pack("<QIIqqiiIIdiiII", 0x3154504357535553, 1, precision, num_cells, 7 * num_cells,
+                         directions, levels, np_, rate_bytes, 0.0, 0, 1, 5, 4)
+    nd = np_ * directions
+    tail = nd * rate_bytes + (nd * 16 + num_cells * 4 if precision == 1 else 3 * nd * rate_bytes)
+    buf = bytearray(header + bytes(7 * 8 * num_cells) + bytes([level_fill]) * num_cells + bytes(tail))
+    return buf, len(header) + 7 * 8 * num_cells
+
+
+def test_checkpoint_validation_rejects_bad_level_before_upload(lib):
+    """sw_load_state's host-side validation: a checkpoint whose level section holds a
+    level >= num_timestep_levels is refused (it would index the device's per-level
+    histograms out of range), as are a bad header and a short buffer."""
+    lib.sw_host_check_checkpoint.restype = ctypes.c_int32
+    lib.sw_host_check_checkpoint.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    for precision, rate_bytes in ((1, 4), (0, 8)):
+        buf, level_off = _checkpoint(precision=precision, rate_bytes=rate_bytes)
+        assert lib.sw_host_check_checkpoint(bytes(buf), len(buf)) == 0
+        bad = bytearray(buf)
+        bad[level_off + 7] = 3  # one cell at level 3 of 3 levels
+        assert lib.sw_host_check_checkpoint(bytes(bad), len(bad)) == 3
+        bad[level_off + 7] = 255
+        assert lib.sw_host_check_checkpoint(bytes(bad), len(bad)) == 3
+        assert lib.sw_host_check_checkpoint(bytes(buf), len(buf) - 1) == 2
+        assert lib.sw_host_check_checkpoint(bytes(buf[:40]), 40) == 2
+        magic = bytearray(buf)
+        magic[0] ^= 1
+        assert lib.sw_host_check_checkpoint(bytes(magic), len(magic)) == 1
+    # a header whose timestep state or counts no handle can have
+    buf, _ = _checkpoint(levels=17)
+    assert lib.sw_host_check_checkpoint(bytes(buf), len(buf)) == 1
+    buf, _ = _checkpoint(num_cells=40, np_=32)
+    assert lib.sw_host_check_checkpoint(bytes(buf), len(buf)) == 1
