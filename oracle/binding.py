@@ -18,6 +18,8 @@ c_int32, c_int64, c_double, c_void_p = ctypes.c_int32, ctypes.c_int64, ctypes.c_
 
 PERIODIC_SNAPSHOT = 0
 PERIODIC_IMMEDIATE = 1
+ORDER_FIFO = 0
+ORDER_HEAP = 1
 
 
 class OrcGrid(ctypes.Structure):
@@ -29,7 +31,8 @@ class OrcParams(ctypes.Structure):
     _fields_ = [("num_directions", c_int32), ("directions", c_void_p), ("num_timestep_levels", c_int32),
                 ("max_timestep", c_double), ("significant_rate_threshold", c_double),
                 ("timestep_safety_factor", c_double), ("chemistry_timestep_safety_factor", c_double),
-                ("prevent_cooling", c_int32), ("scale_factor", c_double), ("periodic_mode", c_int32)]
+                ("prevent_cooling", c_int32), ("scale_factor", c_double), ("periodic_mode", c_int32),
+                ("order", c_int32), ("num_threads", c_int32)]
 
 
 # names of the reference's time-series outputs (src/sweep/time_series.rs:26-48)
@@ -81,17 +84,60 @@ def load() -> ctypes.CDLL:
         [c_double] * 5 + [c_int32, c_double, c_double, c_double, c_double, ctypes.POINTER(c_double),
                           ctypes.POINTER(c_int32)]
     lib.orc_solver_perform_timestep.restype = c_int32
+    lib.orc_voronoi_build.restype = c_void_p
+    lib.orc_voronoi_build.argtypes = [c_void_p, c_int64, c_double, c_int32]
+    for name in ("orc_voronoi_num_faces", "orc_voronoi_failed_cells", "orc_voronoi_dropped_faces"):
+        getattr(lib, name).restype = c_int64
+        getattr(lib, name).argtypes = [c_void_p]
+    lib.orc_voronoi_copy.argtypes = [c_void_p] * 8
+    lib.orc_voronoi_free.argtypes = [c_void_p]
+    lib.orc_directions_from_num.argtypes = [c_int32, c_void_p]
+    lib.orc_directions_from_num.restype = c_int32
+    lib.orc_heap_replay.argtypes = [c_void_p, c_int64, c_void_p, c_int64, c_void_p]
+    lib.orc_heap_replay.restype = c_int64
     lib.orc_outgoing_rate.argtypes = [c_double] * 5
     lib.orc_outgoing_rate.restype = c_double
     _lib = lib
     return lib
 
 
+def directions_from_num(num: int) -> np.ndarray:
+    """The reference's direction table for `num` directions (Directions::from_num)."""
+    out = np.zeros((num, 3))
+    if load().orc_directions_from_num(num, out.ctypes.data) != 0:
+        raise ValueError(f"no direction table for {num} directions")
+    return out
+
+
+def voronoi(points: np.ndarray, box: float, num_threads: int = 1) -> dict:
+    """Periodic Voronoi tessellation of `points` in [0, box)^3 by the oracle's own
+    producer (voronoi_oracle.cpp): the CSR arrays as a dict (the fields of a sweep
+    grid) plus the counts of failed cells and dropped one-sided faces."""
+    lib = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    n = pts.shape[0]
+    h = lib.orc_voronoi_build(pts.ctypes.data, n, float(box), int(num_threads))
+    if not h:
+        raise ValueError("invalid Voronoi arguments")
+    try:
+        e = lib.orc_voronoi_num_faces(h)
+        g = {"row_ptr": np.zeros(n + 1, np.int64), "nbr": np.zeros(e, np.int32), "kind": np.zeros(e, np.uint8),
+             "area": np.zeros(e), "normal": np.zeros((e, 3)), "volume": np.zeros(n), "size": np.zeros(n)}
+        lib.orc_voronoi_copy(h, *(g[k].ctypes.data for k in ("row_ptr", "nbr", "kind", "area", "normal",
+                                                              "volume", "size")))
+        g["failed_cells"] = lib.orc_voronoi_failed_cells(h)
+        g["dropped_faces"] = lib.orc_voronoi_dropped_faces(h)
+        return g
+    finally:
+        lib.orc_voronoi_free(h)
+
+
 class OracleSweep:
     """The oracle's Sweep<HydrogenOnly>, built from the same inputs as subsweep_gb300.Sweep."""
 
     def __init__(self, params, grid, density, xhii, temperature, source, directions: np.ndarray,
-                 scale_factor: float = 1.0, periodic_mode: int = PERIODIC_SNAPSHOT):
+                 scale_factor: float = 1.0, periodic_mode: int = PERIODIC_SNAPSHOT, order: int = ORDER_FIFO,
+                 num_threads: int = 1):
         lib = load()
         self._lib = lib
         n = grid.num_cells
@@ -112,7 +158,7 @@ class OracleSweep:
                       timestep_safety_factor=params.timestep_safety_factor,
                       chemistry_timestep_safety_factor=params.chemistry_timestep_safety_factor,
                       prevent_cooling=int(params.prevent_cooling), scale_factor=scale_factor,
-                      periodic_mode=periodic_mode)
+                      periodic_mode=periodic_mode, order=order, num_threads=num_threads)
         g = OrcGrid(num_cells=n, row_ptr=arr(grid.row_ptr, np.int64), nbr=arr(grid.nbr, np.int32),
                     kind=arr(grid.kind, np.uint8), area=arr(grid.area, np.float64),
                     normal=arr(grid.normal.reshape(-1), np.float64), volume=arr(grid.volume, np.float64),

@@ -35,6 +35,14 @@ enum { ORC_LOCAL = 0, ORC_LOCAL_PERIODIC = 1, ORC_BOUNDARY = 2 };
  * visibility depends on the (unstable) task order; kept to measure the deviation. */
 enum { ORC_PERIODIC_SNAPSHOT = 0, ORC_PERIODIC_IMMEDIATE = 1 };
 
+/* Task order within a level sweep.  FIFO: per direction (highest first), a FIFO queue
+ * of ready tasks.  HEAP: the reference's std BinaryHeap keyed by direction only
+ * (src/sweep/mod.rs:104, task.rs:25-35), restated from the Rust standard library, fed
+ * in the reference's order (get_initial_tasks, mod.rs:388-398); with one thread and
+ * ORC_PERIODIC_IMMEDIATE this is the reference's single-rank computation, task for
+ * task. */
+enum { ORC_ORDER_FIFO = 0, ORC_ORDER_HEAP = 1 };
+
 typedef struct {
   int64_t num_cells;
   const int64_t* row_ptr; /* [num_cells+1] */
@@ -57,6 +65,11 @@ typedef struct {
   int32_t prevent_cooling;
   double scale_factor;
   int32_t periodic_mode; /* ORC_PERIODIC_* */
+  int32_t order;         /* ORC_ORDER_* */
+  /* Worker threads (<= 1: one).  A level sweep splits the directions between them
+   * (directions t, t + T, ... to worker t, each with its own queue or heap) and the
+   * chemistry the cells.  With ORC_ORDER_FIFO results do not depend on the count. */
+  int32_t num_threads;
 } orc_params;
 
 typedef struct orc_sim orc_sim;
@@ -113,6 +126,31 @@ int32_t orc_solver_perform_timestep(double* xhii, double* temperature, double de
                                     double scale_factor, int32_t has_floor, double floor_t,
                                     double floor_x, double timestep, double safety,
                                     double* timescale_out, int32_t* process_out);
+
+/* The task heap on its own: BinaryHeap::from of n_init tasks with directions
+ * init_dirs (task i gets cell id i), then ops in order: a value >= 0 pushes a task of
+ * that direction (cell ids continue from n_init), -1 pops and writes the popped cell
+ * id to out (in order).  Returns the number of ids written; -1 on a pop of an empty
+ * heap. */
+int64_t orc_heap_replay(const int64_t* init_dirs, int64_t n_init, const int64_t* ops, int64_t n_ops,
+                        int64_t* out);
+
+/* Periodic Voronoi tessellation of n generators in [0, box)^3 (voronoi_oracle.cpp),
+ * built on num_threads threads, as face-neighbour CSR with the kinds above.  NULL on
+ * invalid arguments; failed cells (none expected) and faces dropped for want of a
+ * reciprocal are counted. */
+typedef struct orc_voronoi orc_voronoi;
+orc_voronoi* orc_voronoi_build(const double* points, int64_t n, double box, int32_t num_threads);
+int64_t orc_voronoi_num_faces(const orc_voronoi* g);
+int64_t orc_voronoi_failed_cells(const orc_voronoi* g);
+int64_t orc_voronoi_dropped_faces(const orc_voronoi* g);
+void orc_voronoi_copy(const orc_voronoi* g, int64_t* row_ptr, int32_t* nbr, uint8_t* kind, double* area,
+                      double* normal, double* volume, double* size);
+void orc_voronoi_free(orc_voronoi* g);
+
+/* Directions::from_num (src/sweep/direction/mod.rs:58-75): the reference's direction
+ * table for num in {1, 16, 21, 32, 64, 84} into out[num*3]; 0 on success, -1 otherwise. */
+int32_t orc_directions_from_num(int32_t num, double* out);
 
 /* Outgoing rate of one task (hydrogen_only/mod.rs:72-88). */
 double orc_outgoing_rate(double density, double xhii, double size, double incoming_rate,

@@ -7,11 +7,17 @@
 // functions are glibc's, which is what Rust's std uses on Linux.
 #include "oracle.h"
 
+// The reference's direction tables (src/sweep/direction/healpix.rs), as the generated
+// data file the library is built with; the tests hold its digests against the reference.
+#include "../subsweep_gb300/csrc/direction_bins.inc"
+
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <thread>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -335,6 +341,121 @@ struct TimestepState {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// The reference's task queue: std::collections::BinaryHeap<Task> (src/sweep/mod.rs:104)
+// with Task ordered by direction alone (task.rs:25-35), so every task of a direction
+// compares equal.  Restated from the Rust standard library's published source
+// (library/alloc/src/collections/binary_heap/mod.rs): FromIterator collects into a
+// Vec and heapifies it (`rebuild`: sift_down from len/2 - 1 down to 0), `push` sifts
+// the new element up, `pop` swaps the last element into the root, sifts that hole down
+// to the bottom always taking the greater child (the right one on ties) and sifts it
+// back up.  Equal keys stop both sifts, which is what fixes the order of equal tasks.
+// ---------------------------------------------------------------------------
+struct Task {
+  int64_t cell;
+  int64_t dir;
+};
+
+class TaskHeap {
+ public:
+  // BinaryHeap::from(Vec): rebuild()
+  void assign(std::vector<Task>&& v) {
+    data_ = std::move(v);
+    size_t n = data_.size() / 2;
+    while (n > 0) {
+      --n;
+      sift_down_range(n, data_.size());
+    }
+  }
+  bool empty() const { return data_.empty(); }
+  size_t size() const { return data_.size(); }
+  // BinaryHeap::push: push then sift_up(0, old_len)
+  void push(Task t) {
+    data_.push_back(t);
+    sift_up(0, data_.size() - 1);
+  }
+  // BinaryHeap::pop: swap the last element into the root, sift_down_to_bottom(0)
+  Task pop() {
+    Task item = data_.back();
+    data_.pop_back();
+    if (!data_.empty()) {
+      std::swap(item, data_[0]);
+      sift_down_to_bottom(0);
+    }
+    return item;
+  }
+
+ private:
+  std::vector<Task> data_;
+
+  size_t sift_up(size_t start, size_t pos) {
+    const Task elem = data_[pos];
+    while (pos > start) {
+      size_t parent = (pos - 1) / 2;
+      if (elem.dir <= data_[parent].dir) break;
+      data_[pos] = data_[parent];
+      pos = parent;
+    }
+    data_[pos] = elem;
+    return pos;
+  }
+  size_t sift_down_range(size_t pos, size_t end) {
+    const Task elem = data_[pos];
+    size_t child = 2 * pos + 1;
+    while (child + 2 <= end) {  // child <= end.saturating_sub(2)
+      if (data_[child].dir <= data_[child + 1].dir) child += 1;
+      if (elem.dir >= data_[child].dir) {
+        data_[pos] = elem;
+        return pos;
+      }
+      data_[pos] = data_[child];
+      pos = child;
+      child = 2 * pos + 1;
+    }
+    if (child + 1 == end && elem.dir < data_[child].dir) {
+      data_[pos] = data_[child];
+      pos = child;
+    }
+    data_[pos] = elem;
+    return pos;
+  }
+  void sift_down_to_bottom(size_t pos) {
+    const size_t end = data_.size(), start = pos;
+    const Task elem = data_[pos];
+    size_t child = 2 * pos + 1;
+    while (child + 2 <= end) {
+      if (data_[child].dir <= data_[child + 1].dir) child += 1;
+      data_[pos] = data_[child];
+      pos = child;
+      child = 2 * pos + 1;
+    }
+    if (child + 1 == end) {
+      data_[pos] = data_[child];
+      pos = child;
+    }
+    data_[pos] = elem;
+    sift_up(start, pos);
+  }
+};
+
+// FIFO queue of one direction's ready tasks (the oracle's default order).
+struct FifoQueue {
+  std::deque<Task> q;
+  bool empty() const { return q.empty(); }
+  void push(Task t) { q.push_back(t); }
+  Task pop() {
+    Task t = q.front();
+    q.pop_front();
+    return t;
+  }
+};
+
+// Work counters of one worker thread.
+struct WorkCount {
+  int64_t tasks = 0, chem_cells = 0, chem_attempts = 0, chem_failures = 0;
+  bool panicked = false;
+};
+
+// ---------------------------------------------------------------------------
 // Sweep<HydrogenOnly>: src/sweep/mod.rs:171-610
 // ---------------------------------------------------------------------------
 struct orc_sim {
@@ -346,7 +467,9 @@ struct orc_sim {
   std::vector<int32_t> nbr;
   std::vector<uint8_t> kind;
   std::vector<double> area, normal, volume, size;
-  // Site (site.rs:12-23) in SoA form, per-(cell,dir) arrays [cell*D + dir]
+  // Site (site.rs:12-23) in SoA form; per-(cell, dir) arrays are direction-major,
+  // [dir * n + cell], so the threads of a level sweep (one set of directions each)
+  // write disjoint memory
   std::vector<double> density, source, xhii, temperature, species_timestep, change_timescale,
       previous_rate;
   std::vector<double> incoming, outgoing, periodic, periodic_pending;
@@ -358,30 +481,40 @@ struct orc_sim {
 
   explicit orc_sim(const orc_params* pp) : p(*pp), ts(pp->max_timestep, pp->num_timestep_levels) {}
 
+  size_t at(int64_t c, int32_t d) const { return (size_t)d * (size_t)n + (size_t)c; }
+  int threads() const { return p.num_threads > 1 ? p.num_threads : 1; }
+
   double get_rate(int64_t c, int32_t d) const {  // site.rs:53-56
     double src = source[c] / (double)D;
-    return incoming[c * D + d] + src + periodic[c * D + d];
+    return incoming[at(c, d)] + src + periodic[at(c, d)];
   }
   bool active(int64_t c, int32_t current) const { return level[c] >= current; }
 
-  // Sweep::init_counts, mod.rs:346-386
-  int64_t init_counts(int32_t current, std::vector<uint32_t>& out) const {
-    int64_t n_active = 0;
-    for (int64_t c = 0; c < n; ++c) {
-      if (!active(c, current)) continue;
-      ++n_active;
-      for (int32_t d = 0; d < D; ++d) {
-        uint32_t cnt = 0;
-        for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
-          bool upwind = dot3(&normal[3 * f], &dirs[3 * d]) < 0.0;
-          if (!upwind || kind[f] == ORC_BOUNDARY) continue;
-          if (!active(nbr[f], current)) continue;
-          if (kind[f] == ORC_LOCAL) cnt += 1;
-        }
-        out[c * D + d] = cnt;
+  // ActiveList::enumerate_active (active_list.rs:55-66): the bins of levels current..L-1
+  // in turn, each bin in index order (update_bins, 143-153)
+  std::vector<int64_t> active_in_bin_order(int32_t current) const {
+    std::vector<int64_t> order;
+    for (int32_t l = current; l < p.num_timestep_levels; ++l)
+      for (int64_t c = 0; c < n; ++c)
+        if (level[c] == l) order.push_back(c);
+    return order;
+  }
+
+  // Sweep::init_counts (mod.rs:346-386) for one direction: upwind faces whose neighbour
+  // is LOCAL and active.
+  void init_counts_dir(int32_t current, int32_t d, const std::vector<int64_t>& act,
+                       std::vector<uint32_t>& out) const {
+    const double* dir = &dirs[3 * d];
+    for (int64_t c : act) {
+      uint32_t cnt = 0;
+      for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
+        bool upwind = dot3(&normal[3 * f], dir) < 0.0;
+        if (!upwind || kind[f] == ORC_BOUNDARY) continue;
+        if (!active(nbr[f], current)) continue;
+        if (kind[f] == ORC_LOCAL) cnt += 1;
       }
+      out[at(c, d)] = cnt;
     }
-    return n_active;
   }
 
   // HydrogenOnly::get_outgoing_rate, hydrogen_only/mod.rs:72-88
@@ -394,12 +527,13 @@ struct orc_sim {
 
   // Sweep::solve_task, mod.rs:423-485 (+ get_outgoing_rate 412-421, handle_local_neighbour
   // 487-503, handle_local_periodic_neighbour 505-513).
-  void solve_task(int64_t c, int32_t d, int32_t current, std::deque<int64_t>& queue) {
-    double& inc = incoming[c * D + d];
+  template <typename Queue>
+  void solve_task(int64_t c, int32_t d, int32_t current, Queue& queue, WorkCount& work) {
+    double& inc = incoming[at(c, d)];
     if (inc < 0.0) inc = 0.0;  // Photons::make_positive, chemistry/mod.rs:61-65
     double out_new = outgoing_rate(c, get_rate(c, d));
-    double corr = out_new - outgoing[c * D + d];
-    outgoing[c * D + d] = out_new;
+    double corr = out_new - outgoing[at(c, d)];
+    outgoing[at(c, d)] = out_new;
     const double* dir = &dirs[3 * d];
     double total_effective_area = 0.0;
     for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
@@ -413,25 +547,37 @@ struct orc_sim {
       double w = corr * (effective_area / total_effective_area);
       int64_t nb = nbr[f];
       if (kind[f] == ORC_LOCAL) {
-        incoming[nb * D + d] += w;
+        incoming[at(nb, d)] += w;
         if (active(nb, current)) {
-          uint32_t& m = missing[nb * D + d];
+          uint32_t& m = missing[at(nb, d)];
           m -= 1;
-          if (m == 0) queue.push_back(nb);
+          if (m == 0) queue.push(Task{nb, d});
         }
       } else if (kind[f] == ORC_LOCAL_PERIODIC) {
         if (p.periodic_mode == ORC_PERIODIC_IMMEDIATE)
-          periodic[nb * D + d] += w;
+          periodic[at(nb, d)] += w;
         else
-          periodic_pending[nb * D + d] += w;
+          periodic_pending[at(nb, d)] += w;
       }
     }
-    ++tasks_solved;
+    ++work.tasks;
   }
 
-  // Sweep::update_chemistry, mod.rs:549-574 (+ HydrogenOnly::update_abundances 90-119)
-  void update_chemistry(int32_t current) {
-    for (int64_t c = 0; c < n; ++c) {
+  // Run `body(worker, work)` on every worker thread (worker 0 on the calling thread).
+  template <typename Body>
+  void on_threads(Body body, std::vector<WorkCount>& work) {
+    const int T = threads();
+    work.assign(T, WorkCount{});
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; ++t) pool.emplace_back([&, t] { body(t, work[t]); });
+    body(0, work[0]);
+    for (std::thread& th : pool) th.join();
+  }
+
+  // Sweep::update_chemistry, mod.rs:549-574 (+ HydrogenOnly::update_abundances 90-119),
+  // for the active cells in [begin, end)
+  void update_chemistry_range(int32_t current, int64_t begin, int64_t end, WorkCount& work) {
+    for (int64_t c = begin; c < end; ++c) {
       if (!active(c, current)) continue;
       double timestep = ts.timestep_at_level(level[c]);
       double rate = 0.0;
@@ -458,43 +604,96 @@ struct orc_sim {
       s.floor_x = xhii[c];
       bool failed = false;
       Timescale chem_ts = s.perform_timestep(timestep, p.chemistry_timestep_safety_factor, &failed,
-                                             chem_attempts);
-      if (failed) ++chem_failures;
-      if (s.clamp_panicked) panicked = true;
+                                             work.chem_attempts);
+      if (failed) ++work.chem_failures;
+      if (s.clamp_panicked) work.panicked = true;
       temperature[c] = s.temperature;
       xhii[c] = s.x;
       species_timestep[c] = chem_ts.time;
       Timescale change = rate_ts.min(chem_ts);
       change_timescale[c] = change.time;
-      ++chem_cells;
+      ++work.chem_cells;
     }
   }
 
-  // Sweep::single_sweep, mod.rs:274-289.  The BinaryHeap keyed by direction only
-  // (task.rs:25-35) pops every task of the highest direction before any lower one,
-  // since new tasks inherit the popped task's direction; within a direction the heap
-  // order is unspecified, and this restatement uses FIFO order.
-  bool single_sweep(int32_t current) {
-    int64_t n_active = init_counts(current, missing);
-    int64_t solved_before = tasks_solved;
-    for (int32_t d = D - 1; d >= 0; --d) {
-      std::deque<int64_t> queue;
+  void add_work(const std::vector<WorkCount>& work) {
+    for (const WorkCount& w : work) {
+      tasks_solved += w.tasks;
+      chem_cells += w.chem_cells;
+      chem_attempts += w.chem_attempts;
+      chem_failures += w.chem_failures;
+      panicked = panicked || w.panicked;
+    }
+  }
+
+  // Directions of worker t: t, t + T, ...
+  std::vector<int32_t> worker_dirs(int t) const {
+    std::vector<int32_t> out;
+    for (int32_t d = t; d < D; d += threads()) out.push_back(d);
+    return out;
+  }
+
+  // One worker's share of a level sweep.  ORDER_HEAP: the reference's single queue,
+  // get_initial_tasks (mod.rs:388-398: directions outer, active sites in bin order
+  // inner) collected into the BinaryHeap restated above and popped to exhaustion
+  // (solve, mod.rs:291-314; on one rank the send/receive pauses do not change the
+  // order); with one worker this is the reference's task order exactly, with several
+  // each worker runs that heap over its own directions.  ORDER_FIFO: per direction,
+  // highest first (the heap's key order), a FIFO queue seeded in index order.
+  void sweep_worker(int32_t current, int t, const std::vector<int64_t>& act, WorkCount& work) {
+    const std::vector<int32_t> mine = worker_dirs(t);
+    for (int32_t d : mine) init_counts_dir(current, d, act, missing);
+    if (p.order == ORC_ORDER_HEAP) {
+      std::vector<Task> initial;
+      for (int32_t d : mine)
+        for (int64_t c : act)
+          if (missing[at(c, d)] == 0) initial.push_back(Task{c, d});
+      TaskHeap heap;
+      heap.assign(std::move(initial));
+      while (!heap.empty()) {
+        Task task = heap.pop();
+        solve_task(task.cell, (int32_t)task.dir, current, heap, work);
+      }
+      return;
+    }
+    for (auto it = mine.rbegin(); it != mine.rend(); ++it) {
+      const int32_t d = *it;
+      FifoQueue queue;
       for (int64_t c = 0; c < n; ++c)  // get_initial_tasks, mod.rs:388-398
-        if (active(c, current) && missing[c * D + d] == 0) queue.push_back(c);
+        if (active(c, current) && missing[at(c, d)] == 0) queue.push(Task{c, d});
       while (!queue.empty()) {
-        int64_t c = queue.front();
-        queue.pop_front();
-        solve_task(c, d, current, queue);
+        Task task = queue.pop();
+        solve_task(task.cell, d, current, queue, work);
       }
     }
-    bool complete = (tasks_solved - solved_before) == n_active * (int64_t)D;
+  }
+
+  // Sweep::single_sweep, mod.rs:274-289.  Directions are independent within a level
+  // sweep (every write of a task goes to its own direction's rates), so the workers
+  // split them; the chemistry, per cell, splits the cells.
+  bool single_sweep(int32_t current) {
+    const std::vector<int64_t> act = active_in_bin_order(current);
+    const int64_t n_active = (int64_t)act.size();
+    std::vector<WorkCount> work;
+    on_threads([&](int t, WorkCount& w) { sweep_worker(current, t, act, w); }, work);
+    int64_t solved = 0;
+    for (const WorkCount& w : work) solved += w.tasks;
+    add_work(work);
+    bool complete = solved == n_active * (int64_t)D;
     if (p.periodic_mode == ORC_PERIODIC_SNAPSHOT) {
       for (size_t i = 0; i < periodic.size(); ++i) {
         periodic[i] += periodic_pending[i];
         periodic_pending[i] = 0.0;
       }
     }
-    update_chemistry(current);
+    const int T = threads();
+    on_threads(
+        [&](int t, WorkCount& w) {
+          int64_t chunk = (n + T - 1) / T;
+          update_chemistry_range(current, std::min(n, t * chunk), std::min(n, (t + 1) * chunk), w);
+        },
+        work);
+    add_work(work);
     return complete;
   }
 
@@ -580,7 +779,7 @@ void orc_sim_get_fields(const orc_sim* s, double* xhii, double* temperature, dou
     if (timestep) timestep[c] = s->species_timestep[c];
     if (rate) {  // mod.rs:727-730: sum of incoming over directions
       double r = 0.0;
-      for (int32_t d = 0; d < s->D; ++d) r += s->incoming[c * s->D + d];
+      for (int32_t d = 0; d < s->D; ++d) r += s->incoming[s->at(c, d)];
       rate[c] = r;
     }
     if (change_timescale) change_timescale[c] = s->change_timescale[c];
@@ -632,17 +831,25 @@ void orc_sim_time_series(const orc_sim* s, double* out) {
 }
 
 void orc_sim_get_rates(const orc_sim* s, double* incoming, double* outgoing, double* periodic) {
-  size_t nd = s->incoming.size();
-  if (incoming) std::memcpy(incoming, s->incoming.data(), nd * sizeof(double));
-  if (outgoing) std::memcpy(outgoing, s->outgoing.data(), nd * sizeof(double));
-  if (periodic) std::memcpy(periodic, s->periodic.data(), nd * sizeof(double));
+  const std::vector<double>* src[3] = {&s->incoming, &s->outgoing, &s->periodic};
+  double* dst[3] = {incoming, outgoing, periodic};
+  for (int k = 0; k < 3; ++k) {
+    if (!dst[k]) continue;
+    for (int64_t c = 0; c < s->n; ++c)
+      for (int32_t d = 0; d < s->D; ++d) dst[k][c * s->D + d] = (*src[k])[s->at(c, d)];
+  }
 }
 
 int64_t orc_sim_init_counts(const orc_sim* s, int32_t level, uint8_t* out) {
   std::vector<uint32_t> tmp((size_t)s->n * s->D, 0);
-  int64_t na = s->init_counts(level, tmp);
-  for (size_t i = 0; i < tmp.size(); ++i) out[i] = (uint8_t)(tmp[i] > 255 ? 255 : tmp[i]);
-  return na;
+  const std::vector<int64_t> act = s->active_in_bin_order(level);
+  for (int32_t d = 0; d < s->D; ++d) s->init_counts_dir(level, d, act, tmp);
+  for (int64_t c = 0; c < s->n; ++c)
+    for (int32_t d = 0; d < s->D; ++d) {
+      uint32_t v = tmp[s->at(c, d)];
+      out[c * s->D + d] = (uint8_t)(v > 255 ? 255 : v);
+    }
+  return (int64_t)act.size();
 }
 
 void orc_sim_level_counts(const orc_sim* s, int64_t* counts) { s->level_counts(counts); }
@@ -729,6 +936,40 @@ int32_t orc_solver_perform_timestep(double* xhii, double* temperature, double de
   if (timescale_out) *timescale_out = t.time;
   if (process_out) *process_out = t.process;
   return failed ? 1 : 0;
+}
+
+int32_t orc_directions_from_num(int32_t num, double* out) {
+  static const double one[1][3] = {{1.0, 0.0, 0.0}};
+  const double(*tab)[3] = nullptr;
+  switch (num) {  // Directions::from_num, src/sweep/direction/mod.rs:58-75
+    case 1: tab = one; break;
+    case 16: tab = kDirectionBins16; break;
+    case 21: tab = kDirectionBins21; break;
+    case 32: tab = kDirectionBins32; break;
+    case 64: tab = kDirectionBins64; break;
+    case 84: tab = kDirectionBins84; break;
+    default: return -1;
+  }
+  for (int32_t i = 0; i < 3 * num; ++i) out[i] = tab[0][i];
+  return 0;
+}
+
+int64_t orc_heap_replay(const int64_t* init_dirs, int64_t n_init, const int64_t* ops, int64_t n_ops,
+                        int64_t* out) {
+  std::vector<Task> v;
+  for (int64_t i = 0; i < n_init; ++i) v.push_back(Task{i, init_dirs[i]});
+  TaskHeap heap;
+  heap.assign(std::move(v));
+  int64_t next = n_init, written = 0;
+  for (int64_t k = 0; k < n_ops; ++k) {
+    if (ops[k] >= 0) {
+      heap.push(Task{next++, ops[k]});
+    } else {
+      if (heap.empty()) return -1;
+      out[written++] = heap.pop().cell;
+    }
+  }
+  return written;
 }
 
 double orc_outgoing_rate(double density, double xhii, double size, double incoming_rate,
