@@ -3,19 +3,21 @@
 
 A *step* is one Sweep::run_sweeps (src/sweep/mod.rs:258-272): every level sweep of the
 timestep hierarchy, the chemistry of each sweep's active cells and the level
-reassignment, over a seeded synthetic workload (default: 128^3 jittered-lattice
-Voronoi cells, lognormal density, 64 sources, 84 directions, 4 levels).  Both GPU
-arithmetics run from identical initial conditions: the FP64 drop-in and the mixed
-path (FP32 transport, FP64 chemistry); `value` is the mixed path's cell-direction
-updates per second, device-timed by CUDA events on the library's launch stream,
-and the error of x_HII / T between the two is reported with it.
+reassignment, over a seeded synthetic workload (default: 256^3 jittered-lattice
+Voronoi cells of 750 pc, density the exponential of a Gaussian random field, 1000
+sources at the density peaks, 84 directions, 4 levels).  Both GPU arithmetics run
+from identical initial conditions, one after the other: the FP64 drop-in and the
+mixed path (FP32 transport, FP64 chemistry); `value` is the mixed path's
+cell-direction updates per second, device-timed by CUDA events on the library's
+launch stream, and the error of x_HII / T between the two is reported with it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 With N > 1 (under torchrun) every rank runs an independent replica on its own GPU
 (the sweep does not shard on one node); value = all ranks' updates / slowest rank.
 `--impl reference` times the CPU restatement of the reference algorithm (oracle/) on
-the host cores instead, one process per core, on a bounded sample of the workload.
+every host core instead, over the same full workload built by the oracle alone; each
+step is a bounded sample of a level-0 sweep (a subset of the directions).
 """
 from __future__ import annotations
 
@@ -178,74 +180,88 @@ def bytes_per_task(f_dn: float, rate_bytes: int, counter_bytes: int = 1) -> floa
     return rate_bytes * (4 + 2 * f_dn) + 2 * counter_bytes * f_dn
 
 
-def build_workload(name: str, n_per_side, nthreads: int, grid_device: str = "host"):
+def build_workload(name: str, n_per_side, nthreads: int, grid_device: str = "host", thick: bool = False,
+                   voronoi=None):
     from subsweep_gb300 import workloads
-    if name == "c2":
-        return workloads.c2_lognormal(n_per_side=n_per_side or 128, nthreads=nthreads, grid_device=grid_device)
+    kw = {"nthreads": nthreads, "voronoi": voronoi}
     if name == "c1":
-        return workloads.c1_small_periodic(n_per_side=n_per_side or 32, nthreads=nthreads, grid_device=grid_device)
+        return workloads.c1_small_periodic(n_per_side=n_per_side or 32, grid_device=grid_device, **kw)
+    if name == "c2":
+        return workloads.c2_lognormal(n_per_side=n_per_side or 128, grid_device=grid_device, thick=thick, **kw)
     if name == "c4":
-        return workloads.c4_grf(n_per_side=n_per_side or 256, nthreads=nthreads, grid_device=grid_device)
+        return workloads.c4_grf(n_per_side=n_per_side or 256, grid_device=grid_device, thick=thick, **kw)
     if name == "c3":
-        return workloads.c3_batched(num_boxes=n_per_side or 256, nthreads=nthreads)
+        return workloads.c3_batched(num_boxes=n_per_side or 256, thick=thick, **kw)
     raise SystemExit(f"unknown workload {name}")
 
 
+def workload_config(w) -> dict:
+    """The `config` of both arms' lines: the workload and its inputs."""
+    return dict(w.describe(), l2="per-(cell,dir) state of %.1f GB per FP32 array > 129 MB L2; no flush needed" %
+                (w.grid.num_cells * ((w.params.num_directions() + 7) // 8 * 8) * 4 / 1e9))
+
+
 # --------------------------------------------------------------------------- CPU arm
-def _cpu_worker(args):
-    """One host core running the oracle on its own copy of the sample workload."""
-    name, n_per_side, warmup, steps, seed_offset = args
-    sys.path.insert(0, str(ROOT))
+def oracle_voronoi(threads: int):
+    """Grid builder for the CPU arm: the oracle's own Voronoi producer, wrapped in the
+    grid record the workload generators fill (a plain dataclass: no library of the
+    package is loaded)."""
     from oracle import binding
-    from subsweep_gb300.sweep import directions_from_num
-    w = sample_workload(name, n_per_side, seed_offset)
-    o = binding.OracleSweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
-                            directions_from_num(w.params.num_directions()))
+    from subsweep_gb300 import grid as gridmod
+
+    def build(points, box):
+        g = binding.voronoi(points, box, threads)
+        if g["failed_cells"] or g["dropped_faces"]:
+            raise RuntimeError(f"oracle Voronoi: {g['failed_cells']} failed cells, {g['dropped_faces']} dropped faces")
+        return gridmod.Grid(row_ptr=g["row_ptr"], nbr=g["nbr"], kind=g["kind"], area=g["area"], normal=g["normal"],
+                            volume=g["volume"], size=g["size"], position=np.asarray(points, np.float64),
+                            box_size=np.full(3, float(box)), periodic=True)
+    return build
+
+
+class OracleSample:
+    """The oracle (the reference's algorithm restated, FP64) on the host cores, over the
+    whole workload grid.  A step is a bounded sample of a level-0 sweep: the transport
+    of `k` of the D directions over every cell, in the reference's task order (its
+    BinaryHeap keyed by direction), one direction per worker thread (directions are
+    independent within a level sweep), followed by the chemistry of k/D of the cells;
+    successive steps take the next directions and cells."""
+
+    def __init__(self, w, threads: int):
+        from oracle import binding
+        self.D = w.params.num_directions()
+        self.k = max(1, min(threads, self.D))
+        self.threads = threads
+        self.n = w.grid.num_cells
+        self.o = binding.OracleSweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature,
+                                     w.source, binding.directions_from_num(self.D), order=binding.ORDER_HEAP,
+                                     num_threads=threads, partition=binding.PARTITION_DIRECTIONS)
+        self.index = 0
+
+    def step(self) -> tuple:
+        i = self.index
+        self.index += 1
+        return self.o.sample_sweep(0, i * self.k, self.k, i * (self.n * self.k // self.D))
+
+    def describe(self, steps: int) -> str:
+        return (f"the full grid ({self.n} cells); each step the level-0 transport of {self.k} of the {self.D} "
+                f"directions (rotating) over every cell in the reference's BinaryHeap task order plus the chemistry "
+                f"of {self.k}/{self.D} of the cells, {self.threads} threads (one direction each), {steps} timed steps")
+
+    def close(self):
+        self.o.close()
+
+
+def time_oracle(sample: OracleSample, warmup: int, steps: int) -> tuple:
     for _ in range(warmup):
-        o.run_sweeps()
-    t0_tasks, t0_chem = o.work()
+        sample.step()
+    tasks = chem = 0
     t0 = time.perf_counter()
     for _ in range(steps):
-        o.run_sweeps()
-    dt = time.perf_counter() - t0
-    t1_tasks, t1_chem = o.work()
-    return t1_tasks - t0_tasks, t1_chem - t0_chem, dt
-
-
-def sample_workload(name: str, n_per_side: int, seed_offset: int):
-    """A bounded CPU sample of a workload: the same generator at n_per_side^3 cells (C4
-    with its sources scaled to the sample's cells), or one C3 box."""
-    from subsweep_gb300 import workloads
-    if name == "c1":
-        return workloads.c1_small_periodic(n_per_side=n_per_side, nthreads=1)
-    if name == "c4":
-        sources = max(1, round(1000 * (n_per_side / 256) ** 3))
-        return workloads.c4_grf(n_per_side=n_per_side, seed=4 + seed_offset, num_sources=sources, nthreads=1)
-    if name == "c3":
-        return workloads.c3_batched(num_boxes=1, seed=3 + seed_offset, nthreads=1)
-    return workloads.c2_lognormal(n_per_side=n_per_side, seed=2 + seed_offset, nthreads=1)
-
-
-def sample_label(name: str, n_per_side: int) -> str:
-    if name == "c3":
-        return "one C3 box (512..64000 cells, 32 dirs, 2 levels) per process"
-    return f"{name.upper()} generator at {n_per_side}^3 cells"
-
-
-def cpu_sample(workload: str, n_per_side: int, warmup: int, steps: int, procs: int):
-    from oracle import binding
-    binding.build()
-    if procs == 1:
-        res = [_cpu_worker((workload, n_per_side, warmup, steps, 0))]
-    else:
-        import multiprocessing as mp
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(procs) as pool:
-            res = pool.map(_cpu_worker, [(workload, n_per_side, warmup, steps, i) for i in range(procs)])
-    tasks = sum(r[0] for r in res)
-    chem = sum(r[1] for r in res)
-    wall = max(r[2] for r in res)
-    return tasks, chem, wall
+        a, b = sample.step()
+        tasks += a
+        chem += b
+    return tasks, chem, time.perf_counter() - t0
 
 
 def cpu_model() -> str:
@@ -260,24 +276,31 @@ def cpu_model() -> str:
 
 
 def run_reference(args, dist: Dist):
+    """CPU arm: the reference's algorithm (the oracle restatement; the reference itself
+    cannot be built) on every host core, over the same full workload, built by the
+    oracle alone (its own Voronoi producer and direction tables)."""
     if dist.rank != 0:
         return
-    from subsweep_gb300 import workloads
-    procs = os.cpu_count() or 1
-    n_side = args.cpu_sample_side
-    tasks, chem, wall = cpu_sample(args.workload, n_side, 1, max(1, args.steps), procs)
+    from oracle import binding
+    binding.build()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    w = build_workload(args.workload, args.n_per_side, threads, thick=args.thick, voronoi=oracle_voronoi(threads))
+    sample = OracleSample(w, threads)
+    setup_s = time.perf_counter() - t0
+    tasks, chem, wall = time_oracle(sample, args.warmup, args.steps)
     value = tasks / wall
-    sample = (f"{sample_label(args.workload, n_side)}, one oracle process per host core "
-              f"({procs}), each 1 warm-up + {max(1, args.steps)} timed steps")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workloads.label(args.workload, args.n_per_side), "cpu": cpu_model()},
+        "config": dict(workload_config(w), cpu=cpu_model(), setup_s=round(setup_s, 1)),
         "chem_cells_per_s": chem / wall,
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample.describe(args.steps)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    sample.close()
     print(json.dumps(line), flush=True)
 
 
@@ -301,6 +324,83 @@ def time_precision(w, precision: str, device: int, warmup: int, steps: int, dist
     return s, d, clocks
 
 
+def precision_errors(mixed: dict, fp64: dict, lv_mixed, lv_fp64, total_source: float) -> dict:
+    """Mixed path against the FP64 drop-in after the same steps from the same inputs:
+    over every cell and over the cells the radiation reaches (photon rate above 1e-6
+    of the total source).  x_HII is compared absolutely and relative to x_HII and to
+    the neutral fraction 1 - x_HII."""
+    x_m, x_f = mixed["ionized_hydrogen_fraction"], fp64["ionized_hydrogen_fraction"]
+    t_m, t_f = mixed["temperature"], fp64["temperature"]
+    r_m, r_f = mixed["photon_rate"], fp64["photon_rate"]
+    lit = r_f > 1e-6 * total_source
+
+    def on(mask):
+        if not mask.any():
+            return None
+        dx = np.abs(x_m[mask] - x_f[mask])
+        return {
+            "cells": int(mask.sum()),
+            "max_abs_dx_HII": float(dx.max()),
+            "max_rel_dx_HII": float((dx / x_f[mask]).max()),
+            "max_rel_d_neutral": float((dx / (1.0 - x_f[mask])).max()),
+            "max_rel_dT": float((np.abs(t_m[mask] - t_f[mask]) / t_f[mask]).max()),
+            "levels_equal_fraction": float((lv_mixed[mask] == lv_fp64[mask]).mean()),
+            # FP32 rates are stored in units of 2^-96 of the total source: below 1e-20
+            # of it the comparison is against that floor
+            "max_rel_photon_rate": float((np.abs(r_m[mask] - r_f[mask]) /
+                                          np.maximum(np.abs(r_f[mask]), 1e-20 * total_source)).max()),
+        }
+    all_cells = on(np.ones_like(lit))
+    return dict(all_cells, lit_cells=on(lit), lit_fraction=float(lit.mean()))
+
+
+def radiation_field(s, w) -> dict:
+    """How far the radiation reaches: the fraction of (cell, direction) incoming rates
+    above 1e-6 of the total source per direction, of cells whose photon rate is above
+    1e-6 of the total source, and of ionized cells."""
+    total = float(w.source.sum())
+    d = w.params.num_directions()
+    inc = s.rates(which=("incoming",))["incoming"]
+    frac_cd = float((inc > 1e-6 * total / d).mean())
+    del inc
+    f = s.fields()
+    return {"cell_dir_above_1e-6_of_source": frac_cd,
+            "cells_above_1e-6_of_source": float((f["photon_rate"] > 1e-6 * total).mean()),
+            "cells_x_HII_above_0.5": float((f["ionized_hydrogen_fraction"] > 0.5).mean()),
+            "cells_x_HII_above_1e-3": float((f["ionized_hydrogen_fraction"] > 1e-3).mean())}
+
+
+def periodic_semantics(name: str, n_side: int, steps: int, device: int) -> dict:
+    """The library's periodic semantics (a correction through a periodic face becomes
+    visible in the next sweep) against the reference's (visible at once, in the order
+    its BinaryHeap pops tasks): the FP64 drop-in against the oracle in the reference's
+    literal order, on the workload's generator at n_side^3 cells."""
+    from oracle import binding
+    from subsweep_gb300 import Sweep
+    sources = {"c4": {"num_sources": max(1, round(1000 * (n_side / 256) ** 3))}}.get(name, {})
+    from subsweep_gb300 import workloads
+    make = {"c1": workloads.c1_small_periodic, "c2": workloads.c2_lognormal, "c4": workloads.c4_grf}[name]
+    w = make(n_per_side=n_side, nthreads=4, **sources)
+    args = (w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source)
+    lit = binding.OracleSweep(*args, binding.directions_from_num(w.params.num_directions()),
+                              periodic_mode=binding.PERIODIC_IMMEDIATE, order=binding.ORDER_HEAP)
+    gpu = Sweep(*args, precision="fp64", device=device)
+    for _ in range(steps):
+        lit.run_sweeps()
+        gpu.run_sweeps()
+    fl, fg = lit.fields(), gpu.fields()
+    levels_gpu = gpu.cell_state()["level"]
+    gpu.close()
+    lit.close()
+    total = float(w.source.sum())
+    return {"sample": f"{w.name}, {steps} steps",
+            "max_abs_dx_HII": float(np.abs(fg["ionized_hydrogen_fraction"] - fl["ionized_hydrogen_fraction"]).max()),
+            "max_rel_dT": float((np.abs(fg["temperature"] - fl["temperature"]) / fl["temperature"]).max()),
+            "max_rel_photon_rate": float((np.abs(fg["photon_rate"] - fl["photon_rate"]) /
+                                          np.maximum(np.abs(fl["photon_rate"]), 1e-20 * total)).max()),
+            "levels_equal_fraction": float((levels_gpu == fl["level"]).mean())}
+
+
 def run_ours(args, dist: Dist):
     from subsweep_gb300 import build as native_build
     native_build.build()
@@ -309,17 +409,20 @@ def run_ours(args, dist: Dist):
     device = dist.local
     t0 = time.perf_counter()
     # the grids of the GPU arm are built on the GPU (csrc/voronoi_gpu.cu)
-    w = build_workload(args.workload, args.n_per_side, nthreads=os.cpu_count() or 1, grid_device=f"gpu:{device}")
+    w = build_workload(args.workload, args.n_per_side, nthreads=os.cpu_count() or 1,
+                       grid_device=f"gpu:{device}", thick=args.thick)
     grid_s = time.perf_counter() - t0
     directions = directions_from_num(w.params.num_directions())
     f_dn = mean_downwind_faces(w.grid, directions)
+    total_source = float(w.source.sum())
 
-    results = {}
-    handles = {}
+    # FP64 drop-in first, alone on the device (its downwind records then fit), then the
+    # mixed path from the same inputs; fields are compared after the same steps
+    results, fields, levels = {}, {}, {}
     precisions = ("fp64", "mixed") if args.precision == "both" else (args.precision,)
+    s = None
     for precision in precisions:
         s, d, clocks = time_precision(w, precision, device, args.warmup, args.steps, dist, graphs=args.graphs)
-        handles[precision] = s
         step_s = d["step_ms"] / 1e3
         max_step_s = dist.allreduce(step_s, "max")
         tasks = dist.allreduce(float(d["tasks"]), "sum")
@@ -328,29 +431,24 @@ def run_ours(args, dist: Dist):
             "cell_dir_updates_per_s": tasks / max_step_s,
             "chem_cells_per_s": chem / max_step_s,
             "ms_per_step": 1e3 * max_step_s / args.steps,
+            "tasks_per_step": tasks / args.steps / args.gpus,
+            "transport_tasks_per_s": (d["tasks"] / (d["transport_kernel_ms"] / 1e3)
+                                      if d["transport_kernel_ms"] else None),
             "tasks": tasks, "chem_cells": chem, "d": d, "clocks": clocks,
         }
-    # error of the mixed path against the FP64 drop-in after identical steps
-    head = "mixed" if "mixed" in results else "fp64"
-    sched_levels = int(handles[head].stats()["schedule_levels"])
-    pull_variant = int(handles[head].stats()["pull_variant"])
+        fields[precision] = s.fields()
+        levels[precision] = s.cell_state()["level"]
+        if precision != precisions[-1]:
+            s.close()
+    head = precisions[-1]
+    sched_levels = int(s.stats()["schedule_levels"])
+    pull_variant = int(s.stats()["pull_variant"])
     err = None
     if len(results) == 2:
-        fm, ff = handles["mixed"].fields(), handles["fp64"].fields()
-        err = {
-            "max_abs_dx_HII": float(np.abs(fm["ionized_hydrogen_fraction"] - ff["ionized_hydrogen_fraction"]).max()),
-            "max_rel_dT": float((np.abs(fm["temperature"] - ff["temperature"]) / ff["temperature"]).max()),
-            "levels_equal_fraction": float((handles["mixed"].cell_state()["level"] ==
-                                            handles["fp64"].cell_state()["level"]).mean()),
-            # FP32 rates are stored in units of 2^-96 of the total source: rates below
-            # 1e-20 of the total luminosity are compared against that floor
-            "max_rel_photon_rate": float((np.abs(fm["photon_rate"] - ff["photon_rate"]) /
-                                          np.maximum(np.abs(ff["photon_rate"]), 1e-20 * float(w.source.sum()))).max()),
-        }
-        handles["fp64"].close()
+        err = precision_errors(fields["mixed"], fields["fp64"], levels["mixed"], levels["fp64"], total_source)
+    field = radiation_field(s, w) if dist.rank == 0 else None
 
     # end to end through the C ABI: each step = sw_step + field write-back to host memory
-    s = handles[head]
     n = w.grid.num_cells
     out = {k: np.empty(n) for k in ("ionized_hydrogen_fraction", "temperature", "timestep", "photon_rate")}
     s.fields(out)  # untimed: the caller's buffers are mapped once, then reused every step
@@ -366,47 +464,56 @@ def run_ours(args, dist: Dist):
     e2e_tasks = dist.allreduce(float(st1["tasks"] - st0["tasks"]), "sum")
     s.close()
 
-    mixed = results[head]
-    d = mixed["d"]
+    main = results[head]
+    d = main["d"]
     peaks = measured_peaks()
     b_task = bytes_per_task(f_dn, 4 if head == "mixed" else 8)
     achieved_gbs = d["tasks"] * b_task / (d["transport_kernel_ms"] / 1e3) / 1e9 if d["transport_kernel_ms"] else None
     launches = d["transport_launches"]
     traffic = (MEASURED_DRAM_BYTES_PER_TASK[head] * d["tasks"] / launches
                if head in MEASURED_DRAM_BYTES_PER_TASK and launches else None)
-    cpu = None
+    cpu = semantics = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
-        c_tasks, c_chem, c_wall = cpu_sample(args.workload, args.cpu_sample_side, 1, 1, 1)
-        cpu = {"value": c_tasks / c_wall, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_model(),
-               "sample": f"{sample_label(args.workload, args.cpu_sample_side)}, oracle, "
-                         f"1 warm-up + 1 timed step ({c_tasks} tasks, {c_wall:.1f} s)",
+        threads = os.cpu_count() or 1
+        sample = OracleSample(w, threads)
+        c_tasks, c_chem, c_wall = time_oracle(sample, 1, 1)
+        cpu = {"value": c_tasks / c_wall, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),
+               "sample": sample.describe(1) + f" ({c_tasks} tasks, {c_wall:.1f} s), after 1 warm-up step",
                "chem_cells_per_s": c_chem / c_wall}
+        sample.close()
+        if args.workload in ("c1", "c2", "c4"):
+            semantics = periodic_semantics(args.workload, 16, 4, device)
     if dist.rank != 0:
         return
+    fp64 = results.get("fp64")
     line = {
         "metric": METRIC,
-        "value": mixed["cell_dir_updates_per_s"],
+        "value": main["cell_dir_updates_per_s"],
         "unit": UNIT,
         "n_gpus": args.gpus,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": mixed["ms_per_step"],
+        "ms_per_step": main["ms_per_step"],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 transport + f64 chemistry" if head == "mixed" else "f64",
         "data": "synthetic",
-        "config": dict(w.describe(), precision=head, replicas=args.gpus, cuda_graph_steps=bool(args.graphs),
-                       l2="per-(cell,dir) state of %.1f GB per array > 129 MB L2; no flush needed" %
-                          (n * ((w.params.num_directions() + 7) // 8 * 8) * 4 / 1e9),
+        "config": dict(workload_config(w), precision=head, replicas=args.gpus, cuda_graph_steps=bool(args.graphs),
                        grid_build_s=round(grid_s, 1), grid_builder="gpu"),
-        "chem_cells_per_s": mixed["chem_cells_per_s"],
-        "chemistry": chemistry_figures(d, mixed),
-        "fp64": ({k: results["fp64"][k] for k in ("cell_dir_updates_per_s", "chem_cells_per_s", "ms_per_step")}
-                 if "fp64" in results else None),
-        "speedup_mixed_vs_fp64": (results["fp64"]["ms_per_step"] / mixed["ms_per_step"]
-                                  if len(results) == 2 else None),
+        "chem_cells_per_s": main["chem_cells_per_s"],
+        "chemistry": chemistry_figures(d, main),
+        "fp64": ({k: fp64[k] for k in ("cell_dir_updates_per_s", "chem_cells_per_s", "ms_per_step", "tasks_per_step",
+                                      "transport_tasks_per_s")} if fp64 and head != "fp64" else None),
+        "speedup_mixed_vs_fp64": ({"per_step": fp64["ms_per_step"] / main["ms_per_step"],
+                                   "per_task": main["cell_dir_updates_per_s"] / fp64["cell_dir_updates_per_s"],
+                                   "transport_kernel_per_task": (main["transport_tasks_per_s"] /
+                                                                 fp64["transport_tasks_per_s"]),
+                                   "tasks_per_step_ratio": main["tasks_per_step"] / fp64["tasks_per_step"]}
+                                  if fp64 and head != "fp64" else None),
         "error_mixed_vs_fp64": err,
+        "radiation_field": field,
+        "periodic_semantics_vs_reference_order": semantics,
         "e2e": {"value": e2e_tasks / e2e_max, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 4 * 8 * n},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -423,8 +530,8 @@ def run_ours(args, dist: Dist):
                      "geometry_bytes_per_cell": 16.0 * w.grid.num_faces / w.grid.num_cells,
                      "peak_source": peaks["source"]},
         "gpu_launches": int(d["kernel_launches"]),
-        "clocks": mixed["clocks"],
-        "clocks_fp64": results["fp64"]["clocks"] if "fp64" in results else None,
+        "clocks": main["clocks"],
+        "clocks_fp64": fp64["clocks"] if fp64 and head != "fp64" else None,
         "cpu_baseline": cpu,
         "stats": {"tasks": d["tasks"], "levelled_sweeps": d["levelled_sweeps"],
                   "transport_attempts": d["transport_attempts"],
@@ -432,9 +539,9 @@ def run_ours(args, dist: Dist):
                   "sweeps": d["level_sweeps"], "schedule_levels": sched_levels,
                   "chem_attempts": d["chem_attempts"], "transport_kernel_ms": d["transport_kernel_ms"],
                   "sweep_ms": d["sweep_ms"], "chem_ms": d["chem_ms"], "level_ms": d["level_ms"],
-                  "fp64_transport_kernel_ms": (results["fp64"]["d"]["transport_kernel_ms"]
-                                               if "fp64" in results else None),
-                  "fp64_chem_ms": results["fp64"]["d"]["chem_ms"] if "fp64" in results else None},
+                  "fp64_transport_kernel_ms": fp64["d"]["transport_kernel_ms"] if fp64 else None,
+                  "fp64_chem_ms": fp64["d"]["chem_ms"] if fp64 else None,
+                  "fp64_tasks": fp64["d"]["tasks"] if fp64 else None},
     }
     print(json.dumps(line), flush=True)
 
@@ -445,9 +552,10 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4"], default="c2")
-    ap.add_argument("--n-per-side", type=int, default=None)
-    ap.add_argument("--cpu-sample-side", type=int, default=40)
+    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4"], default="c4")
+    ap.add_argument("--n-per-side", type=int, default=None,
+                    help="cells per side (C1, C2, C4) or boxes (C3); default the configuration's")
+    ap.add_argument("--thick", action="store_true", help="C2-C4 at C1's 1 Mpc / 32 cell size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--graphs", action="store_true", help="replay each mixed-path step as one CUDA graph")
     ap.add_argument("--precision", choices=["both", "fp64", "mixed"], default="both",

@@ -20,6 +20,8 @@ PERIODIC_SNAPSHOT = 0
 PERIODIC_IMMEDIATE = 1
 ORDER_FIFO = 0
 ORDER_HEAP = 1
+PARTITION_DIRECTIONS = 0
+PARTITION_DOMAINS = 1
 
 
 class OrcGrid(ctypes.Structure):
@@ -32,7 +34,7 @@ class OrcParams(ctypes.Structure):
                 ("max_timestep", c_double), ("significant_rate_threshold", c_double),
                 ("timestep_safety_factor", c_double), ("chemistry_timestep_safety_factor", c_double),
                 ("prevent_cooling", c_int32), ("scale_factor", c_double), ("periodic_mode", c_int32),
-                ("order", c_int32), ("num_threads", c_int32)]
+                ("order", c_int32), ("num_threads", c_int32), ("partition", c_int32)]
 
 
 # names of the reference's time-series outputs (src/sweep/time_series.rs:26-48)
@@ -72,6 +74,8 @@ def load() -> ctypes.CDLL:
     lib.orc_sim_sweep_order.restype = c_int32
     lib.orc_sim_single_sweep.argtypes = [c_void_p, c_int32]
     lib.orc_sim_single_sweep.restype = c_int64
+    lib.orc_sim_sample_sweep.argtypes = [c_void_p, c_int32, c_int32, c_int32, c_int64, ctypes.POINTER(c_int64)]
+    lib.orc_sim_sample_sweep.restype = c_int64
     lib.orc_timestep_level.argtypes = [c_int32, c_double, c_double]
     lib.orc_timestep_level.restype = c_int32
     lib.orc_sweep_order_after.argtypes = [c_int32, c_int32, c_void_p, c_int32]
@@ -137,7 +141,7 @@ class OracleSweep:
 
     def __init__(self, params, grid, density, xhii, temperature, source, directions: np.ndarray,
                  scale_factor: float = 1.0, periodic_mode: int = PERIODIC_SNAPSHOT, order: int = ORDER_FIFO,
-                 num_threads: int = 1):
+                 num_threads: int = 1, partition: int = PARTITION_DIRECTIONS):
         lib = load()
         self._lib = lib
         n = grid.num_cells
@@ -158,7 +162,8 @@ class OracleSweep:
                       timestep_safety_factor=params.timestep_safety_factor,
                       chemistry_timestep_safety_factor=params.chemistry_timestep_safety_factor,
                       prevent_cooling=int(params.prevent_cooling), scale_factor=scale_factor,
-                      periodic_mode=periodic_mode, order=order, num_threads=num_threads)
+                      periodic_mode=periodic_mode, order=order, num_threads=num_threads,
+                      partition=partition)
         g = OrcGrid(num_cells=n, row_ptr=arr(grid.row_ptr, np.int64), nbr=arr(grid.nbr, np.int32),
                     kind=arr(grid.kind, np.uint8), area=arr(grid.area, np.float64),
                     normal=arr(grid.normal.reshape(-1), np.float64), volume=arr(grid.volume, np.float64),
@@ -224,3 +229,11 @@ class OracleSweep:
 
     def single_sweep(self, level: int) -> int:
         return self._lib.orc_sim_single_sweep(self._h, level)
+
+    def sample_sweep(self, level: int, dir_first: int, dir_count: int, chem_first: int) -> tuple:
+        """(tasks, chemistry updates) of a bounded sample of one level sweep."""
+        chem = c_int64()
+        tasks = self._lib.orc_sim_sample_sweep(self._h, level, dir_first, dir_count, chem_first, ctypes.byref(chem))
+        if tasks < 0:
+            raise ValueError("invalid sample")
+        return tasks, chem.value

@@ -43,6 +43,14 @@ enum { ORC_PERIODIC_SNAPSHOT = 0, ORC_PERIODIC_IMMEDIATE = 1 };
  * task. */
 enum { ORC_ORDER_FIFO = 0, ORC_ORDER_HEAP = 1 };
 
+/* How worker threads share a level sweep.  DIRECTIONS: directions t, t + T, ... to
+ * worker t, each with its own queue or heap (with ORC_ORDER_FIFO the results do not
+ * depend on the thread count).  DOMAINS: the reference's parallel scheme, one rank per
+ * thread owning a contiguous block of cell ids, with the reference's own heap per rank
+ * and batched rate-correction messages between ranks (summation order then depends on
+ * timing; for CPU timing). */
+enum { ORC_PARTITION_DIRECTIONS = 0, ORC_PARTITION_DOMAINS = 1 };
+
 typedef struct {
   int64_t num_cells;
   const int64_t* row_ptr; /* [num_cells+1] */
@@ -66,10 +74,10 @@ typedef struct {
   double scale_factor;
   int32_t periodic_mode; /* ORC_PERIODIC_* */
   int32_t order;         /* ORC_ORDER_* */
-  /* Worker threads (<= 1: one).  A level sweep splits the directions between them
-   * (directions t, t + T, ... to worker t, each with its own queue or heap) and the
-   * chemistry the cells.  With ORC_ORDER_FIFO results do not depend on the count. */
+  /* Worker threads (<= 1: one).  A level sweep's transport is shared as `partition`
+   * says; the chemistry splits the cells. */
   int32_t num_threads;
+  int32_t partition; /* ORC_PARTITION_* */
 } orc_params;
 
 typedef struct orc_sim orc_sim;
@@ -102,6 +110,13 @@ int32_t orc_sim_sweep_order(const orc_sim* s, int32_t* levels_out, int32_t cap);
 /* Run a single level sweep + chemistry at `level` (mod.rs:274-289) on the current state,
  * for bounded CPU timing samples.  Returns tasks solved. */
 int64_t orc_sim_single_sweep(orc_sim* s, int32_t level);
+/* A bounded sample of one level sweep, for CPU timing: the transport of directions
+ * dir_first .. dir_first + dir_count - 1 (mod D) over every active cell, then the
+ * chemistry of the same share of the active cells (dir_count / D of them, from the
+ * chem_first-th active cell on, wrapping).  Returns the tasks solved (-1 on invalid
+ * arguments); *chem_cells gets the chemistry updates. */
+int64_t orc_sim_sample_sweep(orc_sim* s, int32_t level, int32_t dir_first, int32_t dir_count, int64_t chem_first,
+                             int64_t* chem_cells);
 
 /* --- Known-answer-test entry points ---------------------------------------- */
 /* TimestepLevel::from_max_timestep_and_desired_timestep (timestep_level.rs:27-36). */

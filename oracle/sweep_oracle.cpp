@@ -11,11 +11,16 @@
 // data file the library is built with; the tests hold its digests against the reference.
 #include "../subsweep_gb300/csrc/direction_bins.inc"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
+#include <chrono>
 #include <deque>
+#include <memory>
+#include <mutex>
 #include <thread>
 #include <utility>
 #include <vector>
@@ -525,43 +530,32 @@ struct orc_sim {
     return incoming_rate * non_absorbed;
   }
 
-  // Sweep::solve_task, mod.rs:423-485 (+ get_outgoing_rate 412-421, handle_local_neighbour
-  // 487-503, handle_local_periodic_neighbour 505-513).
+  // handle_local_neighbour (mod.rs:487-503) and handle_local_periodic_neighbour
+  // (505-513): a rate correction arriving at (nb, d), from a task of this rank or in a
+  // message from another.
   template <typename Queue>
-  void solve_task(int64_t c, int32_t d, int32_t current, Queue& queue, WorkCount& work) {
-    double& inc = incoming[at(c, d)];
-    if (inc < 0.0) inc = 0.0;  // Photons::make_positive, chemistry/mod.rs:61-65
-    double out_new = outgoing_rate(c, get_rate(c, d));
-    double corr = out_new - outgoing[at(c, d)];
-    outgoing[at(c, d)] = out_new;
-    const double* dir = &dirs[3 * d];
-    double total_effective_area = 0.0;
-    for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
-      double dt = dot3(&normal[3 * f], dir);
-      if (dt > 0.0) total_effective_area += area[f] * dt;
+  void deliver(int64_t nb, int32_t d, double w, bool periodic_face, int32_t current, Queue& queue) {
+    if (periodic_face) {
+      if (p.periodic_mode == ORC_PERIODIC_IMMEDIATE)
+        periodic[at(nb, d)] += w;
+      else
+        periodic_pending[at(nb, d)] += w;
+      return;
     }
-    for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
-      double dt = dot3(&normal[3 * f], dir);
-      if (!(dt > 0.0)) continue;
-      double effective_area = area[f] * dt;
-      double w = corr * (effective_area / total_effective_area);
-      int64_t nb = nbr[f];
-      if (kind[f] == ORC_LOCAL) {
-        incoming[at(nb, d)] += w;
-        if (active(nb, current)) {
-          uint32_t& m = missing[at(nb, d)];
-          m -= 1;
-          if (m == 0) queue.push(Task{nb, d});
-        }
-      } else if (kind[f] == ORC_LOCAL_PERIODIC) {
-        if (p.periodic_mode == ORC_PERIODIC_IMMEDIATE)
-          periodic[at(nb, d)] += w;
-        else
-          periodic_pending[at(nb, d)] += w;
-      }
+    incoming[at(nb, d)] += w;
+    if (active(nb, current)) {
+      uint32_t& m = missing[at(nb, d)];
+      m -= 1;
+      if (m == 0) queue.push(Task{nb, d});
     }
-    ++work.tasks;
   }
+
+  // Sweep::solve_task, mod.rs:423-485 (+ get_outgoing_rate 412-421).  With `ranks`,
+  // corrections for cells another rank owns become messages to it (handle_remote_
+  // neighbour / handle_remote_periodic_neighbour, mod.rs:515-547).
+  template <typename Queue>
+  void solve_task(int64_t c, int32_t d, int32_t current, Queue& queue, WorkCount& work,
+                  struct RankCtx* ranks = nullptr);
 
   // Run `body(worker, work)` on every worker thread (worker 0 on the calling thread).
   template <typename Body>
@@ -626,22 +620,23 @@ struct orc_sim {
     }
   }
 
-  // Directions of worker t: t, t + T, ...
-  std::vector<int32_t> worker_dirs(int t) const {
+  // Directions of worker t among `dset`: dset[t], dset[t + T], ...
+  std::vector<int32_t> worker_dirs(int t, const std::vector<int32_t>& dset) const {
     std::vector<int32_t> out;
-    for (int32_t d = t; d < D; d += threads()) out.push_back(d);
+    for (size_t k = (size_t)t; k < dset.size(); k += (size_t)threads()) out.push_back(dset[k]);
     return out;
   }
 
-  // One worker's share of a level sweep.  ORDER_HEAP: the reference's single queue,
-  // get_initial_tasks (mod.rs:388-398: directions outer, active sites in bin order
-  // inner) collected into the BinaryHeap restated above and popped to exhaustion
-  // (solve, mod.rs:291-314; on one rank the send/receive pauses do not change the
-  // order); with one worker this is the reference's task order exactly, with several
-  // each worker runs that heap over its own directions.  ORDER_FIFO: per direction,
-  // highest first (the heap's key order), a FIFO queue seeded in index order.
-  void sweep_worker(int32_t current, int t, const std::vector<int64_t>& act, WorkCount& work) {
-    const std::vector<int32_t> mine = worker_dirs(t);
+  // One worker's share of a level sweep when the workers split the directions.
+  // ORDER_HEAP: the reference's queue, get_initial_tasks (mod.rs:388-398: directions
+  // outer, active sites in bin order inner) collected into the BinaryHeap restated
+  // above and popped to exhaustion (solve, mod.rs:291-314; on one rank the
+  // send/receive pauses do not change the order); with one worker this is the
+  // reference's task order exactly, with several each worker runs that heap over its
+  // own directions.  ORDER_FIFO: per direction, highest first (the heap's key order),
+  // a FIFO queue seeded in index order.
+  void sweep_worker(int32_t current, const std::vector<int32_t>& mine, const std::vector<int64_t>& act,
+                    WorkCount& work) {
     for (int32_t d : mine) init_counts_dir(current, d, act, missing);
     if (p.order == ORC_ORDER_HEAP) {
       std::vector<Task> initial;
@@ -668,33 +663,67 @@ struct orc_sim {
     }
   }
 
-  // Sweep::single_sweep, mod.rs:274-289.  Directions are independent within a level
-  // sweep (every write of a task goes to its own direction's rates), so the workers
-  // split them; the chemistry, per cell, splits the cells.
-  bool single_sweep(int32_t current) {
-    const std::vector<int64_t> act = active_in_bin_order(current);
-    const int64_t n_active = (int64_t)act.size();
-    std::vector<WorkCount> work;
-    on_threads([&](int t, WorkCount& w) { sweep_worker(current, t, act, w); }, work);
-    int64_t solved = 0;
-    for (const WorkCount& w : work) solved += w.tasks;
-    add_work(work);
-    bool complete = solved == n_active * (int64_t)D;
-    if (p.periodic_mode == ORC_PERIODIC_SNAPSHOT) {
-      for (size_t i = 0; i < periodic.size(); ++i) {
-        periodic[i] += periodic_pending[i];
-        periodic_pending[i] = 0.0;
-      }
-    }
+  void domain_rank(int32_t current, const std::vector<int32_t>& dset, const std::vector<int64_t>& act,
+                   struct Domains& dom, int rank, WorkCount& work);
+
+  // The transport of one level sweep over the directions `dset`; returns the tasks
+  // solved.  PARTITION_DIRECTIONS: each worker sweeps its own directions.
+  // PARTITION_DOMAINS: each worker is a rank owning a contiguous block of cell ids
+  // (a spatially compact domain on Morton-ordered grids) and sweeps every direction of
+  // its cells, exchanging rate corrections with the other ranks as the reference's
+  // MPI ranks do.
+  int64_t sweep_transport(int32_t current, const std::vector<int32_t>& dset, const std::vector<int64_t>& act);
+
+  // Sweep::update_chemistry over the active cells act[first .. first + count) (indices
+  // taken modulo the active count), split between the workers.
+  void chemistry(int32_t current, const std::vector<int64_t>& act, int64_t first, int64_t count) {
     const int T = threads();
+    const int64_t na = (int64_t)act.size();
+    if (na == 0 || count <= 0) return;
+    std::vector<int64_t> cells;
+    if (first == 0 && count >= na) {
+      cells = act;
+      std::sort(cells.begin(), cells.end());
+    } else {
+      for (int64_t k = 0; k < count && k < na; ++k) cells.push_back(act[(size_t)((first + k) % na)]);
+    }
+    std::vector<WorkCount> work;
     on_threads(
         [&](int t, WorkCount& w) {
-          int64_t chunk = (n + T - 1) / T;
-          update_chemistry_range(current, std::min(n, t * chunk), std::min(n, (t + 1) * chunk), w);
+          const int64_t m = (int64_t)cells.size(), chunk = (m + T - 1) / T;
+          for (int64_t k = std::min(m, t * chunk); k < std::min(m, (t + 1) * chunk); ++k)
+            update_chemistry_range(current, cells[k], cells[k] + 1, w);
         },
         work);
     add_work(work);
-    return complete;
+  }
+
+  // Snapshot semantics: the periodic contributions of the sweep's directions become
+  // visible now.
+  void merge_periodic_pending(const std::vector<int32_t>& dset) {
+    if (p.periodic_mode != ORC_PERIODIC_SNAPSHOT) return;
+    std::vector<WorkCount> work;
+    on_threads(
+        [&](int t, WorkCount&) {
+          for (size_t k = (size_t)t; k < dset.size(); k += (size_t)threads())
+            for (int64_t c = 0; c < n; ++c) {
+              const size_t i = at(c, dset[k]);
+              periodic[i] += periodic_pending[i];
+              periodic_pending[i] = 0.0;
+            }
+        },
+        work);
+  }
+
+  // Sweep::single_sweep, mod.rs:274-289.
+  bool single_sweep(int32_t current) {
+    std::vector<int32_t> all(D);
+    for (int32_t d = 0; d < D; ++d) all[d] = d;
+    const std::vector<int64_t> act = active_in_bin_order(current);
+    const int64_t solved = sweep_transport(current, all, act);
+    merge_periodic_pending(all);
+    chemistry(current, act, 0, (int64_t)act.size());
+    return solved == (int64_t)act.size() * (int64_t)D;
   }
 
   // Sweep::update_timestep_levels, mod.rs:576-589
@@ -725,6 +754,144 @@ struct orc_sim {
     return status;
   }
 };
+
+// ---------------------------------------------------------------------------
+// Domain decomposition on threads: the reference's parallel scheme (MPI ranks owning
+// spatial domains, src/sweep/mod.rs:291-314 and 515-547, communicator.rs) with one
+// thread per rank and per-rank inboxes in place of MPI messages.  Each rank counts
+// a neighbour in another domain like a local one (Remote, mod.rs:364-371), solves its
+// own tasks from its own queue, sends the corrections for other ranks' cells in
+// batches after every num_tasks_to_solve_before_send_receive tasks (default 10000,
+// parameters.rs:64-78) or when its queue runs dry, and keeps receiving until every
+// rank is done (periodic corrections carry no count, so they may arrive late).
+// ---------------------------------------------------------------------------
+struct Message {
+  int64_t cell;
+  int32_t dir;
+  int32_t periodic;
+  double w;
+};
+
+struct Domains {
+  int ranks;
+  int64_t chunk;  // cells per rank: rank r owns [r * chunk, (r + 1) * chunk)
+  std::vector<std::unique_ptr<std::mutex>> lock;
+  std::vector<std::vector<Message>> inbox;
+  std::atomic<int> done{0};
+  std::atomic<bool> stalled{false};
+  Domains(int r, int64_t n) : ranks(r), chunk((n + r - 1) / r), inbox(r) {
+    for (int k = 0; k < r; ++k) lock.emplace_back(new std::mutex());
+  }
+  int owner(int64_t c) const { return (int)(c / chunk); }
+};
+
+struct RankCtx {
+  int rank;
+  Domains* dom;
+  std::vector<std::vector<Message>> outbox;
+};
+
+template <typename Queue>
+void orc_sim::solve_task(int64_t c, int32_t d, int32_t current, Queue& queue, WorkCount& work, RankCtx* ranks) {
+  double& inc = incoming[at(c, d)];
+  if (inc < 0.0) inc = 0.0;  // Photons::make_positive, chemistry/mod.rs:61-65
+  double out_new = outgoing_rate(c, get_rate(c, d));
+  double corr = out_new - outgoing[at(c, d)];
+  outgoing[at(c, d)] = out_new;
+  const double* dir = &dirs[3 * d];
+  double total_effective_area = 0.0;
+  for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
+    double dt = dot3(&normal[3 * f], dir);
+    if (dt > 0.0) total_effective_area += area[f] * dt;
+  }
+  for (int64_t f = row_ptr[c]; f < row_ptr[c + 1]; ++f) {
+    double dt = dot3(&normal[3 * f], dir);
+    if (!(dt > 0.0)) continue;
+    double effective_area = area[f] * dt;
+    double w = corr * (effective_area / total_effective_area);
+    if (kind[f] == ORC_BOUNDARY) continue;
+    const int64_t nb = nbr[f];
+    const bool periodic_face = kind[f] == ORC_LOCAL_PERIODIC;
+    if (ranks && ranks->dom->owner(nb) != ranks->rank)
+      ranks->outbox[ranks->dom->owner(nb)].push_back(Message{nb, d, periodic_face ? 1 : 0, w});
+    else
+      deliver(nb, d, w, periodic_face, current, queue);
+  }
+  ++work.tasks;
+}
+
+void orc_sim::domain_rank(int32_t current, const std::vector<int32_t>& dset, const std::vector<int64_t>& act,
+                          Domains& dom, int rank, WorkCount& work) {
+  RankCtx ctx{rank, &dom, std::vector<std::vector<Message>>(dom.ranks)};
+  std::vector<int64_t> mine;  // this rank's active cells, in the global bin order
+  for (int64_t c : act)
+    if (dom.owner(c) == rank) mine.push_back(c);
+  for (int32_t d : dset) init_counts_dir(current, d, mine, missing);
+  std::vector<Task> initial;
+  for (int32_t d : dset)
+    for (int64_t c : mine)
+      if (missing[at(c, d)] == 0) initial.push_back(Task{c, d});
+  TaskHeap heap;
+  heap.assign(std::move(initial));
+  const int64_t total = (int64_t)mine.size() * (int64_t)dset.size();
+  const int64_t batch = 10000;
+  std::vector<Message> got;
+  auto flush = [&] {
+    for (int u = 0; u < dom.ranks; ++u) {
+      if (ctx.outbox[u].empty()) continue;
+      std::lock_guard<std::mutex> g(*dom.lock[u]);
+      dom.inbox[u].insert(dom.inbox[u].end(), ctx.outbox[u].begin(), ctx.outbox[u].end());
+      ctx.outbox[u].clear();
+    }
+  };
+  auto drain = [&] {
+    got.clear();
+    {
+      std::lock_guard<std::mutex> g(*dom.lock[rank]);
+      got.swap(dom.inbox[rank]);
+    }
+    for (const Message& m : got) deliver(m.cell, m.dir, m.w, m.periodic != 0, current, heap);
+    return !got.empty();
+  };
+  int64_t solved = 0;
+  auto idle_since = std::chrono::steady_clock::now();
+  while (solved < total && !dom.stalled.load(std::memory_order_relaxed)) {
+    if (heap.empty() && !drain()) {
+      // a dependency cycle would leave every rank waiting (the reference deadlocks)
+      if (std::chrono::steady_clock::now() - idle_since > std::chrono::seconds(120)) dom.stalled = true;
+      std::this_thread::yield();
+      continue;
+    }
+    for (int64_t k = 0; k < batch && !heap.empty(); ++k) {
+      Task task = heap.pop();
+      solve_task(task.cell, (int32_t)task.dir, current, heap, work, &ctx);
+      ++solved;
+    }
+    flush();
+    idle_since = std::chrono::steady_clock::now();
+  }
+  flush();
+  dom.done.fetch_add(1);
+  while (dom.done.load() < dom.ranks && !dom.stalled.load(std::memory_order_relaxed)) {
+    drain();
+    std::this_thread::yield();
+  }
+  drain();
+}
+
+int64_t orc_sim::sweep_transport(int32_t current, const std::vector<int32_t>& dset, const std::vector<int64_t>& act) {
+  std::vector<WorkCount> work;
+  if (p.partition == ORC_PARTITION_DOMAINS && threads() > 1) {
+    Domains dom(threads(), n);
+    on_threads([&](int t, WorkCount& w) { domain_rank(current, dset, act, dom, t, w); }, work);
+  } else {
+    on_threads([&](int t, WorkCount& w) { sweep_worker(current, worker_dirs(t, dset), act, w); }, work);
+  }
+  int64_t solved = 0;
+  for (const WorkCount& w : work) solved += w.tasks;
+  add_work(work);
+  return solved;
+}
 
 extern "C" {
 
@@ -863,6 +1030,20 @@ int32_t orc_sim_sweep_order(const orc_sim* s, int32_t* levels_out, int32_t cap) 
   std::vector<int32_t> o = s->ts.sweep_order();
   for (int32_t i = 0; i < (int32_t)o.size() && i < cap; ++i) levels_out[i] = o[i];
   return (int32_t)o.size();
+}
+
+int64_t orc_sim_sample_sweep(orc_sim* s, int32_t level, int32_t dir_first, int32_t dir_count, int64_t chem_first,
+                             int64_t* chem_cells) {
+  if (dir_count < 1 || dir_count > s->D || level < 0 || level >= s->p.num_timestep_levels) return -1;
+  std::vector<int32_t> dset;
+  for (int32_t k = 0; k < dir_count; ++k) dset.push_back(((dir_first % s->D) + s->D + k) % s->D);
+  const std::vector<int64_t> act = s->active_in_bin_order(level);
+  const int64_t solved = s->sweep_transport(level, dset, act);
+  s->merge_periodic_pending(dset);
+  const int64_t before = s->chem_cells;
+  s->chemistry(level, act, chem_first, (int64_t)act.size() * dir_count / s->D);
+  if (chem_cells) *chem_cells = s->chem_cells - before;
+  return solved;
 }
 
 int64_t orc_sim_single_sweep(orc_sim* s, int32_t level) {

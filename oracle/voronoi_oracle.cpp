@@ -103,9 +103,10 @@ struct Cell {
       P3 o{0, 0, 0};
       for (const P3& v : pts) o = add(o, v);
       o = scale(o, 1.0 / (double)pts.size());
-      P3 u = std::fabs(n.x) < 0.9 ? crossp(n, P3{1, 0, 0}) : crossp(n, P3{0, 1, 0});
+      const P3 nn = scale(n, 1.0 / std::sqrt(dotp(n, n)));
+      P3 u = std::fabs(nn.x) < 0.9 ? crossp(nn, P3{1, 0, 0}) : crossp(nn, P3{0, 1, 0});
       u = scale(u, 1.0 / std::sqrt(dotp(u, u)));
-      const P3 w = crossp(n, u);
+      const P3 w = crossp(nn, u);
       std::vector<std::pair<double, P3>> ang;
       for (const P3& v : pts) ang.push_back({std::atan2(dotp(sub(v, o), w), dotp(sub(v, o), u)), v});
       std::sort(ang.begin(), ang.end(), [](const auto& a, const auto& c) { return a.first < c.first; });

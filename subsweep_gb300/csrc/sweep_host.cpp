@@ -357,9 +357,9 @@ sw_status build_schedule(sw_handle* h) {
 }
 
 // Push path: precomputed downwind fractions of every schedule position, when they fit
-// (records within a quarter and records + slots within half of the free device
-// memory; SUBSWEEP_FP64_RECORDS=0 never builds them, =1 always tries).  Without them
-// the transport computes the geometry on the fly.
+// in the free device memory less a reserve of 1/16 of the device (at least 4 GiB) for
+// later allocations (SUBSWEEP_FP64_RECORDS=0 never builds them, =1 always tries).
+// Without them the transport computes the geometry on the fly.
 sw_status build_push_records(sw_handle* h) {
   swh::DevicePtrs& p = h->p;
   if (!h->ops->push_records || p.num_sched_levels == 0) return SW_OK;
@@ -371,7 +371,9 @@ sw_status build_push_records(sw_handle* h) {
   const size_t rec_bytes = (size_t)positions * sizeof(uint4);
   size_t free_b = 0, total_b = 0;
   SW_CUDA(h, cudaMemGetInfo(&free_b, &total_b), "memory info");
-  if (mode < 0 && rec_bytes > free_b / 4) return SW_OK;
+  const size_t reserve = std::max(total_b / 16, (size_t)4 << 30);
+  const size_t room = free_b > reserve ? free_b - reserve : 0;
+  if (mode < 0 && rec_bytes > room) return SW_OK;
   struct DeviceScratch {
     void* ptr = nullptr;
     ~DeviceScratch() {
@@ -393,7 +395,7 @@ sw_status build_push_records(sw_handle* h) {
   p.push_rec = nullptr;
   if (ce != cudaSuccess) return h->cuda_fail(ce, "downwind fraction count kernels");
   const size_t slot_bytes = (size_t)total * (sizeof(uint32_t) + sizeof(double));
-  if (mode < 0 && rec_bytes + slot_bytes > free_b / 2) return SW_OK;
+  if (mode < 0 && rec_bytes + slot_bytes > room) return SW_OK;
   uint32_t* tgt = nullptr;
   double* frac = nullptr;
   if (!h->alloc(&tgt, std::max<unsigned long long>(total, 1)) || !h->alloc(&frac, std::max<unsigned long long>(total, 1))) {

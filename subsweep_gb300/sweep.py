@@ -219,11 +219,14 @@ class Sweep:
         self._check(self._lib.sw_get_dependency_counts(self._h, level, out.ctypes.data))
         return out
 
-    def rates(self) -> dict:
+    def rates(self, which=("incoming", "outgoing", "periodic")) -> dict:
+        """Per-(cell, direction) incoming, outgoing and periodic rates in photons/s
+        ([cell][dir]); `which` names the arrays to export."""
         shape = (self.num_cells, self.num_directions)
-        inc, outg, per = np.empty(shape), np.empty(shape), np.empty(shape)
-        self._check(self._lib.sw_get_rates(self._h, inc.ctypes.data, outg.ctypes.data, per.ctypes.data))
-        return {"incoming": inc, "outgoing": outg, "periodic": per}
+        out = {k: np.empty(shape) for k in which}
+        self._check(self._lib.sw_get_rates(self._h, *(out[k].ctypes.data if k in out else None
+                                                      for k in ("incoming", "outgoing", "periodic"))))
+        return out
 
     def time_series(self) -> dict:
         """Global averages of the current state (the reference's time-series outputs,

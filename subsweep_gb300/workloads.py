@@ -74,10 +74,12 @@ class Workload:
         }
 
 
-def _voronoi(pts: np.ndarray, box: float, nthreads: int, grid_device: str) -> gridmod.Grid:
+def _voronoi(pts: np.ndarray, box: float, nthreads: int, grid_device: str, voronoi=None) -> gridmod.Grid:
     """Periodic Voronoi grid of the generators on the host (`nthreads` threads) or on
     a GPU (`grid_device="gpu"` or `"gpu:<index>"`, same topology, geometry equal to
-    rounding)."""
+    rounding); `voronoi(points, box) -> Grid`, when given, builds it instead."""
+    if voronoi is not None:
+        return voronoi(pts, box)
     if grid_device.startswith("gpu"):
         index = int(grid_device.split(":")[1]) if ":" in grid_device else 0
         return gridmod.voronoi_gpu(pts, box, periodic=True, device=index)
@@ -126,10 +128,10 @@ def _c3_label(num_boxes: int, min_cells: int, max_cells: int, num_directions: in
 
 
 def c1_small_periodic(n_per_side: int = 32, seed: int = 1, num_directions: int = 84,
-                      nthreads: int = 0, grid_device: str = "host") -> Workload:
+                      nthreads: int = 0, grid_device: str = "host", voronoi=None) -> Workload:
     box = THICK_CELL * n_per_side
     pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
-    g = _voronoi(pts, box, nthreads, grid_device)
+    g = _voronoi(pts, box, nthreads, grid_device, voronoi)
     n = g.num_cells
     src = gridmod.place_sources(g, np.array([[box / 2, box / 2, box / 2]]), np.array([5e48]))
     params = SweepParameters(directions=num_directions, num_timestep_levels=1, periodic=True,
@@ -140,11 +142,11 @@ def c1_small_periodic(n_per_side: int = 32, seed: int = 1, num_directions: int =
 
 
 def c2_lognormal(n_per_side: int = 128, seed: int = 2, num_directions: int = 84, num_levels: int = 4,
-                 nthreads: int = 0, grid_device: str = "host", thick: bool = False) -> Workload:
+                 nthreads: int = 0, grid_device: str = "host", thick: bool = False, voronoi=None) -> Workload:
     box = _cell(thick, C2_CELL) * n_per_side
     rng = np.random.default_rng(seed)
     pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
-    g = _voronoi(pts, box, nthreads, grid_device)
+    g = _voronoi(pts, box, nthreads, grid_device, voronoi)
     n = g.num_cells
     sigma = 1.0
     n_h = 1e-3 * np.exp(sigma * rng.standard_normal(n) - 0.5 * sigma * sigma)
@@ -160,11 +162,11 @@ def c2_lognormal(n_per_side: int = 128, seed: int = 2, num_directions: int = 84,
 
 
 def c3_box(rng: np.random.Generator, seed: int, min_cells: int = 512, max_cells: int = 64000,
-           nthreads: int = 0, thick: bool = False):
+           nthreads: int = 0, thick: bool = False, voronoi=None):
     """One box of the C3 batch: (grid, n_H per cell, source per cell)."""
     n = int(round(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))))
     box = _cell(thick, C3_CELL) * n ** (1.0 / 3.0)
-    g = gridmod.voronoi(gridmod.poisson_points(n, box, seed), box, periodic=True, nthreads=nthreads)
+    g = _voronoi(gridmod.poisson_points(n, box, seed), box, nthreads, "host", voronoi)
     n_h = np.full(g.num_cells, 10.0 ** rng.uniform(-4.0, -2.0))
     k = int(rng.integers(1, 5))
     src = gridmod.place_sources(g, rng.uniform(0.0, box, size=(k, 3)), 10.0 ** rng.uniform(48.0, 49.0, size=k))
@@ -173,12 +175,13 @@ def c3_box(rng: np.random.Generator, seed: int, min_cells: int = 512, max_cells:
 
 def c3_batched(num_boxes: int = 256, seed: int = 3, min_cells: int = 512, max_cells: int = 64000,
                num_directions: int = 32, num_levels: int = 2, nthreads: int = 0, boxes=None,
-               thick: bool = False) -> Workload:
+               thick: bool = False, voronoi=None) -> Workload:
     """C3: independent boxes run as one block-diagonal grid.  `boxes` may pass
     precomputed (grid, n_H, source) triples."""
     rng = np.random.default_rng(seed)
     if boxes is None:
-        boxes = [c3_box(rng, seed * 100003 + b, min_cells, max_cells, nthreads, thick) for b in range(num_boxes)]
+        boxes = [c3_box(rng, seed * 100003 + b, min_cells, max_cells, nthreads, thick, voronoi)
+                 for b in range(num_boxes)]
     g = gridmod.concatenate([b[0] for b in boxes])
     n_h = np.concatenate([b[1] for b in boxes])
     src = np.concatenate([b[2] for b in boxes])
@@ -207,10 +210,10 @@ def gaussian_random_field(m: int, ln_sigma: float, seed: int) -> np.ndarray:
 
 def c4_grf(n_per_side: int = 256, seed: int = 4, ln_sigma: float = 1.5, num_sources: int = 1000,
            num_directions: int = 84, num_levels: int = 4, nthreads: int = 0, grid_device: str = "host",
-           thick: bool = False) -> Workload:
+           thick: bool = False, voronoi=None) -> Workload:
     box = _cell(thick, C4_CELL) * n_per_side
     pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
-    g = _voronoi(pts, box, nthreads, grid_device)
+    g = _voronoi(pts, box, nthreads, grid_device, voronoi)
     n = g.num_cells
     field = gaussian_random_field(n_per_side, ln_sigma, seed)
     ijk = np.minimum((g.position / box * n_per_side).astype(np.int64), n_per_side - 1)

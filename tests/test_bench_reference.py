@@ -26,11 +26,16 @@ def test_label_of_c3_boxes():
 
 
 def test_reference_arm_json_line():
-    """One JSON line with the GPU arm's metric, unit and full-size workload, the bounded
-    sample described in cpu_baseline, and an e2e block without device copies."""
+    """One JSON line with the GPU arm's metric, unit and workload, the whole grid swept
+    in bounded samples described in cpu_baseline, and an e2e block without device
+    copies; the process maps the oracle's library and none of the package's."""
     import bench
-    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--cpu-sample-side", "6",
-                          "--steps", "3", "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    code = ("import sys, bench; sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'c2', "
+            "'--n-per-side', '8', '--steps', '3', '--warmup', '3']; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPPED', sorted({l.split()[-1].rsplit('/', 1)[-1] for l in maps.splitlines() "
+            "if 'subsweep' in l or 'oracle' in l}))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
@@ -38,9 +43,12 @@ def test_reference_arm_json_line():
     assert d["impl"] == "reference"
     assert (d["metric"], d["unit"], d["higher_is_better"]) == (bench.METRIC, bench.UNIT, True)
     assert (d["steps"], d["warmup"], d["n_gpus"]) == (3, 3, 1)
-    assert d["value"] > 0
-    assert d["config"]["workload"] == workloads.label("c2")
+    assert d["value"] > 0 and d["chem_cells_per_s"] > 0
+    assert d["config"]["workload"] == workloads.label("c2", 8)
+    assert d["config"]["cells"] == 512
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
-    assert "6^3" in cb["sample"]
+    assert "full grid (512 cells)" in cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    mapped = [l for l in out.stdout.splitlines() if l.startswith("MAPPED")][0]
+    assert "liboracle.so" in mapped and "libsubsweep" not in mapped, mapped

@@ -184,13 +184,14 @@ def test_oracle_directions_are_the_reference_tables():
         binding.directions_from_num(5)
 
 
-@pytest.mark.parametrize("kind", ["lattice", "poisson"])
-def test_oracle_voronoi_matches_host_producer(kind):
+@pytest.mark.parametrize("kind,scale", [("lattice", 1.0), ("lattice", workloads.C2_CELL), ("lattice", 1e-9),
+                                        ("poisson", 1.0), ("poisson", workloads.C3_CELL)])
+def test_oracle_voronoi_matches_host_producer(kind, scale):
     if kind == "lattice":
-        box = 12.0
+        box = 12.0 * scale
         pts = gridmod.jittered_lattice(12, box, 0.25, 9)
     else:
-        box = 10.0
+        box = 10.0 * scale
         pts = gridmod.poisson_points(1500, box, 4)
     o = binding.voronoi(pts, box, num_threads=3)
     h = gridmod.voronoi(pts, box, periodic=True, nthreads=3)
