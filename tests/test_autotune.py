@@ -21,7 +21,7 @@ CANDIDATES = {84, 93, 94}
 def test_autotuned_equals_fixed(use_graphs, monkeypatch):
     monkeypatch.delenv("SUBSWEEP_PULL_VARIANT", raising=False)
     monkeypatch.delenv("SUBSWEEP_AUTOTUNE", raising=False)
-    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2)
+    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2, thick=True)
     mk = lambda tune, graphs: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature,
                                     w.source, precision="mixed", autotune=tune, use_graphs=graphs)
     tuned, fixed = mk(True, use_graphs), mk(False, False)
@@ -50,7 +50,7 @@ def test_variant_equals_default(variant, monkeypatch):
     lockstep kernel at 4 blocks per SM, bit for bit over steps with dense and sparse
     sweeps above level 0."""
     monkeypatch.delenv("SUBSWEEP_AUTOTUNE", raising=False)
-    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2)
+    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2, thick=True)
     mk = lambda: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
                        precision="mixed", autotune=False)
     monkeypatch.setenv("SUBSWEEP_PULL_VARIANT", "94")

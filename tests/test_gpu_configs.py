@@ -1,0 +1,184 @@
+"""The benchmark configurations against the oracle, through the C ABI.
+
+* C1 at its stated size (32^3 cells, 84 directions, 10 steps of 1 Myr): FP64 drop-in
+  against the oracle run in full.
+* The C2 and C4 generators (optically thin-to-moderate cells, so the radiation field
+  crosses many cells) and a batch of C3 boxes, in both precisions.
+
+Bars.  FP64: levels, per-level cell counts, task and chemistry-update totals exact;
+x_HII, T within 1e-10 relative; every photon rate above 1e-30 of the total source
+within 1e-10 relative.  Mixed (FP32 transport, FP64 chemistry): on the cells whose
+timestep level agrees with the oracle's, x_HII within 1e-4 relative to x_HII and to
+the neutral fraction 1 - x_HII and T within 1e-4 relative; cells whose level differs
+(a level boundary or the significance threshold decided differently by the FP32
+rates) are counted and bounded separately.
+"""
+import numpy as np
+import pytest
+
+from oracle import binding
+from subsweep_gb300 import workloads
+from subsweep_gb300.sweep import Sweep
+
+from test_gpu_parity import oracle_dirs
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10
+MIXED_RTOL = 1e-4
+RATE_FLOOR = 1e-30  # of the total source
+
+
+def oracle_for(w, **kw):
+    return binding.OracleSweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
+                               oracle_dirs(w.params), num_threads=8, **kw)
+
+
+def gpu_for(w, precision):
+    return Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
+                 precision=precision)
+
+
+def assert_rates(a, b, rtol, floor, what):
+    np.testing.assert_allclose(a, b, rtol=rtol, atol=floor, err_msg=what)
+
+
+def check_fp64(gpu, orc, w):
+    fg, fo = gpu.fields(), orc.fields()
+    np.testing.assert_array_equal(gpu.cell_state()["level"], fo["level"])
+    np.testing.assert_array_equal(gpu.level_counts(), orc.level_counts())
+    np.testing.assert_allclose(fg["ionized_hydrogen_fraction"], fo["ionized_hydrogen_fraction"], rtol=FP64_RTOL)
+    np.testing.assert_allclose(1.0 - fg["ionized_hydrogen_fraction"], 1.0 - fo["ionized_hydrogen_fraction"],
+                               rtol=FP64_RTOL)
+    np.testing.assert_allclose(fg["temperature"], fo["temperature"], rtol=FP64_RTOL)
+    floor = RATE_FLOOR * float(w.source.sum())
+    assert_rates(fg["photon_rate"], fo["photon_rate"], FP64_RTOL, floor, "photon rate")
+    rg, ro = gpu.rates(), orc.rates()
+    for k in ("incoming", "outgoing", "periodic"):
+        assert_rates(rg[k], ro[k], FP64_RTOL, floor, k)
+    tasks, chem = orc.work()
+    st = gpu.stats()
+    assert (st["tasks"], st["chem_cells"]) == (tasks, chem)
+
+
+def mixed_errors(gpu, orc, total_source) -> dict:
+    fg, fo = gpu.fields(), orc.fields()
+    same = gpu.cell_state()["level"] == fo["level"]
+    xg, xo = fg["ionized_hydrogen_fraction"], fo["ionized_hydrogen_fraction"]
+    dx = np.abs(xg - xo)
+    dt = np.abs(fg["temperature"] - fo["temperature"]) / fo["temperature"]
+    return {"level_flips": int((~same).sum()), "cells": int(same.size),
+            "rel_x": float((dx / xo)[same].max()), "rel_neutral": float((dx / (1.0 - xo))[same].max()),
+            "rel_T": float(dt[same].max()), "abs_x_all": float(dx.max()), "rel_T_all": float(dt.max()),
+            "lit": float((fo["photon_rate"] > 1e-6 * total_source).mean())}
+
+
+def run(w, steps, precision):
+    gpu, orc = gpu_for(w, precision), oracle_for(w)
+    for _ in range(steps):
+        assert gpu.run_sweeps() == orc.run_sweeps()
+    return gpu, orc
+
+
+def check_mixed(gpu, orc, w, max_flip_fraction):
+    e = mixed_errors(gpu, orc, float(w.source.sum()))
+    print("mixed vs oracle:", e)
+    assert e["rel_x"] <= MIXED_RTOL and e["rel_neutral"] <= MIXED_RTOL and e["rel_T"] <= MIXED_RTOL, e
+    assert e["level_flips"] <= max_flip_fraction * e["cells"], e
+    return e
+
+
+def test_c1_full_size_fp64():
+    """C1 as stated: 32^3 cells, 84 directions, 1 level, 10 steps to 10 Myr."""
+    w = workloads.c1_small_periodic()
+    assert w.grid.num_cells == 32 ** 3 and w.steps == 10
+    gpu, orc = run(w, w.steps, "fp64")
+    check_fp64(gpu, orc, w)
+    gpu.close()
+
+
+def test_c1_full_size_mixed():
+    w = workloads.c1_small_periodic()
+    gpu, orc = run(w, w.steps, "mixed")
+    check_mixed(gpu, orc, w, 0.0)
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c2_generator(precision):
+    """C2's generator at 20^3 (200 pc cells, lognormal density, 64 sources, 84
+    directions, 4 levels): the radiation crosses many cells."""
+    w = workloads.c2_lognormal(n_per_side=20, nthreads=4)
+    gpu, orc = run(w, 6, precision)
+    fo = orc.fields()
+    assert (fo["photon_rate"] > 1e-6 * w.source.sum()).mean() > 0.5  # not a dark box
+    assert len(np.unique(fo["level"])) > 1
+    if precision == "fp64":
+        check_fp64(gpu, orc, w)
+    else:
+        check_mixed(gpu, orc, w, 0.01)
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c4_generator(precision):
+    """C4's generator at 32^3 (750 pc cells, exp of a Gaussian random field, sources at
+    the density peaks with 1e52 photons/s scaled to the cell count, 84 directions, 4
+    levels)."""
+    w = workloads.c4_grf(n_per_side=32, num_sources=4, nthreads=4)
+    gpu, orc = run(w, 5, precision)
+    fo = orc.fields()
+    assert (fo["photon_rate"] > 1e-6 * w.source.sum()).mean() > 0.5
+    if precision == "fp64":
+        check_fp64(gpu, orc, w)
+    else:
+        check_mixed(gpu, orc, w, 0.01)
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c3_batch(precision):
+    """Eight C3 boxes (Poisson Voronoi, 100 pc cells, 32 directions, 2 levels) in one
+    handle against the oracle on the same batch."""
+    rng = np.random.default_rng(31)
+    boxes = [workloads.c3_box(rng, 900 + b, min_cells=512, max_cells=6000, nthreads=4) for b in range(8)]
+    w = workloads.c3_batched(boxes=boxes)
+    gpu, orc = run(w, 4, precision)
+    if precision == "fp64":
+        check_fp64(gpu, orc, w)
+    else:
+        check_mixed(gpu, orc, w, 0.01)
+    gpu.close()
+
+
+# The library's periodic semantics against the reference's literal one (the oracle in
+# the reference's task order: its BinaryHeap and immediate periodic writes), as the
+# largest x_HII difference and relative T difference measured on each generator;
+# the bounds hold those measurements with a margin.
+SEMANTICS_CASES = {
+    "c1": (lambda: workloads.c1_small_periodic(), 10, 1e-6, 1e-6),
+    "c2": (lambda: workloads.c2_lognormal(n_per_side=16, nthreads=4), 4, 5e-2, 5e-2),
+    "c4": (lambda: workloads.c4_grf(n_per_side=24, num_sources=2, nthreads=4), 4, 5e-2, 5e-2),
+    "c3": (lambda: workloads.c3_batched(boxes=[workloads.c3_box(np.random.default_rng(5), 70 + b, 512, 4000,
+                                                                nthreads=4) for b in range(4)]), 4, 5e-2, 5e-2),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SEMANTICS_CASES))
+def test_periodic_semantics_against_reference_order(name):
+    make, steps, dx_bound, dt_bound = SEMANTICS_CASES[name]
+    w = make()
+    gpu = gpu_for(w, "fp64")
+    lit = binding.OracleSweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
+                              oracle_dirs(w.params), periodic_mode=binding.PERIODIC_IMMEDIATE,
+                              order=binding.ORDER_HEAP)
+    for _ in range(steps):
+        assert gpu.run_sweeps() == lit.run_sweeps()
+    fg, fl = gpu.fields(), lit.fields()
+    dx = float(np.abs(fg["ionized_hydrogen_fraction"] - fl["ionized_hydrogen_fraction"]).max())
+    dt = float((np.abs(fg["temperature"] - fl["temperature"]) / fl["temperature"]).max())
+    flips = int((gpu.cell_state()["level"] != fl["level"]).sum())
+    print(f"{name}: snapshot vs reference order: max |dx_HII| {dx:.3e}, max rel dT {dt:.3e}, "
+          f"level flips {flips} of {w.grid.num_cells}")
+    assert dx <= dx_bound and dt <= dt_bound
+    gpu.close()

@@ -81,7 +81,7 @@ def test_c2_small_lognormal_levels_fp64_parity(transport, records, monkeypatch):
     fractions, or computing the geometry on the fly) and the dependency-driven queue."""
     monkeypatch.setenv("SUBSWEEP_TRANSPORT", transport)
     monkeypatch.setenv("SUBSWEEP_FP64_RECORDS", records)
-    w = workloads.c2_lognormal(n_per_side=12, num_directions=84, num_levels=4, nthreads=2)
+    w = workloads.c2_lognormal(n_per_side=12, num_directions=84, num_levels=4, nthreads=2, thick=True)
     gpu, orc = run_and_compare(w, steps=6)
     # the level hierarchy must actually be exercised
     assert len(np.unique(orc.fields()["level"])) > 1
@@ -167,7 +167,7 @@ def test_mixed_compaction_and_in_kernel_stamping_agree(monkeypatch):
     """Sweeps above level 0 either compact the active positions (stamping the inactive
     tasks' words in the compaction) or stamp them in the sweep kernel.  The two paths
     compute the same sums in the same order: fields and every rate agree bit for bit."""
-    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2)
+    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2, thick=True)
     out = {}
     for mode in ("always", "never"):
         monkeypatch.setenv("SUBSWEEP_COMPACT", mode)

@@ -23,7 +23,7 @@ def make(w, use_graphs):
 @pytest.mark.parametrize("name", ["c2", "c3"])
 def test_graph_steps_equal_direct_steps(name):
     if name == "c2":
-        w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2)
+        w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2, thick=True)
     else:
         rng = np.random.default_rng(5)
         boxes = [workloads.c3_box(rng, 40 + b, min_cells=200, max_cells=1500, nthreads=2) for b in range(4)]

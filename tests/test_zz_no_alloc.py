@@ -27,7 +27,7 @@ def _noalloc_counts(sweep: Sweep, level: int) -> np.ndarray:
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_noalloc_counts_match_allocating_entry_point(precision):
-    w = workloads.c2_lognormal(n_per_side=10, num_directions=84, num_levels=4, nthreads=2)
+    w = workloads.c2_lognormal(n_per_side=10, num_directions=84, num_levels=4, nthreads=2, thick=True)
     s = Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
               precision=precision)
     for _ in range(3):  # spread the cells over several timestep levels
