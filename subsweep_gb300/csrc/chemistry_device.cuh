@@ -16,9 +16,10 @@
 // smaller of x and y is the accurate one and the other is re-derived from it.
 //
 // Work per try_timestep_update attempt (counted by ncu on a level-0 launch of C2 64^3,
-// about one attempt per cell, mixed path): 366 DFMA, 63 DADD and 156 DMUL thread
-// instructions, 951 FP64 flops (the reference's expressions, as on the FP64 path:
-// 535 / 128 / 169, 1367 flops); the kernel keeps the FP64 pipe 78 % busy.
+// about one attempt per cell): the FP64 path (the reference's expressions) 535 DFMA, 128
+// DADD and 169 DMUL thread instructions, 1367 FP64 flops.  The mixed path shares the
+// fits' powers and exponentials and evaluates the transcendental factors in FP32
+// (before that: 366 / 63 / 156, 951 FP64 flops with the FP64 pipe 78 % busy).
 #pragma once
 
 #include <cfloat>
@@ -60,6 +61,23 @@ __device__ __forceinline__ Timescale ts_min(Timescale a, Timescale b) {
   return a.time < b.time ? a : b;
 }
 
+// Mixed path: the transcendental factors of the rate fits evaluated in FP32 (the fits
+// are empirical to a few per cent; FP32 carries them to ~1e-6 relative, the rounding of
+// the argument included), returned as FP64; every other operation of the solve, and
+// its state, stays FP64.  rcp / rsqrt: an FP32 estimate refined by one FP64 Newton step
+// (relative error ~1e-14).
+__device__ __forceinline__ double exp_f32(double a) { return (double)expf((float)a); }
+__device__ __forceinline__ double log_f32(double a) { return (double)logf((float)a); }
+__device__ __forceinline__ double log1p_f32(double a) { return (double)log1pf((float)a); }
+__device__ __forceinline__ double rcp_refined(double a) {
+  const double r = (double)__frcp_rn((float)a);
+  return r * fma(-a, r, 2.0);
+}
+__device__ __forceinline__ double rsqrt_refined(double a) {
+  const double r = (double)rsqrtf((float)a);
+  return r * fma(-0.5 * a * r, r, 1.5);
+}
+
 template <bool kCarryNeutral>
 struct ChemSolver {
   double x;   // ionized hydrogen fraction
@@ -92,24 +110,24 @@ struct ChemSolver {
 
   // Mixed path (kCarryNeutral): the same fits with one reciprocal of T, rsqrt for both
   // square roots and exp / log1p for the powers ((1 + q)^-c = exp(-c log1p(q)) gives the
-  // reciprocal power directly), FP64 throughout.  Each value agrees with the reference's
-  // expression to a few ulps; the FP64 drop-in keeps the reference's expressions.
+  // reciprocal power directly), the transcendental factors in FP32 (exp_f32 above), the
+  // rest FP64.  The FP64 drop-in keeps the reference's expressions.
   struct TFits {
     double inv_t, rsq, sq, s5, inv_s5, inv_1s5;
   };
   __device__ static TFits t_fits(double t) {
     TFits f;
-    f.inv_t = 1.0 / t;
-    f.rsq = rsqrt(t);
+    f.inv_t = rcp_refined(t);
+    f.rsq = rsqrt_refined(t);
     f.sq = t * f.rsq;                         // sqrt(t)
     f.s5 = f.sq * 0.003162277660168379;       // sqrt(t / 1e5)
     f.inv_s5 = f.rsq * 316.22776601683796;    // 1 / sqrt(t / 1e5)
-    f.inv_1s5 = 1.0 / (1.0 + f.s5);
+    f.inv_1s5 = rcp_refined(1.0 + f.s5);
     return f;
   }
   __device__ static void collision_fits_fast(double t, const TFits& g, double& fit, double& fitd) {
     const double c1 = 1.0 / 1e5, c2 = 157809.1;
-    const double e = exp(-c2 * g.inv_t);
+    const double e = exp_f32(-c2 * g.inv_t);
     fit = g.sq * g.inv_1s5 * e;
     fitd = (e * (c1 * c2 * t + 0.5 * g.s5 * (2.0 * c2 + t))) * (g.inv_t * g.rsq) * g.inv_s5 *
            (g.inv_1s5 * g.inv_1s5);
@@ -123,17 +141,17 @@ struct ChemSolver {
     const TFits g = t_fits(t);
     double fit, fitd;
     collision_fits_fast(t, g, fit, fitd);
-    const double e_exc = exp(-118348.0 * g.inv_t);
+    const double e_exc = exp_f32(-118348.0 * g.inv_t);
     const double exc = (7.5e-19 * g.inv_1s5 * e_exc) * Units::kErgsCentimetersCubedPerS;
     const double c3 = 1.0 / 1e5, c2e = 118348.0;
     const double dexc = ((7.5e-19 * e_exc * (c2e * c3 * t - 0.5 * c3 * (t * t) + c2e * g.s5)) *
                          (g.inv_t * g.inv_t) * g.inv_s5 * (g.inv_1s5 * g.inv_1s5)) *
                         Units::kErgsCentimetersCubedPerS;
     const double lambda = 315614.0 * g.inv_t;
-    const double ln_lambda = log(lambda);
-    const double l197 = exp(1.97 * ln_lambda);
-    const double q = exp(0.376 * (ln_lambda - 0.8109302162163288));  // ln 2.25
-    const double inv_a = exp(-3.72 * log1p(q));                      // (1 + q)^-3.72
+    const double ln_lambda = log_f32(lambda);
+    const double l197 = exp_f32(1.97 * ln_lambda);
+    const double q = exp_f32(0.376 * (ln_lambda - 0.8109302162163288));  // ln 2.25
+    const double inv_a = exp_f32(-3.72 * log1p_f32(q));                  // (1 + q)^-3.72
     const double recomb_rate = (3.435e-30 * t * l197 * inv_a) * Units::kErgsCentimetersCubedPerS;
     const double c2r = 1.97, c3r = 0.376, c4r = 3.72;
     const double drecomb_rate = (3.435e-30 * ((inv_a / (1.0 + q)) *
@@ -201,8 +219,12 @@ struct ChemSolver {
   }
 
   // 312-319: photons absorbed per photon arriving, 1 - exp(-n_HI sigma size); both
-  // updates of an attempt use it with the x of the attempt's start
-  __device__ double absorbed_fraction() const { return 1.0 - exp(-n_neutral() * Units::kSigma * length); }
+  // updates of an attempt use it with the x of the attempt's start.  Mixed path:
+  // -expm1 in FP32, accurate to ~1e-7 relative also for optically thin cells.
+  __device__ double absorbed_fraction() const {
+    if (kCarryNeutral) return -(double)expm1f((float)(-n_neutral() * Units::kSigma * length));
+    return 1.0 - exp(-n_neutral() * Units::kSigma * length);
+  }
 
   // 304-310 (+ photoheating_rate 321-325)
   __device__ double temperature_change(double timestep, double absorbed) const {
@@ -233,8 +255,8 @@ struct ChemSolver {
       const double lambda = 315614.0 * g.inv_t;
       const double dlambda_dt = -lambda * g.inv_t;
       const double sl = 561.7953363992976 * g.rsq;                            // sqrt(lambda)
-      const double p = exp(0.407 * (log(lambda) - 1.007957920399979));         // (lambda / 2.74)^0.407
-      const double inv_b = exp(-2.242 * log1p(p));                             // (1 + p)^-2.242
+      const double p = exp_f32(0.407 * (log_f32(lambda) - 1.007957920399979));  // (lambda / 2.74)^0.407
+      const double inv_b = exp_f32(-2.242 * log1p_f32(p));                      // (1 + p)^-2.242
       alpha = (2.753e-14 * (lambda * sl) * inv_b) * Units::kCentimetersCubedPerS;
       const double da = -sl * (inv_b / (p + 1.0)) * (c2a * c3a * p - 1.5 * p - 1.5);
       dalpha = ((2.753e-14 * da) * Units::kCentimetersCubedPerS) * dlambda_dt;

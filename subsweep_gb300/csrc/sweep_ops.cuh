@@ -272,8 +272,10 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 }
 
 // Variants of the pull kernel: warp-lockstep blocks of four positions (90 + target
-// blocks per SM), their nested-loop form (80 + blocks per SM) and the level-synchronous
-// wavefronts (72: registers, 78: TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
+// blocks per SM), their nested-loop form (80 + blocks per SM), the nested-loop form
+// with its shape as parameters (100 * prefetch depth + 10 * lanes per task (4, 8, or 6
+// for 16) + blocks per SM: 184 is 84's shape) and the level-synchronous wavefronts
+// (72: registers, 78: TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
 
 const void* pull_kernel(int variant) {
   switch (variant) {
@@ -282,6 +284,12 @@ const void* pull_kernel(int variant) {
     case 95: return (const void*)swk::k_sweep_pull_lock<5>;
     case 83: return (const void*)swk::k_sweep_pull_lock2<3>;
     case 84: return (const void*)swk::k_sweep_pull_lock2<4>;
+    case 143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1>;
+    case 164: return (const void*)swk::k_sweep_pull_lockg<4, 16, 1>;
+    case 184: return (const void*)swk::k_sweep_pull_lockg<4, 8, 1>;
+    case 242: return (const void*)swk::k_sweep_pull_lockg<2, 4, 2>;
+    case 264: return (const void*)swk::k_sweep_pull_lockg<4, 16, 2>;
+    case 283: return (const void*)swk::k_sweep_pull_lockg<3, 8, 2>;
     case 72: return (const void*)swk::k_sweep_pull_wave<2>;
     case 78: return (const void*)swk::k_sweep_pull_staged;
     default: return nullptr;

@@ -43,14 +43,27 @@ def test_autotuned_equals_fixed(use_graphs, monkeypatch):
     fixed.close()
 
 
-@pytest.mark.parametrize("variant", [93, 95, 84, 72, 78])
-def test_variant_equals_default(variant, monkeypatch):
+def _poisson_boxes():
+    """Poisson Voronoi boxes: cells with more than 16 upwind faces occur, so the slots
+    beyond the registers are exercised."""
+    rng = np.random.default_rng(17)
+    return workloads.c3_batched(boxes=[workloads.c3_box(rng, 50 + b, 1500, 3000, nthreads=2) for b in range(2)],
+                                num_directions=32, num_levels=3)
+
+
+@pytest.mark.parametrize("variant", [93, 95, 84, 72, 78, 143, 164, 184, 242, 264, 283])
+@pytest.mark.parametrize("grid", ["lattice", "poisson"])
+def test_variant_equals_default(variant, grid, monkeypatch):
     """Each transport variant (lockstep at 3 and 5 blocks per SM, the nested-loop
-    lockstep, the level-synchronous wavefront, its fully TMA-staged form) against the
-    lockstep kernel at 4 blocks per SM, bit for bit over steps with dense and sparse
+    lockstep, the level-synchronous wavefront, its fully TMA-staged form, the
+    nested-loop form at 4, 8 and 16 lanes per task and prefetch depths 1 and 2) against
+    the lockstep kernel at 4 blocks per SM, bit for bit over steps with dense and sparse
     sweeps above level 0."""
     monkeypatch.delenv("SUBSWEEP_AUTOTUNE", raising=False)
-    w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2, thick=True)
+    if grid == "lattice":
+        w = workloads.c2_lognormal(n_per_side=12, num_directions=32, num_levels=4, nthreads=2, thick=True)
+    else:
+        w = _poisson_boxes()
     mk = lambda: Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
                        precision="mixed", autotune=False)
     monkeypatch.setenv("SUBSWEEP_PULL_VARIANT", "94")

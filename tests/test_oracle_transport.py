@@ -5,6 +5,7 @@ agreement."""
 import math
 
 import numpy as np
+import pytest
 
 from oracle import binding
 from subsweep_gb300 import workloads, grid as gridmod
@@ -50,21 +51,30 @@ def test_flux_conservation_periodic_voronoi():
     assert (rhs > 0).all()
 
 
-def test_periodic_snapshot_vs_immediate_deviation_is_bounded():
-    """The reference makes periodic contributions visible in task order (unstable heap);
-    the snapshot semantics defer them to the next sweep.  After a few steps both agree
-    closely on this small box (the deviation is reported, not pinned)."""
-    w = workloads.c1_small_periodic(n_per_side=6, num_directions=16, nthreads=1)
-    dirs = __import__("subsweep_gb300").directions_from_num(16)
+@pytest.mark.parametrize("name,dx_bound,dt_bound", [("c1", 0.0, 0.0), ("c2", 1e-6, 0.2)])
+def test_periodic_snapshot_vs_reference_order(name, dx_bound, dt_bound):
+    """The reference makes a correction through a periodic face visible at once, so
+    whether its target reads it in the same sweep depends on the task order of its
+    BinaryHeap; the snapshot semantics defer every such correction to the next sweep.
+    Measured after three steps against the oracle in the reference's literal order:
+    identical on a C1 box (optically thick cells: nothing crosses the periodic faces),
+    max |dx_HII| 4.7e-7 and relative T 0.089 on an 8^3 C2 box of thin cells."""
+    if name == "c1":
+        w = workloads.c1_small_periodic(n_per_side=6, num_directions=16, nthreads=1)
+    else:
+        w = workloads.c2_lognormal(n_per_side=8, num_directions=16, num_levels=3, nthreads=1)
+    dirs = binding.directions_from_num(16)
     outs = []
-    for mode in (binding.PERIODIC_SNAPSHOT, binding.PERIODIC_IMMEDIATE):
+    for kw in ({"periodic_mode": binding.PERIODIC_SNAPSHOT},
+               {"periodic_mode": binding.PERIODIC_IMMEDIATE, "order": binding.ORDER_HEAP}):
         o = binding.OracleSweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature,
-                                w.source, dirs, periodic_mode=mode)
+                                w.source, dirs, **kw)
         for _ in range(3):
             o.run_sweeps()
         outs.append(o.fields())
     dx = np.abs(outs[0]["ionized_hydrogen_fraction"] - outs[1]["ionized_hydrogen_fraction"]).max()
-    assert dx < 0.05
+    dt = (np.abs(outs[0]["temperature"] - outs[1]["temperature"]) / outs[1]["temperature"]).max()
+    assert dx <= dx_bound and dt <= dt_bound, (dx, dt)
 
 
 def pull_form_incoming(g, dirs, outgoing):
