@@ -73,8 +73,9 @@ typedef struct {
                                   time is still recorded, the sweep / chemistry split is not.
                                   Default 0. */
   int32_t autotune;            /* mixed path: the first dense sweeps (each step opens with one)
-                                  try each transport kernel variant (loop form, resident blocks
-                                  per SM; three candidates, so tuning ends within three steps)
+                                  try each transport kernel variant (lanes per task, prefetch
+                                  depth, resident blocks per SM; three candidates, so tuning
+                                  ends within three steps)
                                   and keep the fastest per task; every variant computes
                                   identical results.  Default 1. */
 } sw_params;

@@ -12,6 +12,7 @@
 #include "sweep_pull.cuh"
 #include "sweep_pull_setup.cuh"
 #include "sweep_pull_lockstep.cuh"
+#include "sweep_pull_lane.cuh"
 #include "sweep_pull_wavefront.cuh"
 #include "sweep_pull_fold.cuh"
 #else
@@ -274,8 +275,9 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 // Variants of the pull kernel: warp-lockstep blocks of four positions (90 + target
 // blocks per SM), their nested-loop form (80 + blocks per SM), the nested-loop form
 // with its shape as parameters (100 * prefetch depth + 10 * lanes per task (4, 8, or 6
-// for 16) + blocks per SM: 184 is 84's shape) and the level-synchronous wavefronts
-// (72: registers, 78: TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
+// for 16) + blocks per SM: 184 is 84's shape), one lane per task with its own cursor
+// (110 + blocks per SM) and the level-synchronous wavefronts (72: registers, 78:
+// TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
 
 const void* pull_kernel(int variant) {
   switch (variant) {
@@ -284,6 +286,8 @@ const void* pull_kernel(int variant) {
     case 95: return (const void*)swk::k_sweep_pull_lock<5>;
     case 83: return (const void*)swk::k_sweep_pull_lock2<3>;
     case 84: return (const void*)swk::k_sweep_pull_lock2<4>;
+    case 112: return (const void*)swk::k_sweep_pull_lane<2>;
+    case 113: return (const void*)swk::k_sweep_pull_lane<3>;
     case 143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1>;
     case 164: return (const void*)swk::k_sweep_pull_lockg<4, 16, 1>;
     case 184: return (const void*)swk::k_sweep_pull_lockg<4, 8, 1>;
@@ -308,13 +312,16 @@ int pull_variant(const DevicePtrs* p = nullptr) {
   return pull_kernel(v) ? v : kDefaultPullVariant;
 }
 
-// candidates of the autotuner: the nested-loop lockstep form at 4 target blocks per SM
-// and the lockstep blocks of four positions at 3 and 4 (measured on C2 128^3: the
-// nested-loop form at 5 or 6 blocks and the lockstep at 5 or 6 keep too many warps ahead
-// of the dependency front and retry up to twice per task; the independent-cursor
-// variants measured slower everywhere).  Only dense sweeps are trials and a step may
-// offer a single one (its first), so three candidates finish within three steps.
-constexpr int kTuneVariants[] = {84, 93, 94};
+// candidates of the autotuner: the nested-loop lockstep form with 8 lanes per task at 4
+// target blocks per SM, with 4 lanes per task at 3, and with 4 lanes per task and the
+// slots prefetched two blocks ahead at 2.  Measured on the C4 generator at 128^3
+// (transport G tasks/s over whole steps): 84 10.6, 143 11.0, 242 10.9, 184 10.2, the
+// lockstep blocks 93 9.1, prefetch depth 2 with 8 lanes 283 8.6, 16 lanes per task 164
+// 5.9 and 264 6.4 (on C2 128^3 the forms at 5 or 6 blocks per SM kept too many warps
+// ahead of the dependency front and retried up to twice per task).  Only dense sweeps
+// are trials and a step may offer a single one (its first), so three candidates finish
+// within three steps.
+constexpr int kTuneVariants[] = {84, 143, 242};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM

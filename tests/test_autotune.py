@@ -1,8 +1,8 @@
 """Autotuning of the mixed path's transport kernel.
 
 The first dense sweeps of a handle try each candidate variant (the nested-loop lockstep
-form at 4 target blocks per SM, lockstep blocks of four positions at 3 and 4) and
-keep the fastest per task.  Every variant sums in the same order, so a tuned
+form with 8 lanes per task at 4 target blocks per SM, with 4 lanes per task at 3, and
+with 4 lanes per task and a two-block prefetch at 2) and keep the fastest per task.  Every variant sums in the same order, so a tuned
 handle, with or without graph replay after tuning, matches a handle fixed on the
 default variant bit for bit.
 """
@@ -14,7 +14,7 @@ from subsweep_gb300.sweep import Sweep
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = {84, 93, 94}
+CANDIDATES = {84, 143, 242}
 
 
 @pytest.mark.parametrize("use_graphs", [False, True])
@@ -51,12 +51,13 @@ def _poisson_boxes():
                                 num_directions=32, num_levels=3)
 
 
-@pytest.mark.parametrize("variant", [93, 95, 84, 72, 78, 143, 164, 184, 242, 264, 283])
+@pytest.mark.parametrize("variant", [93, 95, 84, 72, 78, 143, 164, 184, 242, 264, 283, 112, 113])
 @pytest.mark.parametrize("grid", ["lattice", "poisson"])
 def test_variant_equals_default(variant, grid, monkeypatch):
     """Each transport variant (lockstep at 3 and 5 blocks per SM, the nested-loop
     lockstep, the level-synchronous wavefront, its fully TMA-staged form, the
-    nested-loop form at 4, 8 and 16 lanes per task and prefetch depths 1 and 2) against
+    nested-loop form at 4, 8 and 16 lanes per task and prefetch depths 1 and 2, one
+    lane per task with its own cursor at 2 and 3 blocks per SM) against
     the lockstep kernel at 4 blocks per SM, bit for bit over steps with dense and sparse
     sweeps above level 0."""
     monkeypatch.delenv("SUBSWEEP_AUTOTUNE", raising=False)
