@@ -357,12 +357,20 @@ def precision_errors(mixed: dict, fp64: dict, lv_mixed, lv_fp64, total_source: f
         if not mask.any():
             return None
         dx = np.abs(x_m[mask] - x_f[mask])
+        rel_t = np.abs(t_m[mask] - t_f[mask]) / t_f[mask]
+        rel_x, rel_n = dx / x_f[mask], dx / (1.0 - x_f[mask])
         return {
             "cells": int(mask.sum()),
             "max_abs_dx_HII": float(dx.max()),
-            "max_rel_dx_HII": float((dx / x_f[mask]).max()),
-            "max_rel_d_neutral": float((dx / (1.0 - x_f[mask])).max()),
-            "max_rel_dT": float((np.abs(t_m[mask] - t_f[mask]) / t_f[mask]).max()),
+            "max_rel_dx_HII": float(rel_x.max()),
+            "max_rel_d_neutral": float(rel_n.max()),
+            "max_rel_dT": float(rel_t.max()),
+            # how many cells exceed 1e-4, and the error that all but 1e-5 of the cells meet
+            "cells_above_1e-4": {"abs_dx_HII": int((dx > 1e-4).sum()), "rel_dx_HII": int((rel_x > 1e-4).sum()),
+                                 "rel_d_neutral": int((rel_n > 1e-4).sum()), "rel_dT": int((rel_t > 1e-4).sum())},
+            "quantile_1e-5": {"rel_dx_HII": float(np.quantile(rel_x, 1 - 1e-5)),
+                              "rel_d_neutral": float(np.quantile(rel_n, 1 - 1e-5)),
+                              "rel_dT": float(np.quantile(rel_t, 1 - 1e-5))},
             "levels_equal_fraction": float((lv_mixed[mask] == lv_fp64[mask]).mean()),
             # FP32 rates are stored in units of 2^-96 of the total source: below 1e-20
             # of it the comparison is against that floor
@@ -370,7 +378,10 @@ def precision_errors(mixed: dict, fp64: dict, lv_mixed, lv_fp64, total_source: f
                                           np.maximum(np.abs(r_f[mask]), 1e-20 * total_source)).max()),
         }
     all_cells = on(np.ones_like(lit))
-    return dict(all_cells, lit_cells=on(lit), lit_fraction=float(lit.mean()))
+    worst = int(np.argmax(np.abs(t_m - t_f) / t_f))
+    return dict(all_cells, lit_cells=on(lit), lit_fraction=float(lit.mean()),
+                worst_T_cell={"x_HII": float(x_f[worst]), "T": float(t_f[worst]), "T_mixed": float(t_m[worst]),
+                              "level": int(lv_fp64[worst]), "photon_rate_rel": float(r_f[worst] / total_source)})
 
 
 def radiation_field(s, w) -> dict:
