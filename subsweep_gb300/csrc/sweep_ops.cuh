@@ -274,8 +274,8 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 
 // Variants of the pull kernel: warp-lockstep blocks of four positions (90 + target
 // blocks per SM), their nested-loop form (80 + blocks per SM), the nested-loop form
-// with its shape as parameters (100 * prefetch depth + 10 * lanes per task (4, 8, or 6
-// for 16) + blocks per SM: 184 is 84's shape), one lane per task with its own cursor
+// with its shape as parameters (100 * prefetch depth (3: the next slots into L1 only) +
+// 10 * lanes per task (4, 8, or 6 for 16) + blocks per SM: 184 is 84's shape), one lane per task with its own cursor
 // (110 + blocks per SM) and the level-synchronous wavefronts (72: registers, 78:
 // TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
 
@@ -294,6 +294,10 @@ const void* pull_kernel(int variant) {
     case 242: return (const void*)swk::k_sweep_pull_lockg<2, 4, 2>;
     case 264: return (const void*)swk::k_sweep_pull_lockg<4, 16, 2>;
     case 283: return (const void*)swk::k_sweep_pull_lockg<3, 8, 2>;
+    case 343: return (const void*)swk::k_sweep_pull_lockg<3, 4, 3>;
+    case 344: return (const void*)swk::k_sweep_pull_lockg<4, 4, 3>;
+    case 384: return (const void*)swk::k_sweep_pull_lockg<4, 8, 3>;
+    case 144: return (const void*)swk::k_sweep_pull_lockg<4, 4, 1>;
     case 72: return (const void*)swk::k_sweep_pull_wave<2>;
     case 78: return (const void*)swk::k_sweep_pull_staged;
     default: return nullptr;

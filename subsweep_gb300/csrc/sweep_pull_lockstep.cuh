@@ -361,7 +361,7 @@ namespace swk {
 // The nested-loop lockstep kernel with its shape as template parameters, for the
 // autotuner: G lanes per task (4, 8 or 16: 8, 4 or 2 tasks per warp block) and the
 // prefetch depth PF of the slots and cell data (1: the next block's, 2: also the one
-// after).  Whatever the shape, the incoming rate is summed in one fixed order, so every
+// after; 3: the next block's cell data, its slots only into L1).  Whatever the shape, the incoming rate is summed in one fixed order, so every
 // shape gives the same bits: eight partial sums, partial j over the slots j, j + 8 (and
 // j + 16, j + 24, ... for tasks with more than 16 upwind faces) by fused multiply-adds
 // in slot order, then combined pairwise as an eight-lane butterfly (xor 1, 2, 4).  With
@@ -370,7 +370,7 @@ namespace swk {
 template <int kMinBlocks, int G, int PF>
 __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(PullArgs a) {
   static_assert(G == 4 || G == 8 || G == 16, "4, 8 or 16 lanes per task");
-  static_assert(PF == 1 || PF == 2, "prefetch depth 1 or 2");
+  static_assert(PF == 1 || PF == 2 || PF == 3, "prefetch depth 1 or 2, or 3: next slots into L1 only");
   static_assert(kPullGroup == 8 && kPullRounds == 2, "eight partial sums of two register slots");
   constexpr uint32_t kGroups = 32 / G;
   constexpr int V = G <= 8 ? 8 / G : 1;  // partial sums per lane
@@ -397,6 +397,14 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
 #pragma unroll
     for (int k = 0; k < S; ++k)
       if (slot_of(k) < n) s[k] = __ldg(base + slot_of(k));
+  };
+  // PF = 3: the next block's slots are only brought into L1 (three lanes of the group
+  // touch the lines of its first 24 slots) and loaded from there when the block starts,
+  // which keeps them out of the registers
+  auto prefetch_s = [&](const uint4& r) {
+    const uint32_t n = rec_count(r);
+    if (gl < 3 && gl * 8 < n)
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(a.slots + rec_offset(r) + gl * 8));
   };
   const bool cell_lane = check_level || gl == 0;
   auto load_cell = [&](const uint4& r, uint2& pk, float& pr) {
@@ -445,7 +453,10 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
       if (idx(b + 4 * W) < count) pn = pull_pos(a, idx(b + 4 * W));
     } else {
       if (idx(b + W) < count) {
-        load_s(n1, sn);
+        if constexpr (PF == 3)
+          prefetch_s(n1);
+        else
+          load_s(n1, sn);
         if (cell_lane) load_cell(n1, cpn, pern);
       }
       if (idx(b + 2 * W) < count) nn = a.rec[p3];
@@ -582,8 +593,12 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
       n1 = n2;
       n2 = nn;
     } else {
+      if constexpr (PF == 3) {
+        if (idx(b) < count) load_s(cur, s);
+      } else {
 #pragma unroll
-      for (int k = 0; k < S; ++k) s[k] = sn[k];
+        for (int k = 0; k < S; ++k) s[k] = sn[k];
+      }
       cp = cpn;
       per = pern;
       n1 = nn;
