@@ -15,11 +15,10 @@
 // neutral density keeps full relative precision near complete ionisation; the
 // smaller of x and y is the accurate one and the other is re-derived from it.
 //
-// Work per try_timestep_update attempt (counted by ncu on a level-0 launch of C2 64^3,
-// about one attempt per cell): the FP64 path (the reference's expressions) 535 DFMA, 128
-// DADD and 169 DMUL thread instructions, 1367 FP64 flops.  The mixed path shares the
-// fits' powers and exponentials and evaluates the transcendental factors in FP32
-// (before that: 366 / 63 / 156, 951 FP64 flops with the FP64 pipe 78 % busy).
+// Work per try_timestep_update attempt: the FP64 path (the reference's expressions) 535
+// DFMA, 128 DADD and 169 DMUL thread instructions, 1367 FP64 flops (ncu, C2 64^3).  The
+// mixed path evaluates the rate fits in FP32 (Fits32) and keeps the densities, the
+// sums, the implicit updates and their accept / reject tests in FP64.
 #pragma once
 
 #include <cfloat>
@@ -61,21 +60,57 @@ __device__ __forceinline__ Timescale ts_min(Timescale a, Timescale b) {
   return a.time < b.time ? a : b;
 }
 
-// Mixed path: the transcendental factors of the rate fits evaluated in FP32 (the fits
-// are empirical to a few per cent; FP32 carries them to ~1e-6 relative, the rounding of
-// the argument included), returned as FP64; every other operation of the solve, and
-// its state, stays FP64.  rcp / rsqrt: an FP32 estimate refined by one FP64 Newton step
-// (relative error ~1e-14).
-__device__ __forceinline__ double exp_f32(double a) { return (double)expf((float)a); }
-__device__ __forceinline__ double log_f32(double a) { return (double)logf((float)a); }
-__device__ __forceinline__ double log1p_f32(double a) { return (double)log1pf((float)a); }
-__device__ __forceinline__ double rcp_refined(double a) {
-  const double r = (double)__frcp_rn((float)a);
-  return r * fma(-a, r, 2.0);
-}
-__device__ __forceinline__ double rsqrt_refined(double a) {
-  const double r = (double)rsqrtf((float)a);
-  return r * fma(-0.5 * a * r, r, 1.5);
+// Mixed path: the Rosdahl et al. (2015) rate fits and their temperature derivatives
+// (hydrogen_only/mod.rs:161-273) evaluated in FP32 in the fits' own units (erg cm^3/s,
+// cm^3/s), at one temperature: the shared factors as in the FP64 forms below (one
+// reciprocal of T, rsqrt for both square roots, exp / log1p for the powers).  The
+// values carry ~1e-6 relative error; they enter the FP64 update as coefficients.
+struct Fits32 {
+  float fit, fitd;          // collision_fit and its derivative (161-173)
+  float exc, dexc;          // collisional excitation cooling / 7.5e-19-scaled form, and d/dT (237-253)
+  float recc, drecc;        // case B recombination cooling and d/dT (196-216)
+  float brems, dbrems;      // bremsstrahlung cooling and d/dT (255-263)
+  float alpha, dalpha;      // case B recombination rate and d/dT (175-194)
+};
+
+__device__ __forceinline__ Fits32 fits32(float t) {
+  Fits32 f;
+  const float inv_t = 1.0f / t;
+  const float rsq = rsqrtf(t);
+  const float sq = t * rsq;                      // sqrt(t)
+  const float s5 = sq * 0.0031622777f;           // sqrt(t / 1e5)
+  const float inv_s5 = rsq * 316.22776f;         // 1 / sqrt(t / 1e5)
+  const float inv_1s5 = 1.0f / (1.0f + s5);
+  // collision fit
+  const float c1 = 1e-5f, c2 = 157809.1f;
+  const float e = expf(-c2 * inv_t);
+  f.fit = sq * inv_1s5 * e;
+  f.fitd = (e * (c1 * c2 * t + 0.5f * s5 * (2.0f * c2 + t))) * (inv_t * rsq) * inv_s5 * (inv_1s5 * inv_1s5);
+  // collisional excitation cooling
+  const float c2e = 118348.0f;
+  const float e_exc = expf(-c2e * inv_t);
+  f.exc = 7.5e-19f * inv_1s5 * e_exc;
+  f.dexc = (7.5e-19f * e_exc * (c2e * c1 * t - 0.5f * c1 * (t * t) + c2e * s5)) * (inv_t * inv_t) * inv_s5 *
+           (inv_1s5 * inv_1s5);
+  // case B recombination cooling: lambda^1.97 and (lambda / 2.25)^0.376 from one logarithm
+  const float lambda = 315614.0f * inv_t;
+  const float ln_lambda = logf(lambda);
+  const float l197 = expf(1.97f * ln_lambda);
+  const float q = expf(0.376f * (ln_lambda - 0.81093021f));  // ln 2.25
+  const float inv_a = expf(-3.72f * log1pf(q));               // (1 + q)^-3.72
+  f.recc = 3.435e-30f * t * l197 * inv_a;
+  f.drecc = 3.435e-30f * ((inv_a / (1.0f + q)) * (1.0f - 1.97f + (1.0f - 1.97f + 0.376f * 3.72f) * q) * l197);
+  // bremsstrahlung
+  f.brems = 1.42e-27f * sq;
+  f.dbrems = 1.42e-27f * 0.5f * rsq;
+  // case B recombination rate: (lambda / 2.74)^0.407, (1 + p)^-2.242
+  const float sl = 561.79534f * rsq;                          // sqrt(lambda)
+  const float p = expf(0.407f * (ln_lambda - 1.0079579f));    // ln 2.74
+  const float inv_b = expf(-2.242f * log1pf(p));
+  f.alpha = 2.753e-14f * (lambda * sl) * inv_b;
+  const float da = -sl * (inv_b / (p + 1.0f)) * (0.407f * 2.242f * p - 1.5f * p - 1.5f);
+  f.dalpha = (2.753e-14f * da) * (-lambda * inv_t);  // d lambda / dT = -lambda / T
+  return f;
 }
 
 template <bool kCarryNeutral>
@@ -108,67 +143,23 @@ struct ChemSolver {
     fitd = (e * (c1 * c2 * t + 0.5 * s5 * (2.0 * c2 + t))) / ((t * sqrt_t) * s5 * ((s5 + 1.0) * (s5 + 1.0)));
   }
 
-  // Mixed path (kCarryNeutral): the same fits with one reciprocal of T, rsqrt for both
-  // square roots and exp / log1p for the powers ((1 + q)^-c = exp(-c log1p(q)) gives the
-  // reciprocal power directly), the transcendental factors in FP32 (exp_f32 above), the
-  // rest FP64.  The FP64 drop-in keeps the reference's expressions.
-  struct TFits {
-    double inv_t, rsq, sq, s5, inv_s5, inv_1s5;
-  };
-  __device__ static TFits t_fits(double t) {
-    TFits f;
-    f.inv_t = rcp_refined(t);
-    f.rsq = rsqrt_refined(t);
-    f.sq = t * f.rsq;                         // sqrt(t)
-    f.s5 = f.sq * 0.003162277660168379;       // sqrt(t / 1e5)
-    f.inv_s5 = f.rsq * 316.22776601683796;    // 1 / sqrt(t / 1e5)
-    f.inv_1s5 = rcp_refined(1.0 + f.s5);
-    return f;
-  }
-  __device__ static void collision_fits_fast(double t, const TFits& g, double& fit, double& fitd) {
-    const double c1 = 1.0 / 1e5, c2 = 157809.1;
-    const double e = exp_f32(-c2 * g.inv_t);
-    fit = g.sq * g.inv_1s5 * e;
-    fitd = (e * (c1 * c2 * t + 0.5 * g.s5 * (2.0 * c2 + t))) * (g.inv_t * g.rsq) * g.inv_s5 *
-           (g.inv_1s5 * g.inv_1s5);
-  }
-
-  __device__ void cooling_fast(double& lambda_c, double& dlambda_c) const {
+  // Mixed path: cooling_rate and its derivative from the FP32 fits; the densities, the
+  // sums and the unit factors in FP64.
+  __device__ void cooling32(double& lambda_c, double& dlambda_c) const {
     const double t = temperature;
     const double ne = n_ionized();
     const double nhn = n_neutral();
     const double nhi = n_ionized();
-    const TFits g = t_fits(t);
-    double fit, fitd;
-    collision_fits_fast(t, g, fit, fitd);
-    const double e_exc = exp_f32(-118348.0 * g.inv_t);
-    const double exc = (7.5e-19 * g.inv_1s5 * e_exc) * Units::kErgsCentimetersCubedPerS;
-    const double c3 = 1.0 / 1e5, c2e = 118348.0;
-    const double dexc = ((7.5e-19 * e_exc * (c2e * c3 * t - 0.5 * c3 * (t * t) + c2e * g.s5)) *
-                         (g.inv_t * g.inv_t) * g.inv_s5 * (g.inv_1s5 * g.inv_1s5)) *
-                        Units::kErgsCentimetersCubedPerS;
-    const double lambda = 315614.0 * g.inv_t;
-    const double ln_lambda = log_f32(lambda);
-    const double l197 = exp_f32(1.97 * ln_lambda);
-    const double q = exp_f32(0.376 * (ln_lambda - 0.8109302162163288));  // ln 2.25
-    const double inv_a = exp_f32(-3.72 * log1p_f32(q));                  // (1 + q)^-3.72
-    const double recomb_rate = (3.435e-30 * t * l197 * inv_a) * Units::kErgsCentimetersCubedPerS;
-    const double c2r = 1.97, c3r = 0.376, c4r = 3.72;
-    const double drecomb_rate = (3.435e-30 * ((inv_a / (1.0 + q)) *
-                                             (1.0 - 1.0 * c2r + (1.0 - 1.0 * c2r + c3r * c4r) * q) * l197)) *
-                                Units::kErgsCentimetersCubedPerS;
+    const Fits32 f = fits32((float)t);
+    const double u = Units::kErgsCentimetersCubedPerS;
     const double xx = 2.727 / scale_factor;
     const double x2 = xx * xx;
     const double compton = (1.017e-37 * (x2 * x2) * (t - xx)) * Units::kErgsPerS;
     const double dcompton = (1.017e-37 * (x2 * x2)) * Units::kErgsPerS;
-    const double coll = (exc + (1.27e-21 * fit) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
-    const double recomb = recomb_rate * ne * nhi;
-    const double brems = ((1.42e-27 * g.sq) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
-    lambda_c = coll + recomb + brems + compton * ne;
-    const double dcoll = (dexc + (1.27e-21 * fitd) * Units::kErgsCentimetersCubedPerS) * ne * nhn;
-    const double drecomb = drecomb_rate * ne * nhi;
-    const double dbrems = ((1.42e-27 * 0.5 * g.rsq) * Units::kErgsCentimetersCubedPerS) * ne * nhi;
-    dlambda_c = dcoll + drecomb + dbrems + dcompton * ne;
+    const double coll = ((double)f.exc + 1.27e-21 * (double)f.fit) * u * ne * nhn;
+    const double dcoll = ((double)f.dexc + 1.27e-21 * (double)f.fitd) * u * ne * nhn;
+    lambda_c = coll + ((double)f.recc + (double)f.brems) * u * ne * nhi + compton * ne;
+    dlambda_c = dcoll + ((double)f.drecc + (double)f.dbrems) * u * ne * nhi + dcompton * ne;
   }
 
   // cooling_rate 275-287 and cooling_rate_derivative 289-302 at the current temperature:
@@ -232,7 +223,7 @@ struct ChemSolver {
     double heating, lc, dlc;
     if (kCarryNeutral) {
       heating = ((rate * absorbed) / volume) * (Units::kPhotonAverageEnergy - Units::kRydberg);
-      cooling_fast(lc, dlc);
+      cooling32(lc, dlc);
     } else {
       heating = ((timestep * rate * absorbed) / volume) * (Units::kPhotonAverageEnergy - Units::kRydberg) / timestep;
       cooling(lc, dlc);
@@ -251,16 +242,11 @@ struct ChemSolver {
     double alpha, dalpha, fit, fitd, photo;
     const double c2a = 0.407, c3a = 2.242;
     if (kCarryNeutral) {
-      const TFits g = t_fits(t);
-      const double lambda = 315614.0 * g.inv_t;
-      const double dlambda_dt = -lambda * g.inv_t;
-      const double sl = 561.7953363992976 * g.rsq;                            // sqrt(lambda)
-      const double p = exp_f32(0.407 * (log_f32(lambda) - 1.007957920399979));  // (lambda / 2.74)^0.407
-      const double inv_b = exp_f32(-2.242 * log1p_f32(p));                      // (1 + p)^-2.242
-      alpha = (2.753e-14 * (lambda * sl) * inv_b) * Units::kCentimetersCubedPerS;
-      const double da = -sl * (inv_b / (p + 1.0)) * (c2a * c3a * p - 1.5 * p - 1.5);
-      dalpha = ((2.753e-14 * da) * Units::kCentimetersCubedPerS) * dlambda_dt;
-      collision_fits_fast(t, g, fit, fitd);
+      const Fits32 f = fits32((float)t);
+      alpha = (double)f.alpha * Units::kCentimetersCubedPerS;
+      dalpha = (double)f.dalpha * Units::kCentimetersCubedPerS;
+      fit = (double)f.fit;
+      fitd = (double)f.fitd;
       photo = (rate * absorbed) / (n_neutral() * volume);
     } else {
       const double lambda = 315614.0 / t;
