@@ -1284,9 +1284,12 @@ sw_status sw_step(sw_handle* h, double* time_elapsed_out) {
     if (h->trace) {
       swk::SweepCtl c{};
       cudaMemcpy(&c, h->p.ctl, sizeof(c), cudaMemcpyDeviceToHost);
-      std::fprintf(stderr, "subsweep sweep level=%d active_tasks=%llu kernel_ms=%.3f transport_ms=%.3f chem_ms=%.3f attempts=%llu\n",
+      std::fprintf(stderr,
+                   "subsweep sweep level=%d active_tasks=%llu kernel_ms=%.3f transport_ms=%.3f chem_ms=%.3f "
+                   "attempts=%llu chem_cells=%llu chem_attempts=%llu\n",
                    level, (unsigned long long)h->n_ge_host[level] * (unsigned long long)h->D, k, a, b,
-                   (unsigned long long)c.attempts);
+                   (unsigned long long)c.attempts, (unsigned long long)c.chem_cells,
+                   (unsigned long long)c.chem_attempts);
     }
     uint32_t err = 0;
     SW_CUDA(h, cudaMemcpy(&err, &h->p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
