@@ -156,10 +156,11 @@ TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0
                   "on C2 64^3, per task")
 
 
-# FP64 work of one try_timestep_update attempt of the chemistry kernel (mixed path),
-# counted by ncu on a level-0 launch of C2 64^3 (about one attempt per cell): 366 DFMA,
-# 63 DADD, 156 DMUL thread instructions, i.e. 2 * 366 + 63 + 156 FP64 flops.
-CHEM_FP64_FLOPS_PER_ATTEMPT = 2 * 366 + 63 + 156
+# FP64 work of one try_timestep_update attempt of the chemistry kernel (mixed path: rate
+# fits in FP32, the update in FP64), counted by ncu on the second chemistry launch of
+# the C4 generator at 64^3 (84.97 M attempts): 62.1 DFMA, 43.0 DMUL and 9.0 DADD thread
+# instructions per attempt, i.e. 2 * 62 + 43 + 9 FP64 flops.
+CHEM_FP64_FLOPS_PER_ATTEMPT = 2 * 62 + 43 + 9
 
 
 def chemistry_figures(d: dict, res: dict) -> dict:
