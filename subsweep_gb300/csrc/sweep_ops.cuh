@@ -298,6 +298,10 @@ const void* pull_kernel(int variant) {
     case 344: return (const void*)swk::k_sweep_pull_lockg<4, 4, 3>;
     case 384: return (const void*)swk::k_sweep_pull_lockg<4, 8, 3>;
     case 144: return (const void*)swk::k_sweep_pull_lockg<4, 4, 1>;
+    case 1143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1, true>;
+    case 1084: return (const void*)swk::k_sweep_pull_lockg<4, 8, 1, true>;
+    case 1242: return (const void*)swk::k_sweep_pull_lockg<2, 4, 2, true>;
+    case 1344: return (const void*)swk::k_sweep_pull_lockg<4, 4, 3, true>;
     case 72: return (const void*)swk::k_sweep_pull_wave<2>;
     case 78: return (const void*)swk::k_sweep_pull_staged;
     default: return nullptr;

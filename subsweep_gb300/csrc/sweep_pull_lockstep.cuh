@@ -361,13 +361,14 @@ namespace swk {
 // The nested-loop lockstep kernel with its shape as template parameters, for the
 // autotuner: G lanes per task (4, 8 or 16: 8, 4 or 2 tasks per warp block) and the
 // prefetch depth PF of the slots and cell data (1: the next block's, 2: also the one
-// after; 3: the next block's cell data, its slots only into L1).  Whatever the shape, the incoming rate is summed in one fixed order, so every
+// after; 3: the next block's cell data, its slots only into L1) and CS, whether the
+// records and slots are loaded with the streaming (evict-first) cache hint.  Whatever the shape, the incoming rate is summed in one fixed order, so every
 // shape gives the same bits: eight partial sums, partial j over the slots j, j + 8 (and
 // j + 16, j + 24, ... for tasks with more than 16 upwind faces) by fused multiply-adds
 // in slot order, then combined pairwise as an eight-lane butterfly (xor 1, 2, 4).  With
 // G = 4 a lane holds partials j and j + 4; with G = 16 lanes 8..15 hand their slot's
 // weight and word to lanes 0..7.
-template <int kMinBlocks, int G, int PF>
+template <int kMinBlocks, int G, int PF, bool CS = false>
 __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(PullArgs a) {
   static_assert(G == 4 || G == 8 || G == 16, "4, 8 or 16 lanes per task");
   static_assert(PF == 1 || PF == 2 || PF == 3, "prefetch depth 1 or 2, or 3: next slots into L1 only");
@@ -386,6 +387,9 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
   const bool sparse = a.act != nullptr && a.current_level > 0;
   uint32_t b = blockIdx.x * (kPullThreads / 32) + threadIdx.x / 32;
   auto idx = [&](uint32_t bb) { return bb * kGroups + g; };
+  // CS: records and slots are read once per sweep, so they are loaded with the
+  // evict-first (streaming) hint and leave L2 to the words and cell packs
+  auto ld_rec = [&](uint32_t pos) -> uint4 { return CS ? __ldcs(a.rec + pos) : a.rec[pos]; };
   // slot index held in register k of this lane
   auto slot_of = [&](int k) -> uint32_t {
     if constexpr (G <= 8) return gl + (uint32_t)(k / 2) * G + (uint32_t)(k & 1) * 8u;
@@ -396,7 +400,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
     const uint2* base = a.slots + rec_offset(r);
 #pragma unroll
     for (int k = 0; k < S; ++k)
-      if (slot_of(k) < n) s[k] = __ldg(base + slot_of(k));
+      if (slot_of(k) < n) s[k] = CS ? __ldcs(base + slot_of(k)) : __ldg(base + slot_of(k));
   };
   // PF = 3: the next block's slots are only brought into L1 (three lanes of the group
   // touch the lines of its first 24 slots) and loaded from there when the block starts,
@@ -419,10 +423,10 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
   uint2 cp = make_uint2(0u, 0u), cp1 = make_uint2(0u, 0u);
   float per = 0.f, per1 = 0.f;
   uint32_t p3 = 0;
-  if (idx(b) < count) cur = a.rec[pull_pos(a, idx(b))];
-  if (idx(b + W) < count) n1 = a.rec[pull_pos(a, idx(b + W))];
+  if (idx(b) < count) cur = ld_rec(pull_pos(a, idx(b)));
+  if (idx(b + W) < count) n1 = ld_rec(pull_pos(a, idx(b + W)));
   if constexpr (PF == 2) {
-    if (idx(b + 2 * W) < count) n2 = a.rec[pull_pos(a, idx(b + 2 * W))];
+    if (idx(b + 2 * W) < count) n2 = ld_rec(pull_pos(a, idx(b + 2 * W)));
     if (idx(b + 3 * W) < count) p3 = pull_pos(a, idx(b + 3 * W));
   } else {
     if (idx(b + 2 * W) < count) p3 = pull_pos(a, idx(b + 2 * W));
@@ -449,7 +453,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
         load_s(n2, sn);
         if (cell_lane) load_cell(n2, cpn, pern);
       }
-      if (idx(b + 3 * W) < count) nn = a.rec[p3];
+      if (idx(b + 3 * W) < count) nn = ld_rec(p3);
       if (idx(b + 4 * W) < count) pn = pull_pos(a, idx(b + 4 * W));
     } else {
       if (idx(b + W) < count) {
@@ -459,7 +463,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
           load_s(n1, sn);
         if (cell_lane) load_cell(n1, cpn, pern);
       }
-      if (idx(b + 2 * W) < count) nn = a.rec[p3];
+      if (idx(b + 2 * W) < count) nn = ld_rec(p3);
       if (idx(b + 3 * W) < count) pn = pull_pos(a, idx(b + 3 * W));
     }
     bool have = idx(b) < count;

@@ -51,7 +51,7 @@ def _poisson_boxes():
                                 num_directions=32, num_levels=3)
 
 
-@pytest.mark.parametrize("variant", [93, 95, 84, 72, 78, 143, 144, 164, 184, 242, 264, 283, 343, 344, 384, 112, 113])
+@pytest.mark.parametrize("variant", [93, 95, 84, 72, 78, 143, 144, 164, 184, 242, 264, 283, 343, 344, 384, 1084, 1143, 1242, 1344, 112, 113])
 @pytest.mark.parametrize("grid", ["lattice", "poisson"])
 def test_variant_equals_default(variant, grid, monkeypatch):
     """Each transport variant (lockstep at 3 and 5 blocks per SM, the nested-loop
