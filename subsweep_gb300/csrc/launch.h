@@ -58,7 +58,7 @@ struct DevicePtrs {
   void* pending;
   uint32_t* counters;
   uint32_t* queue;
-  unsigned long long* qe;    // pull path: {q, sweep number} per task
+  unsigned long long* qe;    // pull path: {q, sweep number} and incoming rate per schedule position
   uint32_t epoch;            // pull path: number of the current level sweep
   const uint32_t* epoch_base; // graph replay: sweep numbers are *epoch_base + epoch
   uint32_t* cell_sweep;      // pull path: number of the last sweep that solved each cell
@@ -77,7 +77,7 @@ struct DevicePtrs {
   uint32_t* act_counts;      // pull path: their lengths [32] (device)
   uint32_t* pos_of_task;     // pull path: schedule position of every task (inverse order)
   uint8_t* fold_cnt;         // pull path: upwind periodic faces per (periodic cell, direction)
-  void* fold_slots;          // pull path: their uint2 {upwind task, weight}, 4 per entry
+  void* fold_slots;          // pull path: their uint2 {upwind schedule position, weight}, 4 per entry
   uint8_t* fold_changed;     // pull path: per periodic cell, a periodic neighbour was active
   uint32_t* act_bits;        // pull path: one bit per schedule position (sparse compaction)
   int sparse_sweep;          // pull path: this launch runs over the compacted list of its level
@@ -133,9 +133,9 @@ struct PrecisionOps {
   cudaError_t (*push_records)(const DevicePtrs&, int phase, unsigned long long* scratch, cudaStream_t);
 };
 
-// pull path: transport kernel variant used without autotuning (lockstep blocks of four
-// positions, 4 target blocks per SM)
-constexpr int kDefaultPullVariant = 84;
+// pull path: transport kernel variant used without autotuning (the lockstep kernel with
+// 4 lanes per task, 3 target blocks per SM)
+constexpr int kDefaultPullVariant = 143;
 
 extern const PrecisionOps kOpsFP64;
 extern const PrecisionOps kOpsMixed;
@@ -183,7 +183,6 @@ cudaError_t launch_update_levels(const DevicePtrs&, int lowest_allowed, cudaStre
 cudaError_t launch_level_hist(const DevicePtrs&, cudaStream_t);
 // `time_dev`, when given, is read on the device instead of `time` (graph replay)
 cudaError_t launch_ionization_time(const DevicePtrs&, double time, cudaStream_t, const double* time_dev = nullptr);
-cudaError_t launch_schedule_scatter(const DevicePtrs&, const uint16_t* task_level, uint32_t* cursor, cudaStream_t);
 // Time series from per-cell summed rates: `partial` holds kTimeSeriesPartials doubles,
 // `out6` receives the six averages (device memory).
 constexpr int kTimeSeriesPartials = 256 * 8;

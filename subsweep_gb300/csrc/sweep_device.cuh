@@ -417,20 +417,6 @@ __global__ void k_kahn_round(SweepArgs<R> a, uint32_t* order, uint32_t begin, ui
   }
 }
 
-// Counting sort of the schedule by level: tasks are visited in increasing task id
-// (direction-major, cells along the space-filling curve) and appended to their level's
-// segment, so each level lists one direction's cells after another in nearly
-// increasing order and consecutive groups touch neighbouring 32-byte sectors.
-static __global__ void k_schedule_scatter(uint32_t n_tasks_padded, uint32_t N, uint32_t Np,
-                                          const uint16_t* task_level, uint32_t* cursor, uint32_t* order) {
-  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tasks_padded; t += gridDim.x * blockDim.x) {
-    const uint32_t c = t % Np;
-    if (c >= N) continue;
-    const uint32_t slot = atomicAdd(cursor + task_level[t], 1u);
-    order[slot] = t;
-  }
-}
-
 constexpr int kGroup = 8;                   // lanes per task in the scheduled sweep
 constexpr int kGroupsPerWarp = 32 / kGroup;
 constexpr int kLevelThreads = 256;
@@ -668,8 +654,11 @@ struct ChemArgs {
   int current_level;
   int D;
   uint32_t Np;
-  const R* incoming;          // incoming rate of task t at incoming[t * incoming_stride]
+  // incoming rate of task t at incoming[i * incoming_stride], i = incoming_pos[t] (the
+  // pull path's schedule position) or t when incoming_pos is null
+  const R* incoming;
   uint32_t incoming_stride;
+  const uint32_t* incoming_pos;
   const R* periodic;
   double rate_scale;
   const double* source;
@@ -705,18 +694,37 @@ __global__ void k_chemistry(ChemArgs<R> a) {
       rate = 0.0;  // sum over directions of Site::get_rate, in direction order
       for (int d = 0; d < a.D; ++d) {
         const size_t t = (size_t)d * a.Np + c;
-        rate += ((double)a.incoming[t * a.incoming_stride] + src) + (double)a.periodic[t];
+        const size_t i = a.incoming_pos ? (size_t)__ldg(a.incoming_pos + t) : t;
+        rate += ((double)a.incoming[i * a.incoming_stride] + src) + (double)a.periodic[t];
       }
     } else {
-      // compensated FP32 sum of the scaled transported rates, the source added in FP64
+      // compensated FP32 sum of the scaled transported rates in direction order, the
+      // source added in FP64.  The rates are loaded eight directions at a time: on the
+      // pull path each goes through its task's schedule position (a dependent load), so
+      // the positions of a batch are requested together, then its rates.
+      constexpr int kBatch = 8;
       float s = 0.f, comp = 0.f;
-      for (int d = 0; d < a.D; ++d) {
-        const size_t t = (size_t)d * a.Np + c;
-        const float v = (float)a.incoming[t * a.incoming_stride] + (float)a.periodic[t];
-        const float yv = v - comp;
-        const float tt = s + yv;
-        comp = (tt - s) - yv;
-        s = tt;
+      for (int d0 = 0; d0 < a.D; d0 += kBatch) {
+        size_t i[kBatch];
+        float v[kBatch];
+#pragma unroll
+        for (int j = 0; j < kBatch; ++j) {
+          const size_t t = (size_t)(d0 + j) * a.Np + c;
+          i[j] = d0 + j < a.D ? (a.incoming_pos ? (size_t)__ldg(a.incoming_pos + t) : t) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < kBatch; ++j) {
+          const size_t t = (size_t)(d0 + j) * a.Np + c;
+          v[j] = d0 + j < a.D ? (float)a.incoming[i[j] * a.incoming_stride] + (float)a.periodic[t] : 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < kBatch; ++j) {
+          if (d0 + j >= a.D) break;
+          const float yv = v[j] - comp;
+          const float tt = s + yv;
+          comp = (tt - s) - yv;
+          s = tt;
+        }
       }
       rate = (double)s * a.rate_scale + a.source[c];
     }

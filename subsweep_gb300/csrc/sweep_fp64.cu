@@ -34,14 +34,6 @@ cudaError_t launch_level_hist(const DevicePtrs& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_schedule_scatter(const DevicePtrs& p, const uint16_t* task_level, uint32_t* cursor,
-                                    cudaStream_t s) {
-  const uint32_t total = (uint32_t)((uint64_t)p.Np * p.D);
-  swk::k_schedule_scatter<<<grid_for_cells(total), 256, 0, s>>>(total, (uint32_t)p.num_cells, p.Np, task_level,
-                                                                cursor, p.order);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_time_series(const DevicePtrs& p, const double* cell_rate, bool carry_neutral, double* partial,
                                double* out6, cudaStream_t s) {
   static_assert(kTimeSeriesPartials == swk::kSeriesBlocks * swk::kSeriesSums, "partial buffer size");

@@ -108,6 +108,9 @@ struct sw_handle {
   std::string last_error;
   double* scratch = nullptr;  // N doubles for field export
   uint32_t stats_schedule_levels = 0;
+  // fingerprint of the levelled schedule (direction groups and segment offsets): the pull
+  // path's checkpointed words are indexed by schedule position
+  uint64_t schedule_hash = 0;
   int64_t stats_upwind_slots = 0;
   int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
   bool trace = false;  // SUBSWEEP_TRACE: one stderr line per level sweep
@@ -286,6 +289,67 @@ sw_status sync_ctl(sw_handle* h) {
   return SW_OK;
 }
 
+// Tasks t in [t0, t1) with t % Np < N listed by level from order[base] on, in id order
+// within a level (so each level lists one direction's cells after another in increasing
+// order along the space-filling curve, and consecutive tasks touch neighbouring 32-byte
+// sectors): each thread counts its contiguous share of the range per level, an
+// exclusive scan over (level, thread) gives every share its first slot in each level,
+// and the shares are written in parallel.  Returns the tasks per level ([L]).
+static std::vector<uint64_t> stable_level_order(const uint16_t* level, uint32_t Np, uint32_t N, uint64_t t0,
+                                                uint64_t t1, size_t L, uint64_t base, uint32_t* order) {
+  const int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<std::vector<uint64_t>> cnt(nt, std::vector<uint64_t>(L, 0u));
+  auto range = [&](int t, uint64_t& b, uint64_t& e) {
+    b = t0 + (t1 - t0) * t / nt;
+    e = t0 + (t1 - t0) * (t + 1) / nt;
+  };
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&, t]() {
+      uint64_t b, e;
+      range(t, b, e);
+      for (uint64_t i = b; i < e; ++i)
+        if (i % Np < N) ++cnt[t][level[i]];
+    });
+  for (auto& x : th) x.join();
+  th.clear();
+  std::vector<uint64_t> per_level(L, 0u);
+  uint64_t at = base;
+  for (size_t l = 0; l < L; ++l) {
+    for (int t = 0; t < nt; ++t) {
+      const uint64_t n = cnt[t][l];
+      cnt[t][l] = at;
+      at += n;
+      per_level[l] += n;
+    }
+  }
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&, t]() {
+      uint64_t b, e;
+      range(t, b, e);
+      std::vector<uint64_t>& cur = cnt[t];
+      for (uint64_t i = b; i < e; ++i)
+        if (i % Np < N) order[cur[level[i]]++] = (uint32_t)i;
+    });
+  for (auto& x : th) x.join();
+  return per_level;
+}
+
+// Number of direction groups of the schedule: SUBSWEEP_DIR_GROUPS, else as many as keep
+// a group's levels about 40 K tasks wide on average (one per 40 K tasks of the average
+// level, rounded).  That is about the number of tasks the lockstep kernels hold in
+// flight (152 SMs x 32 warps x 8 tasks), so a task seldom waits for an upwind word, and
+// a level's records, slots and words (~100 bytes a task) stay a small part of L2.
+// Measured on the C4 generator at 256^3 x 84 (4,927 levels, 286 K tasks per level):
+// 1, 4, 7 and 12 groups move 367, 169, 121 and 106 B of DRAM traffic per task in a
+// level-0 sweep of 105, 94, 91 and 93 ms.
+static int schedule_dir_groups(int D, uint64_t tasks, size_t levels) {
+  constexpr uint64_t kGroupWidth = 40960;
+  int g = (int)std::min<uint64_t>((tasks / std::max<size_t>(levels, 1) + kGroupWidth / 2) / kGroupWidth, (uint64_t)D);
+  if (const char* env = std::getenv("SUBSWEEP_DIR_GROUPS")) g = std::atoi(env);
+  return std::max(1, std::min(g, D));
+}
+
 // Levelled schedule (Kahn levels of all N*D tasks with every cell active), built once
 // per grid on the device.  A dependency cycle leaves tasks unscheduled; such a grid
 // keeps only the dependency-driven path, whose sweep then reports the stall as the
@@ -299,7 +363,7 @@ sw_status build_schedule(sw_handle* h) {
     ~DeviceScratch() {
       if (ptr) cudaFree(ptr);
     }
-  } level_scratch, cursor_scratch;
+  } level_scratch;
   SW_CUDA(h, cudaMalloc(&level_scratch.ptr, (size_t)h->Np * h->D * sizeof(uint16_t)), "schedule scratch");
   uint16_t* task_level = static_cast<uint16_t*>(level_scratch.ptr);
   SW_CUDA(h, cudaMemsetAsync(task_level, 0, (size_t)h->Np * h->D * sizeof(uint16_t), h->stream), "schedule scratch");
@@ -337,22 +401,54 @@ sw_status build_schedule(sw_handle* h) {
     SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
     return SW_OK;
   }
+  // The positions: the directions are cut into `groups` contiguous groups, each group's
+  // tasks listed after the previous group's, by Kahn level, in task-id order within a
+  // level.  Directions never depend on one another, so this is a topological order, and
+  // its segments (one per non-empty (group, level)) are levels of a valid levelled
+  // schedule.  Fewer directions per level keep the words a level reads (written one or a
+  // few levels before) in L2 on large grids.  The order is a stable counting sort on
+  // the host, so every handle on the same grid gets the same schedule: the pull path's
+  // words are indexed by schedule position, and checkpoints hold them in that order.
+  const size_t L = lvl.size() - 1;
+  const int groups = schedule_dir_groups(h->D, total, L);
+  std::vector<uint32_t> seg = {0};
+  {
+    std::vector<uint16_t> tl((size_t)h->Np * h->D);
+    SW_CUDA(h, cudaMemcpy(tl.data(), task_level, tl.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost),
+            "read task levels");
+    std::vector<uint32_t> order(total);
+    uint64_t base = 0;
+    for (int g = 0; g < groups; ++g) {
+      const uint64_t d0 = (uint64_t)h->D * g / groups, d1 = (uint64_t)h->D * (g + 1) / groups;
+      const std::vector<uint64_t> n =
+          stable_level_order(tl.data(), h->Np, (uint32_t)h->N, d0 * h->Np, d1 * h->Np, L, base, order.data());
+      for (size_t l = 0; l < L; ++l)
+        if (n[l]) {
+          base += n[l];
+          seg.push_back((uint32_t)base);
+        }
+    }
+    if (base != total) return h->fail(SW_ERR_CUDA, "schedule order incomplete");
+    SW_CUDA(h, cudaMemcpy(p.order, order.data(), order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+            "upload order");
+  }
   uint32_t* d_lvl;
   // padded to a multiple of four entries: the staged wavefront kernel copies them whole
-  const size_t lvl_words = (lvl.size() + 3) & ~(size_t)3;
+  const size_t lvl_words = (seg.size() + 3) & ~(size_t)3;
   if (!h->alloc(&d_lvl, lvl_words)) return h->fail(SW_ERR_OOM, "device allocation of the schedule failed");
   SW_CUDA(h, cudaMemset(d_lvl, 0, lvl_words * sizeof(uint32_t)), "schedule");
-  SW_CUDA(h, cudaMemcpy(d_lvl, lvl.data(), lvl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload schedule");
+  SW_CUDA(h, cudaMemcpy(d_lvl, seg.data(), seg.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload schedule");
   p.lvl_words = (uint32_t)lvl_words;
-  // rewrite each level's segment in task-id order (counting sort by level)
-  SW_CUDA(h, cudaMalloc(&cursor_scratch.ptr, lvl.size() * sizeof(uint32_t)), "schedule scratch");
-  uint32_t* cursor = static_cast<uint32_t*>(cursor_scratch.ptr);
-  SW_CUDA(h, cudaMemcpy(cursor, lvl.data(), lvl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "schedule");
-  SW_CUDA(h, swh::launch_schedule_scatter(p, task_level, cursor, h->stream), "schedule scatter kernel");
-  SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule scatter");
   p.lvl = d_lvl;
-  p.num_sched_levels = (uint32_t)(lvl.size() - 1);
-  h->stats_schedule_levels = p.num_sched_levels;
+  p.num_sched_levels = (uint32_t)(seg.size() - 1);
+  h->stats_schedule_levels = (uint32_t)L;  // the dependency depth
+  uint64_t hash = 0xcbf29ce484222325ull;  // FNV-1a over the group count and the offsets
+  auto mix = [&](uint32_t v) {
+    for (int k = 0; k < 4; ++k) hash = (hash ^ ((v >> (8 * k)) & 0xffu)) * 0x100000001b3ull;
+  };
+  mix((uint32_t)groups);
+  for (uint32_t o : seg) mix(o);
+  h->schedule_hash = hash;
   return SW_OK;
 }
 
@@ -883,14 +979,14 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     const size_t nd = (size_t)Np * D;
     const size_t rb = (size_t)h->ops->rate_bytes;
     // push path (FP64): incoming, outgoing, periodic, pending rates and the ready queue;
-    // pull path (mixed): incoming and periodic rates and the {q, sweep} words.
+    // pull path (mixed): incoming and periodic rates and the {q, sweep} words (incoming
+    // rates and words indexed by schedule position).
     const bool pull = h->ops->pull;
     char *inc = nullptr, *outg = nullptr, *per = nullptr, *pend = nullptr;
     uint32_t *cnt = nullptr, *queue = nullptr, *order = nullptr;
     unsigned long long* qe = nullptr;
     swk::SweepCtl* ctl = nullptr;
-    // the pull path keeps each task's incoming rate beside its word (16 bytes per task)
-    bool ok = (pull || h->alloc(&inc, nd * rb)) && h->alloc(&per, nd * rb) && h->alloc(&cnt, nd / 4) &&
+    bool ok = h->alloc(&inc, nd * rb) && h->alloc(&per, nd * rb) && h->alloc(&cnt, nd / 4) &&
               h->alloc(&order, nd) && h->alloc(&ctl, 1);
     uint4* rec = nullptr;
     uint32_t *act_counts = nullptr, *chunk = nullptr, *pos_of_task = nullptr, *act_bits = nullptr;
@@ -900,7 +996,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
     if (ok) ok = h->alloc(&chunk, chunks);
     if (ok && pull)
-      ok = h->alloc(&qe, 2 * nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
+      ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
            h->alloc(&act_bits, (nd + 31) / 32) && h->alloc(&cell_sweep, (size_t)h->Np) &&
            h->alloc(&cellpack, (size_t)h->Np) &&
            // per-position periodic sources: only for the staged wavefront kernel (78)
@@ -908,15 +1004,14 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
-              (pull ? rb + 49 : 4 * rb + 9) * nd >> 20);
+              (pull ? 2 * rb + 41 : 4 * rb + 9) * nd >> 20);
       return bail(SW_ERR_OOM);
     }
-    if (!pull) cudaMemset(inc, 0, nd * rb);
+    cudaMemset(inc, 0, nd * rb);
     cudaMemset(per, 0, nd * rb);
     cudaMemset(cnt, 0, nd);
     if (pull) {
-      cudaMemset(qe, 0, 2 * nd * sizeof(unsigned long long));
-      inc = reinterpret_cast<char*>(qe) + 8;  // task 0's incoming rate; stride 16 bytes
+      cudaMemset(qe, 0, nd * sizeof(unsigned long long));
       cudaMemset(cell_sweep, 0, (size_t)h->Np * sizeof(uint32_t));
       if (per_pos) cudaMemset(per_pos, 0, ((size_t)h->N * h->D + 4) * sizeof(float));
     } else {
@@ -957,6 +1052,32 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (st == SW_OK) st = build_records(h);
     if (st == SW_OK) st = build_push_records(h);
     if (st != SW_OK) return bail(st);
+  }
+  // SUBSWEEP_L2_PERSIST=1 (mixed path): keep the per-cell packs the transport gathers at
+  // random (8 B per cell) in the persisting part of L2, through an access-policy window
+  // on the handle's stream.  It sets the context's persisting-L2 limit, which the
+  // calling process shares, so it stays opt-in.
+  if (p.cellpack) {
+    const char* env = std::getenv("SUBSWEEP_L2_PERSIST");
+    int max_persist = 0, max_window = 0;
+    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, h->device);
+    cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, h->device);
+    if (env && env[0] == '1' && max_persist > 0 && max_window > 0) {
+      const size_t bytes = std::min((size_t)h->Np * sizeof(uint2), (size_t)max_window);
+      const size_t keep = std::min(bytes, (size_t)max_persist);
+      cudaStreamAttrValue v{};
+      v.accessPolicyWindow.base_ptr = p.cellpack;
+      v.accessPolicyWindow.num_bytes = bytes;
+      v.accessPolicyWindow.hitRatio = (float)((double)keep / (double)bytes);
+      v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+      v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+      if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, keep) != cudaSuccess ||
+          cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess)
+        (void)cudaGetLastError();  // a hint: run without it
+      if (h->trace)
+        std::fprintf(stderr, "subsweep L2 persisting window %zu of %zu bytes (limit %d, window %d)\n", keep, bytes,
+                     max_persist, max_window);
+    }
   }
   *out = h;
   return SW_OK;
@@ -1441,8 +1562,12 @@ struct CheckpointHeader {
   double sim_time;
   int32_t ts_lowest, ts_first_done;
   uint32_t epoch, last_epoch;
+  uint64_t schedule_hash;  // pull path: fingerprint of the schedule the words are ordered by
 };
 constexpr uint64_t kCheckpointMagic = 0x3154504357535553ull;  // "SUSWCPT1"
+// 2: the mixed path's words (8 bytes) and incoming rates (4 bytes) in two sections, by
+// schedule position
+constexpr uint32_t kCheckpointVersion = 2;
 
 struct CheckpointSection {
   void* dev;
@@ -1458,7 +1583,8 @@ static std::vector<CheckpointSection> checkpoint_sections(sw_handle* h) {
       {p.periodic, nd * rb},
   };
   if (h->ops->pull) {
-    v.push_back({p.qe, nd * 16});  // words and incoming rates
+    v.push_back({p.qe, nd * 8});  // words and incoming rates, by schedule position
+    v.push_back({p.incoming, nd * 4});
     v.push_back({p.cell_sweep, n * 4});
   } else {
     v.push_back({p.incoming, nd * rb});
@@ -1489,7 +1615,7 @@ static size_t checkpoint_bytes_for(const CheckpointHeader& hd) {
     return 0;
   const size_t n = (size_t)hd.num_cells, nd = (size_t)hd.np * (size_t)hd.num_directions, rb = hd.rate_bytes;
   size_t total = checkpoint_level_offset(hd.num_cells) + n + nd * rb;
-  total += hd.precision == SW_PRECISION_MIXED ? nd * 16 + n * 4 : 3 * nd * rb;
+  total += hd.precision == SW_PRECISION_MIXED ? nd * 12 + n * 4 : 3 * nd * rb;
   return total;
 }
 
@@ -1500,7 +1626,7 @@ static int32_t check_checkpoint(const void* buffer, size_t bytes, CheckpointHead
   CheckpointHeader hd;
   std::memcpy(&hd, buffer, sizeof(hd));
   if (hd_out) *hd_out = hd;
-  if (hd.magic != kCheckpointMagic || hd.version != 1) return 1;
+  if (hd.magic != kCheckpointMagic || hd.version != kCheckpointVersion) return 1;
   const size_t need = checkpoint_bytes_for(hd);
   if (need == 0 || hd.ts_lowest < 0 || hd.ts_lowest >= hd.num_levels) return 1;
   if (bytes < need) return 2;
@@ -1528,7 +1654,7 @@ sw_status sw_save_state(sw_handle* h, void* buffer, size_t bytes) {
   SW_DEVICE_SCOPE(h);
   CheckpointHeader hd{};
   hd.magic = kCheckpointMagic;
-  hd.version = 1;
+  hd.version = kCheckpointVersion;
   hd.precision = (uint32_t)h->params.precision;
   hd.num_cells = h->N;
   hd.num_faces = h->E;
@@ -1541,6 +1667,7 @@ sw_status sw_save_state(sw_handle* h, void* buffer, size_t bytes) {
   hd.ts_first_done = h->ts.first_done ? 1 : 0;
   hd.epoch = h->p.epoch;
   hd.last_epoch = h->last_epoch;
+  hd.schedule_hash = h->ops->pull ? h->schedule_hash : 0;
   char* out = static_cast<char*>(buffer);
   std::memcpy(out, &hd, sizeof(hd));
   size_t off = sizeof(hd);
@@ -1559,13 +1686,15 @@ sw_status sw_load_state(sw_handle* h, const void* buffer, size_t bytes) {
   const int32_t check = check_checkpoint(buffer, bytes, &hd);
   if (check == 2 && bytes < sizeof(CheckpointHeader))
     return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
-  if (hd.magic != kCheckpointMagic || hd.version != 1) return h->fail(SW_ERR_INVALID_ARG, "not a checkpoint");
+  if (hd.magic != kCheckpointMagic || hd.version != kCheckpointVersion) return h->fail(SW_ERR_INVALID_ARG, "not a checkpoint");
   if (hd.precision != (uint32_t)h->params.precision || hd.num_cells != h->N || hd.num_faces != h->E ||
       hd.num_directions != h->D || hd.num_levels != h->L || hd.np != h->Np ||
       hd.rate_bytes != (uint32_t)h->ops->rate_bytes)
     return h->fail(SW_ERR_INVALID_ARG, "checkpoint was written by a handle with another grid, parameters or precision");
   if (checkpoint_bytes_for(hd) != checkpoint_bytes(h))
     return h->fail(SW_ERR_INVALID_ARG, "checkpoint layout does not match this handle");
+  if (h->ops->pull && hd.schedule_hash != h->schedule_hash)
+    return h->fail(SW_ERR_INVALID_ARG, "checkpoint was written with another transport schedule (direction groups)");
   if (check == 1) return h->fail(SW_ERR_INVALID_ARG, "corrupt checkpoint header");
   if (check == 2) return h->fail(SW_ERR_INVALID_ARG, "checkpoint buffer too small");
   if (check == 3) return h->fail(SW_ERR_INVALID_ARG, "corrupt checkpoint: a cell's timestep level is out of range");

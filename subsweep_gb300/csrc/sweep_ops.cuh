@@ -12,7 +12,6 @@
 #include "sweep_pull.cuh"
 #include "sweep_pull_setup.cuh"
 #include "sweep_pull_lockstep.cuh"
-#include "sweep_pull_lane.cuh"
 #include "sweep_pull_wavefront.cuh"
 #include "sweep_pull_fold.cuh"
 #else
@@ -186,7 +185,8 @@ cudaError_t chemistry(const DevicePtrs& p, int level, cudaStream_t s) {
   a.D = p.D;
   a.Np = p.Np;
   a.incoming = static_cast<const R*>(p.incoming);
-  a.incoming_stride = SWK_PULL ? 4u : 1u;  // pull path: beside each task's word, 16 bytes apart
+  a.incoming_stride = 1u;
+  a.incoming_pos = SWK_PULL ? p.pos_of_task : nullptr;  // pull path: indexed by schedule position
   a.periodic = static_cast<const R*>(p.periodic);
   a.rate_scale = p.rate_scale;
   a.source = p.source;
@@ -230,6 +230,7 @@ swk::PullArgs pull_args(const DevicePtrs& p, int level) {
   a.threshold = (float)(p.threshold / p.rate_scale);
   a.periodic = static_cast<const float*>(p.periodic);
   a.qe = p.qe;
+  a.inc = static_cast<float*>(p.incoming);
   a.ctl = p.ctl;
   a.current_level = level;
   a.epoch = p.epoch;
@@ -272,34 +273,29 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
   return cudaGetLastError();
 }
 
-// Variants of the pull kernel: warp-lockstep blocks of four positions (90 + target
-// blocks per SM), their nested-loop form (80 + blocks per SM), the nested-loop form
-// with its shape as parameters (100 * prefetch depth (3: the next slots into L1 only) +
-// 10 * lanes per task (4, 8, or 6 for 16) + blocks per SM: 184 is 84's shape), one lane per task with its own cursor
-// (110 + blocks per SM) and the level-synchronous wavefronts (72: registers, 78:
+// Variants of the pull kernel: the warp-lockstep kernel with its shape as parameters
+// (100 * prefetch depth (3: the next slots into L1 only) + 10 * lanes per task (4, 8, or
+// 6 for 16) + blocks per SM, + 1000 with streaming loads of records and slots; 83 and
+// 84 name 183 and 184) and the level-synchronous wavefronts (72: registers, 78:
 // TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
 
 const void* pull_kernel(int variant) {
   switch (variant) {
-    case 93: return (const void*)swk::k_sweep_pull_lock<3>;
-    case 94: return (const void*)swk::k_sweep_pull_lock<4>;
-    case 95: return (const void*)swk::k_sweep_pull_lock<5>;
-    case 83: return (const void*)swk::k_sweep_pull_lock2<3>;
-    case 84: return (const void*)swk::k_sweep_pull_lock2<4>;
-    case 112: return (const void*)swk::k_sweep_pull_lane<2>;
-    case 113: return (const void*)swk::k_sweep_pull_lane<3>;
-    case 143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1>;
-    case 164: return (const void*)swk::k_sweep_pull_lockg<4, 16, 1>;
+    case 83:
+    case 183: return (const void*)swk::k_sweep_pull_lockg<3, 8, 1>;
+    case 84:
     case 184: return (const void*)swk::k_sweep_pull_lockg<4, 8, 1>;
+    case 143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1>;
+    case 144: return (const void*)swk::k_sweep_pull_lockg<4, 4, 1>;
+    case 164: return (const void*)swk::k_sweep_pull_lockg<4, 16, 1>;
     case 242: return (const void*)swk::k_sweep_pull_lockg<2, 4, 2>;
     case 264: return (const void*)swk::k_sweep_pull_lockg<4, 16, 2>;
     case 283: return (const void*)swk::k_sweep_pull_lockg<3, 8, 2>;
     case 343: return (const void*)swk::k_sweep_pull_lockg<3, 4, 3>;
     case 344: return (const void*)swk::k_sweep_pull_lockg<4, 4, 3>;
     case 384: return (const void*)swk::k_sweep_pull_lockg<4, 8, 3>;
-    case 144: return (const void*)swk::k_sweep_pull_lockg<4, 4, 1>;
-    case 1143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1, true>;
     case 1084: return (const void*)swk::k_sweep_pull_lockg<4, 8, 1, true>;
+    case 1143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1, true>;
     case 1242: return (const void*)swk::k_sweep_pull_lockg<2, 4, 2, true>;
     case 1344: return (const void*)swk::k_sweep_pull_lockg<4, 4, 3, true>;
     case 72: return (const void*)swk::k_sweep_pull_wave<2>;
@@ -320,16 +316,14 @@ int pull_variant(const DevicePtrs* p = nullptr) {
   return pull_kernel(v) ? v : kDefaultPullVariant;
 }
 
-// candidates of the autotuner: the nested-loop lockstep form with 8 lanes per task at 4
-// target blocks per SM, with 4 lanes per task at 3, and with 4 lanes per task and the
-// slots prefetched two blocks ahead at 2.  Measured on the C4 generator at 128^3
-// (transport G tasks/s over whole steps): 84 10.6, 143 11.0, 242 10.9, 184 10.2, the
-// lockstep blocks 93 9.1, prefetch depth 2 with 8 lanes 283 8.6, 16 lanes per task 164
-// 5.9 and 264 6.4 (on C2 128^3 the forms at 5 or 6 blocks per SM kept too many warps
-// ahead of the dependency front and retried up to twice per task).  Only dense sweeps
-// are trials and a step may offer a single one (its first), so three candidates finish
-// within three steps.
-constexpr int kTuneVariants[] = {84, 143, 242};
+// candidates of the autotuner: the lockstep kernel with 4 lanes per task at 3 target
+// blocks per SM, and at 4 with the next block's slots brought into L1 only, with and
+// without streaming loads of records and slots.  Measured on the C4 generator
+// (transport G tasks/s over whole steps, direction-grouped schedule): at 256^3 344 16.6,
+// 143 16.1, 1344 15.9, 84 10.3, 242 10.2; at 128^3 143 14.3, 1344 13.1, 344 13.0.  Only
+// dense sweeps are trials and a step may offer a single one (its first), so three
+// candidates finish within three steps.
+constexpr int kTuneVariants[] = {143, 344, 1344};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM
@@ -404,13 +398,15 @@ cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
   // run the handle's lockstep variant (which tests the upwind cells' levels) or the
   // default one
   const bool wave = variant >= 70 && variant < 80;
-  const void* fn = pull_kernel((wave && (p.sparse_sweep || p.num_sched_levels == 0)) ? kDefaultPullVariant : variant);
+  int v = (wave && (p.sparse_sweep || p.num_sched_levels == 0)) ? kDefaultPullVariant : variant;
+  const void* fn = pull_kernel(v);
   void* args[] = {&a};
   uint32_t cap = 0;
   size_t smem = 0;
   if (fn == (const void*)swk::k_sweep_pull_staged && (!p.per_pos || staged_layout(p, &cap, &smem) != cudaSuccess)) {
     (void)cudaGetLastError();
-    fn = pull_kernel(kDefaultPullVariant);  // no room for the stages: the lockstep kernel
+    v = kDefaultPullVariant;  // no room for the stages: the lockstep kernel
+    fn = pull_kernel(v);
   }
   if (fn == (const void*)swk::k_sweep_pull_staged) {  // one block of 1024 threads per SM
     uint32_t words = p.lvl_words;

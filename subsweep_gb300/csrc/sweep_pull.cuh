@@ -49,9 +49,10 @@ struct PullArgs {
   const double* att;
   float threshold;
   const float* periodic;
-  // per task t, 16 bytes at qe + 2 t: the word {q (float bits) low, sweep number high}
-  // and the task's incoming rate (float bits, low half of the second 8 bytes)
+  // per schedule position p: the word {q (float bits) low, sweep number high} at qe[p]
+  // and the task's incoming rate at inc[p]
   unsigned long long* qe;
+  float* inc;
   SweepCtl* ctl;
   int current_level;
   uint32_t epoch;
@@ -97,20 +98,18 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
   WordRef(*p).store(v, cuda::memory_order_relaxed);
 }
 
-// Task t's slot: its word, and beside it its incoming rate.  A commit writes both with
-// one 16-byte store; each 8-byte element of a vector access is single-copy atomic, so
-// readers of the word see either the old or the new word whole.
-__device__ __forceinline__ unsigned long long* word_ptr(unsigned long long* qe, size_t t) { return qe + 2 * t; }
-__device__ __forceinline__ const unsigned long long* word_ptr(const unsigned long long* qe, size_t t) {
-  return qe + 2 * t;
+// Position p's word (8 bytes, four to a 32-byte sector, so neighbouring tasks' upwind
+// words share sectors) and its incoming rate, kept apart: a sweep reads only words, and
+// the incoming rates only after the sweep (chemistry, periodic fold, export).  A commit
+// writes the word with one relaxed device-scope store, so readers see the old or the
+// new word whole.
+__device__ __forceinline__ unsigned long long* word_ptr(unsigned long long* qe, size_t p) { return qe + p; }
+__device__ __forceinline__ const unsigned long long* word_ptr(const unsigned long long* qe, size_t p) {
+  return qe + p;
 }
-__device__ __forceinline__ float stored_incoming(const unsigned long long* qe, size_t t) {
-  return __uint_as_float((uint32_t)qe[2 * t + 1]);
-}
-__device__ __forceinline__ void commit_slot(unsigned long long* qe, size_t t, unsigned long long word, float in) {
-  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(qe + 2 * t), "l"(word),
-               "l"((unsigned long long)__float_as_uint(in))
-               : "memory");
+__device__ __forceinline__ void commit_slot(const PullArgs& a, size_t p, unsigned long long word, float in) {
+  a.inc[p] = in;
+  st_relaxed_u64(a.qe + p, word);
 }
 
 // {q, sweep << 1}: solved in `sweep`; {q, sweep << 1 | 1}: stamped (inactive in `sweep`)

@@ -135,7 +135,8 @@ __global__ void __launch_bounds__(kCompactThreads) k_pull_slots(PullArgs a, uint
       if ((g.w >> kKindShift) != kKindLocal) continue;
       const float sj = face_eff(g, fx, fy, fz, a.geo64 + beg + j, dx, dy, dz);
       if (sj < 0.f) {
-        if (written < n_up) slots[o + written] = make_uint2(dnp + (g.w & kNbrMask), __float_as_uint(-sj));
+        if (written < n_up)
+          slots[o + written] = make_uint2(a.pos_of_task[dnp + (g.w & kNbrMask)], __float_as_uint(-sj));
         ++written;
       }
     }

@@ -55,11 +55,13 @@ struct WaveTask {
   uint4 r;
   uint2 s[kWaveSlots];
   float src, per, att;
+  uint32_t pos;  // schedule position (the index of the task's word)
   bool live;
 };
 
 __device__ __forceinline__ void wave_fetch(const PullArgs& a, uint32_t i, bool check_level, WaveTask& w) {
   w.r = __ldg(a.rec + i);
+  w.pos = i;
   const uint32_t c = w.r.x;
   const uint2 cp = __ldg(a.cellpack + c);  // {(float) attenuation or inactive mark, source}
   w.live = cp.x != kInactiveCell;
@@ -100,10 +102,9 @@ __device__ __forceinline__ void wave_solve(const PullArgs& a, const WaveTask& w,
     }
   }
   const float in = ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
-  const uint32_t t = rec_dir(w.r) * a.Np + w.r.x;
   const float rt = (in + w.src) + w.per;                    // Site::get_rate, site.rs:53-56
   const float out = (rt < a.threshold) ? 0.f : rt * w.att;  // get_outgoing_rate
-  commit_slot(a.qe, t, pack_qe(out * __uint_as_float(w.r.y), sweep), in);
+  commit_slot(a, w.pos, pack_qe(out * __uint_as_float(w.r.y), sweep), in);
   ++solved;
 }
 
@@ -193,12 +194,12 @@ struct StgCell {
 };
 
 
+// `pos`: the task's schedule position (the index of its word)
 __device__ __forceinline__ void stg_commit(const PullArgs& a, const uint4& r, const StgCell& c, float in,
-                                           uint32_t sweep) {
-  const uint32_t t = rec_dir(r) * a.Np + r.x;
+                                           uint32_t sweep, uint32_t pos) {
   const float rt = (in + c.src) + c.per;                    // Site::get_rate, site.rs:53-56
   const float out = (rt < a.threshold) ? 0.f : rt * c.att;  // get_outgoing_rate
-  commit_slot(a.qe, t, pack_qe(out * __uint_as_float(r.y), sweep), in);
+  commit_slot(a, pos, pack_qe(out * __uint_as_float(r.y), sweep), in);
 }
 
 // Fully staged wavefront kernel (one block of 1024 threads per SM).  A plain load still
@@ -242,8 +243,8 @@ __host__ __device__ constexpr size_t stg_smem_bytes(uint32_t cap, uint32_t lvl_w
 // q of a word published before the last grid barrier.  No word of an earlier level is
 // written during a level, and the barrier's acquire fence leaves no stale line in L1, so
 // the load may be served by L1: neighbouring tasks of a block share many upwind words.
-__device__ __forceinline__ uint32_t stg_word(const PullArgs& a, uint32_t t) {
-  return *reinterpret_cast<const unsigned int*>(word_ptr(a.qe, t));
+__device__ __forceinline__ uint32_t stg_word(const PullArgs& a, uint32_t p) {
+  return *reinterpret_cast<const unsigned int*>(word_ptr(a.qe, p));
 }
 
 // incoming rate of one task (the lockstep kernels' sum): the first 16 neighbours' words
@@ -401,7 +402,7 @@ __global__ void __launch_bounds__(kStgThreads, 1) k_sweep_pull_staged(PullArgs a
         c.att = __uint_as_float(cp.x);
         c.per = per_st[s3 * kStgPers + cu.peroff + tt];
         c.live = true;
-        stg_commit(a, r, c, in, sweep);
+        stg_commit(a, r, c, in, sweep, cu.first + tt);
         ++solved;
       }
     }

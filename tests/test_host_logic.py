@@ -68,10 +68,10 @@ def _checkpoint(num_cells=10, directions=4, levels=3, np_=32, precision=1, rate_
     """A checkpoint buffer laid out as sw_save_state writes it: the header, seven
     per-cell double arrays, the per-cell levels, then the per-task sections."""
     import struct
-    header = struct.pack("<QIIqqiiIIdiiII", 0x3154504357535553, 1, precision, num_cells, 7 * num_cells,
-                         directions, levels, np_, rate_bytes, 0.0, 0, 1, 5, 4)
+    header = struct.pack("<QIIqqiiIIdiiIIQ", 0x3154504357535553, 2, precision, num_cells, 7 * num_cells,
+                         directions, levels, np_, rate_bytes, 0.0, 0, 1, 5, 4, 0)
     nd = np_ * directions
-    tail = nd * rate_bytes + (nd * 16 + num_cells * 4 if precision == 1 else 3 * nd * rate_bytes)
+    tail = nd * rate_bytes + (nd * 12 + num_cells * 4 if precision == 1 else 3 * nd * rate_bytes)
     buf = bytearray(header + bytes(7 * 8 * num_cells) + bytes([level_fill]) * num_cells + bytes(tail))
     return buf, len(header) + 7 * 8 * num_cells
 
