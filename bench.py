@@ -146,14 +146,14 @@ def mean_downwind_faces(grid, directions: np.ndarray, sample: int = 60000, seed:
     return float((dots > 0).sum() / (len(cells) * directions.shape[0])) if counts.sum() else 0.0
 
 
-# DRAM bytes per task of the pull transport kernel (nested-loop lockstep variant, the
-# autotuner's choice on C2), measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on a level-0 launch of the C2 grid at 64^3 (22,020,096 tasks):
-# 2.411 GB per launch.  The per-launch traffic at other sizes is scaled by the tasks of
-# a launch.
-MEASURED_DRAM_BYTES_PER_TASK = {"mixed": 109.5}
-TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 k_sweep_pull_lock2 launch "
-                  "on C2 64^3, per task")
+# DRAM bytes per task of the pull transport kernel (lockstep kernel with 2 lanes per
+# task, variant 122, the autotuner's choice on C4 256^3), measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on a level-0 launch of the
+# C4 generator at 256^3 (1,409,286,144 tasks): 142.04 + 20.99 GB per launch.  The
+# per-launch traffic of other launches is scaled by their tasks.
+MEASURED_DRAM_BYTES_PER_TASK = {"mixed": 115.7}
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0 k_sweep_pull_lockg<2,2,1> "
+                  "launch on C4 256^3, per task")
 
 
 # FP64 work of one try_timestep_update attempt of the chemistry kernel (mixed path: rate

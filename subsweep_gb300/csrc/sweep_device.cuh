@@ -654,11 +654,7 @@ struct ChemArgs {
   int current_level;
   int D;
   uint32_t Np;
-  // incoming rate of task t at incoming[i * incoming_stride], i = incoming_pos[t] (the
-  // pull path's schedule position) or t when incoming_pos is null
-  const R* incoming;
-  uint32_t incoming_stride;
-  const uint32_t* incoming_pos;
+  const R* incoming;           // incoming rate of task t at incoming[t]
   const R* periodic;
   double rate_scale;
   const double* source;
@@ -694,28 +690,19 @@ __global__ void k_chemistry(ChemArgs<R> a) {
       rate = 0.0;  // sum over directions of Site::get_rate, in direction order
       for (int d = 0; d < a.D; ++d) {
         const size_t t = (size_t)d * a.Np + c;
-        const size_t i = a.incoming_pos ? (size_t)__ldg(a.incoming_pos + t) : t;
-        rate += ((double)a.incoming[i * a.incoming_stride] + src) + (double)a.periodic[t];
+        rate += ((double)a.incoming[t] + src) + (double)a.periodic[t];
       }
     } else {
       // compensated FP32 sum of the scaled transported rates in direction order, the
-      // source added in FP64.  The rates are loaded eight directions at a time: on the
-      // pull path each goes through its task's schedule position (a dependent load), so
-      // the positions of a batch are requested together, then its rates.
+      // source added in FP64; the rates are loaded eight directions at a time
       constexpr int kBatch = 8;
       float s = 0.f, comp = 0.f;
       for (int d0 = 0; d0 < a.D; d0 += kBatch) {
-        size_t i[kBatch];
         float v[kBatch];
 #pragma unroll
         for (int j = 0; j < kBatch; ++j) {
           const size_t t = (size_t)(d0 + j) * a.Np + c;
-          i[j] = d0 + j < a.D ? (a.incoming_pos ? (size_t)__ldg(a.incoming_pos + t) : t) : 0;
-        }
-#pragma unroll
-        for (int j = 0; j < kBatch; ++j) {
-          const size_t t = (size_t)(d0 + j) * a.Np + c;
-          v[j] = d0 + j < a.D ? (float)a.incoming[i[j] * a.incoming_stride] + (float)a.periodic[t] : 0.f;
+          v[j] = d0 + j < a.D ? (float)a.incoming[t] + (float)a.periodic[t] : 0.f;
         }
 #pragma unroll
         for (int j = 0; j < kBatch; ++j) {

@@ -979,8 +979,8 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     const size_t nd = (size_t)Np * D;
     const size_t rb = (size_t)h->ops->rate_bytes;
     // push path (FP64): incoming, outgoing, periodic, pending rates and the ready queue;
-    // pull path (mixed): incoming and periodic rates and the {q, sweep} words (incoming
-    // rates and words indexed by schedule position).
+    // pull path (mixed): incoming and periodic rates and the {q, sweep} words (words
+    // indexed by schedule position).
     const bool pull = h->ops->pull;
     char *inc = nullptr, *outg = nullptr, *per = nullptr, *pend = nullptr;
     uint32_t *cnt = nullptr, *queue = nullptr, *order = nullptr;
@@ -1565,8 +1565,8 @@ struct CheckpointHeader {
   uint64_t schedule_hash;  // pull path: fingerprint of the schedule the words are ordered by
 };
 constexpr uint64_t kCheckpointMagic = 0x3154504357535553ull;  // "SUSWCPT1"
-// 2: the mixed path's words (8 bytes) and incoming rates (4 bytes) in two sections, by
-// schedule position
+// 2: the mixed path's words (8 bytes, by schedule position) and incoming rates (4 bytes,
+// by task) in two sections
 constexpr uint32_t kCheckpointVersion = 2;
 
 struct CheckpointSection {
@@ -1583,7 +1583,7 @@ static std::vector<CheckpointSection> checkpoint_sections(sw_handle* h) {
       {p.periodic, nd * rb},
   };
   if (h->ops->pull) {
-    v.push_back({p.qe, nd * 8});  // words and incoming rates, by schedule position
+    v.push_back({p.qe, nd * 8});  // words, by schedule position
     v.push_back({p.incoming, nd * 4});
     v.push_back({p.cell_sweep, n * 4});
   } else {

@@ -185,8 +185,6 @@ cudaError_t chemistry(const DevicePtrs& p, int level, cudaStream_t s) {
   a.D = p.D;
   a.Np = p.Np;
   a.incoming = static_cast<const R*>(p.incoming);
-  a.incoming_stride = 1u;
-  a.incoming_pos = SWK_PULL ? p.pos_of_task : nullptr;  // pull path: indexed by schedule position
   a.periodic = static_cast<const R*>(p.periodic);
   a.rate_scale = p.rate_scale;
   a.source = p.source;
@@ -274,8 +272,8 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 }
 
 // Variants of the pull kernel: the warp-lockstep kernel with its shape as parameters
-// (100 * prefetch depth (3: the next slots into L1 only) + 10 * lanes per task (4, 8, or
-// 6 for 16) + blocks per SM, + 1000 with streaming loads of records and slots; 83 and
+// (100 * prefetch depth (3: the next slots into L1 only) + 10 * lanes per task (2, 4, 8,
+// or 6 for 16) + blocks per SM, + 1000 with streaming loads of records and slots; 83 and
 // 84 name 183 and 184) and the level-synchronous wavefronts (72: registers, 78:
 // TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
 
@@ -285,6 +283,10 @@ const void* pull_kernel(int variant) {
     case 183: return (const void*)swk::k_sweep_pull_lockg<3, 8, 1>;
     case 84:
     case 184: return (const void*)swk::k_sweep_pull_lockg<4, 8, 1>;
+    case 122: return (const void*)swk::k_sweep_pull_lockg<2, 2, 1>;
+    case 123: return (const void*)swk::k_sweep_pull_lockg<3, 2, 1>;
+    case 322: return (const void*)swk::k_sweep_pull_lockg<2, 2, 3>;
+    case 323: return (const void*)swk::k_sweep_pull_lockg<3, 2, 3>;
     case 143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1>;
     case 144: return (const void*)swk::k_sweep_pull_lockg<4, 4, 1>;
     case 164: return (const void*)swk::k_sweep_pull_lockg<4, 16, 1>;
@@ -316,14 +318,14 @@ int pull_variant(const DevicePtrs* p = nullptr) {
   return pull_kernel(v) ? v : kDefaultPullVariant;
 }
 
-// candidates of the autotuner: the lockstep kernel with 4 lanes per task at 3 target
-// blocks per SM, and at 4 with the next block's slots brought into L1 only, with and
-// without streaming loads of records and slots.  Measured on the C4 generator
-// (transport G tasks/s over whole steps, direction-grouped schedule): at 256^3 344 16.6,
-// 143 16.1, 1344 15.9, 84 10.3, 242 10.2; at 128^3 143 14.3, 1344 13.1, 344 13.0.  Only
-// dense sweeps are trials and a step may offer a single one (its first), so three
-// candidates finish within three steps.
-constexpr int kTuneVariants[] = {143, 344, 1344};
+// candidates of the autotuner: the lockstep kernel with 2 lanes per task at 2 target
+// blocks per SM, with 4 lanes per task at 3, and at 4 with the next block's slots
+// brought into L1 only.  Measured on the C4 generator (transport G tasks/s over whole
+// steps, direction-grouped schedule): at 256^3 122 18.6, 323 17.6, 344 16.7, 322 16.3,
+// 143 16.1, 1344 15.9, 84 10.3, 242 10.2; at 128^3 143 14.3, 122 14.0, 344 13.6, 1344
+// 13.1, 323 12.6.  Only dense sweeps are trials and a step may offer a single one (its
+// first), so three candidates finish within three steps.
+constexpr int kTuneVariants[] = {122, 143, 344};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM

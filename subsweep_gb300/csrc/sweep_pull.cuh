@@ -49,8 +49,8 @@ struct PullArgs {
   const double* att;
   float threshold;
   const float* periodic;
-  // per schedule position p: the word {q (float bits) low, sweep number high} at qe[p]
-  // and the task's incoming rate at inc[p]
+  // per schedule position p: the word {q (float bits) low, sweep number high} at qe[p];
+  // per task t: its incoming rate at inc[t]
   unsigned long long* qe;
   float* inc;
   SweepCtl* ctl;
@@ -99,17 +99,14 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
 }
 
 // Position p's word (8 bytes, four to a 32-byte sector, so neighbouring tasks' upwind
-// words share sectors) and its incoming rate, kept apart: a sweep reads only words, and
-// the incoming rates only after the sweep (chemistry, periodic fold, export).  A commit
+// words share sectors).  The incoming rates are kept apart, by task: a sweep reads only
+// words, and the incoming rates are read after the sweep (chemistry, periodic fold,
+// export), the chemistry's per-cell sum over directions in coalesced rows.  A commit
 // writes the word with one relaxed device-scope store, so readers see the old or the
 // new word whole.
 __device__ __forceinline__ unsigned long long* word_ptr(unsigned long long* qe, size_t p) { return qe + p; }
 __device__ __forceinline__ const unsigned long long* word_ptr(const unsigned long long* qe, size_t p) {
   return qe + p;
-}
-__device__ __forceinline__ void commit_slot(const PullArgs& a, size_t p, unsigned long long word, float in) {
-  a.inc[p] = in;
-  st_relaxed_u64(a.qe + p, word);
 }
 
 // {q, sweep << 1}: solved in `sweep`; {q, sweep << 1 | 1}: stamped (inactive in `sweep`)
@@ -162,5 +159,12 @@ __device__ __forceinline__ unsigned long long rec_offset(const uint4& r) {
 __device__ __forceinline__ uint32_t rec_count(const uint4& r) { return r.w & 0x7fu; }
 __device__ __forceinline__ uint32_t rec_dir(const uint4& r) { return (r.w >> 7) & 0x7fu; }
 __device__ __forceinline__ bool rec_periodic(const uint4& r) { return (r.w & kRecPeriodic) != 0u; }
+
+// commit of the task with record r at position p
+__device__ __forceinline__ void commit_slot(const PullArgs& a, size_t p, const uint4& r, unsigned long long word,
+                                            float in) {
+  a.inc[(size_t)rec_dir(r) * a.Np + r.x] = in;
+  st_relaxed_u64(a.qe + p, word);
+}
 
 }  // namespace swk

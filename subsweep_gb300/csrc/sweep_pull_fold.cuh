@@ -112,9 +112,9 @@ __device__ __forceinline__ bool cell_current(const PullArgs& a, uint32_t c) {
 // inactive cells).
 __device__ __forceinline__ float current_incoming(const PullArgs& a, uint32_t c, uint32_t d, uint32_t last_epoch,
                                                   bool cell_is_current) {
-  const size_t pos = a.pos_of_task[(size_t)d * a.Np + c];
-  if (cell_is_current) return a.inc[pos];
-  if ((uint32_t)(*word_ptr(a.qe, pos) >> 32) == (last_epoch << 1)) return a.inc[pos];  // solved
+  const size_t t = (size_t)d * a.Np + c;
+  if (cell_is_current) return a.inc[t];
+  if ((uint32_t)(*word_ptr(a.qe, a.pos_of_task[t]) >> 32) == (last_epoch << 1)) return a.inc[t];  // solved
   return gather_in(a, c, d, false);
 }
 

@@ -31,7 +31,7 @@ __device__ __forceinline__ uint32_t cell_at(const PullArgs& a, uint32_t p) {
 
 // ---------------------------------------------------------------------------------------
 // The nested-loop lockstep kernel with its shape as template parameters, for the
-// autotuner: G lanes per task (4, 8 or 16: 8, 4 or 2 tasks per warp block) and the
+// autotuner: G lanes per task (2, 4, 8 or 16: 16, 8, 4 or 2 tasks per warp block) and the
 // prefetch depth PF of the slots and cell data (1: the next block's, 2: also the one
 // after; 3: the next block's cell data, its slots only into L1) and CS, whether the
 // records and slots are loaded with the streaming (evict-first) cache hint.  Whatever
@@ -39,11 +39,12 @@ __device__ __forceinline__ uint32_t cell_at(const PullArgs& a, uint32_t p) {
 // same bits: eight partial sums, partial j over the slots j, j + 8 (and
 // j + 16, j + 24, ... for tasks with more than 16 upwind faces) by fused multiply-adds
 // in slot order, then combined pairwise as an eight-lane butterfly (xor 1, 2, 4).  With
-// G = 4 a lane holds partials j and j + 4; with G = 16 lanes 8..15 hand their slot's
-// weight and word to lanes 0..7.
+// G = 4 a lane holds partials j and j + 4 (xor 4 within the lane); with G = 2 lane j
+// holds partials j, j + 2, j + 4, j + 6 (xor 2 and 4 within the lane); with G = 16
+// lanes 8..15 hand their slot's weight and word to lanes 0..7.
 template <int kMinBlocks, int G, int PF, bool CS = false>
 __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(PullArgs a) {
-  static_assert(G == 4 || G == 8 || G == 16, "4, 8 or 16 lanes per task");
+  static_assert(G == 2 || G == 4 || G == 8 || G == 16, "2, 4, 8 or 16 lanes per task");
   static_assert(PF == 1 || PF == 2 || PF == 3, "prefetch depth 1 or 2, or 3: next slots into L1 only");
   static_assert(kPullGroup == 8 && kPullRounds == 2, "eight partial sums of two register slots");
   constexpr uint32_t kGroups = 32 / G;
@@ -210,10 +211,15 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
         }
       }
       const uint32_t badmask = __ballot_sync(0xffffffffu, bad);
-      // butterfly over the eight partials: xor 1 and 2 between lanes (xor 4 between lanes
-      // for G >= 8, within the lane for G = 4)
+      // butterfly over the eight partials: xor 1 between lanes; xor 2 between lanes for
+      // G >= 4, within the lane for G = 2; xor 4 between lanes for G >= 8, within the lane
+      // for G <= 4
       float in;
-      if constexpr (G == 4) {
+      if constexpr (G == 2) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) part[v] += __shfl_xor_sync(0xffffffffu, part[v], 1, 2);
+        in = (part[0] + part[1]) + (part[2] + part[3]);
+      } else if constexpr (G == 4) {
 #pragma unroll
         for (int o = 1; o < 4; o <<= 1) {
           part[0] += __shfl_xor_sync(0xffffffffu, part[0], o, 4);
@@ -230,7 +236,7 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
       if (commit && gl == 0) {
         const float rt = (in + src) + per;                      // Site::get_rate, site.rs:53-56
         const float out = (rt < a.threshold) ? 0.f : rt * att;  // get_outgoing_rate
-        commit_slot(a, pos, pack_qe(out * __uint_as_float(cur.y), sweep), in);
+        commit_slot(a, pos, cur, pack_qe(out * __uint_as_float(cur.y), sweep), in);
         ++solved;
       }
       have = have && !commit;

@@ -104,7 +104,7 @@ __device__ __forceinline__ void wave_solve(const PullArgs& a, const WaveTask& w,
   const float in = ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
   const float rt = (in + w.src) + w.per;                    // Site::get_rate, site.rs:53-56
   const float out = (rt < a.threshold) ? 0.f : rt * w.att;  // get_outgoing_rate
-  commit_slot(a, w.pos, pack_qe(out * __uint_as_float(w.r.y), sweep), in);
+  commit_slot(a, w.pos, w.r, pack_qe(out * __uint_as_float(w.r.y), sweep), in);
   ++solved;
 }
 
@@ -199,7 +199,7 @@ __device__ __forceinline__ void stg_commit(const PullArgs& a, const uint4& r, co
                                            uint32_t sweep, uint32_t pos) {
   const float rt = (in + c.src) + c.per;                    // Site::get_rate, site.rs:53-56
   const float out = (rt < a.threshold) ? 0.f : rt * c.att;  // get_outgoing_rate
-  commit_slot(a, pos, pack_qe(out * __uint_as_float(r.y), sweep), in);
+  commit_slot(a, pos, r, pack_qe(out * __uint_as_float(r.y), sweep), in);
 }
 
 // Fully staged wavefront kernel (one block of 1024 threads per SM).  A plain load still
