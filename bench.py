@@ -191,6 +191,8 @@ def build_workload(name: str, n_per_side, nthreads: int, grid_device: str = "hos
         return workloads.c2_lognormal(n_per_side=n_per_side or 128, grid_device=grid_device, thick=thick, **kw)
     if name == "c4":
         return workloads.c4_grf(n_per_side=n_per_side or 256, grid_device=grid_device, thick=thick, **kw)
+    if name == "c5":
+        return workloads.c5_grf(n_per_side=n_per_side or 384, grid_device=grid_device, thick=thick, **kw)
     if name == "c3":
         return workloads.c3_batched(num_boxes=n_per_side or 256, thick=thick, **kw)
     raise SystemExit(f"unknown workload {name}")
@@ -341,6 +343,8 @@ def time_precision(w, precision: str, device: int, warmup: int, steps: int, dist
     st1 = s.stats()
     dist.barrier()
     d = {k: st1[k] - st0[k] for k in st1}
+    for k in ("task_spaces", "device_bytes", "pull_variant", "schedule_levels"):  # states, not counters
+        d[k] = st1[k]
     return s, d, clocks, {"per_step_ms": per_step, "wall_s": wall, "snapshot": snap}
 
 
@@ -391,9 +395,11 @@ def radiation_field(s, w) -> dict:
     1e-6 of the total source, and of ionized cells."""
     total = float(w.source.sum())
     d = w.params.num_directions()
-    inc = s.rates(which=("incoming",))["incoming"]
-    frac_cd = float((inc > 1e-6 * total / d).mean())
-    del inc
+    frac_cd = None
+    if w.grid.num_cells * d < 1 << 31:  # C5's per-task rates would take 38 GB of host memory
+        inc = s.rates(which=("incoming",))["incoming"]
+        frac_cd = float((inc > 1e-6 * total / d).mean())
+        del inc
     f = s.fields()
     return {"cell_dir_above_1e-6_of_source": frac_cd,
             "cells_above_1e-6_of_source": float((f["photon_rate"] > 1e-6 * total).mean()),
@@ -453,6 +459,8 @@ def run_ours(args, dist: Dist):
     # field comparison are taken over those common steps.
     results, snaps = {}, {}
     precisions = ("fp64", "mixed") if args.precision == "both" else (args.precision,)
+    if args.workload == "c5":  # 4.76 G tasks: beyond the FP64 path's 32-bit task ids
+        precisions = ("mixed",)
     head = precisions[-1]
     k_common = min(args.steps, 4) if len(precisions) == 2 else args.steps
     s = None
@@ -495,10 +503,13 @@ def run_ours(args, dist: Dist):
     b_task = bytes_per_task(f_dn, 4 if head == "mixed" else 8)
     achieved_gbs = d["tasks"] * b_task / (d["transport_kernel_ms"] / 1e3) / 1e9 if d["transport_kernel_ms"] else None
     launches = d["transport_launches"]
+    # the measured bytes per task are the full state's lockstep kernel's; the compact
+    # state (C5) runs the geometry kernel, whose traffic is not captured
     traffic = (MEASURED_DRAM_BYTES_PER_TASK[head] * d["tasks"] / launches
-               if head in MEASURED_DRAM_BYTES_PER_TASK and launches else None)
+               if head in MEASURED_DRAM_BYTES_PER_TASK and launches and not d.get("task_spaces") else None)
     cpu = semantics = None
-    if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
+    # C5's full-grid CPU sample would hold its per-task FP64 state (4.76 G tasks) in host memory
+    if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline and args.workload != "c5":
         threads = os.cpu_count() or 1
         sample = OracleSample(w, threads)
         c_tasks, c_chem, c_wall = time_oracle(sample, 1, 1)
@@ -569,7 +580,8 @@ def run_ours(args, dist: Dist):
                   "sweep_ms": d["sweep_ms"], "chem_ms": d["chem_ms"], "level_ms": d["level_ms"],
                   "fp64_transport_kernel_ms": fp64["d"]["transport_kernel_ms"] if fp64 else None,
                   "fp64_chem_ms": fp64["d"]["chem_ms"] if fp64 else None,
-                  "fp64_tasks": fp64["d"]["tasks"] if fp64 else None},
+                  "fp64_tasks": fp64["d"]["tasks"] if fp64 else None,
+                  "task_spaces": d.get("task_spaces"), "device_bytes": d.get("device_bytes")},
     }
     print(json.dumps(line), flush=True)
 
@@ -580,7 +592,8 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4"], default="c4")
+    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4", "c5"], default="c4",
+                    help="c5: the stress configuration, mixed path only (its FP64 state would not fit)")
     ap.add_argument("--n-per-side", type=int, default=None,
                     help="cells per side (C1, C2, C4) or boxes (C3); default the configuration's")
     ap.add_argument("--thick", action="store_true", help="C2-C4 at C1's 1 Mpc / 32 cell size")

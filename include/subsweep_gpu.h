@@ -128,7 +128,11 @@ typedef struct {
                                   ones on the pull path, downwind LOCAL / LOCAL_PERIODIC ones on
                                   the push path (0 when the push path computes geometry) */
   int64_t graph_launches;      /* steps replayed from a CUDA graph */
-  int64_t pull_variant;        /* mixed path: transport kernel variant in use (autotuned or set) */
+  int64_t pull_variant;        /* mixed path: transport kernel variant in use (autotuned or set);
+                                  0 in the compact state (the geometry kernel) */
+  int64_t task_spaces;         /* mixed path, compact state: task spaces the directions are split
+                                  into (0: the full state with task records and upwind slots) */
+  int64_t device_bytes;        /* device memory the handle holds (grid, state, schedule) */
 } sw_stats;
 
 /* Fill the reference's defaults (num_directions 84, levels 1, max_timestep 1 Myr). */

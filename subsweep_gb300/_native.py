@@ -110,6 +110,8 @@ class SwStats(ctypes.Structure):
         ("upwind_slots", c_int64),
         ("graph_launches", c_int64),
         ("pull_variant", c_int64),
+        ("task_spaces", c_int64),
+        ("device_bytes", c_int64),
     ]
 
 

@@ -16,6 +16,9 @@ struct SweepCtl;
 
 namespace swh {
 
+// Task spaces of the compact pull state: directions [space_d0[s], space_d0[s + 1]).
+constexpr int kMaxSpaces = 8;
+
 // Raw device pointers of one handle.  Rate arrays are double (FP64) or float (mixed);
 // per-task arrays are [dir][cell] with cell stride Np.
 struct DevicePtrs {
@@ -80,6 +83,16 @@ struct DevicePtrs {
   void* fold_slots;          // pull path: their uint2 {upwind schedule position, weight}, 4 per entry
   uint8_t* fold_changed;     // pull path: per periodic cell, a periodic neighbour was active
   uint32_t* act_bits;        // pull path: one bit per schedule position (sparse compaction)
+  // pull path, compact state (geo_mode): no task records, upwind slots or inverse order
+  // (pos_of_task is null and the words are indexed by task); the geometry kernel sweeps
+  // every position of each task space (directions split so that a space holds fewer
+  // than 2^31 tasks), one space after another, with its own levelled schedule
+  int geo_mode;
+  int num_spaces;                       // 1 unless geo_mode splits the directions
+  int space_d0[kMaxSpaces + 1];
+  uint32_t* space_lvl[kMaxSpaces];      // segment offsets of each space's schedule
+  uint32_t space_segments[kMaxSpaces];
+  uint32_t space_lvl_words[kMaxSpaces];
   int sparse_sweep;          // pull path: this launch runs over the compacted list of its level
   int compact_now;           // pull path: ... and builds that list first
   uint32_t* chunk;           // pull path: compaction chunk offsets, count at [num_chunks]
@@ -136,6 +149,35 @@ struct PrecisionOps {
 // pull path: transport kernel variant used without autotuning (the lockstep kernel with
 // 4 lanes per task, 3 target blocks per SM)
 constexpr int kDefaultPullVariant = 143;
+
+// The pointers of task space s of a compact pull state: its directions, its per-task
+// arrays (incoming, periodic, words, counters: [dir][cell] slices; FP32 rates), its
+// schedule and its periodic fold entries.  Task ids and positions inside a view are
+// local to the space.  With one space the view is the handle's pointers.
+inline DevicePtrs space_view(const DevicePtrs& p, int s) {
+  if (p.num_spaces <= 1) return p;
+  DevicePtrs v = p;
+  const int d0 = p.space_d0[s];
+  const size_t off = (size_t)d0 * p.Np;
+  v.D = p.space_d0[s + 1] - d0;
+  for (int i = 0; i < 3 * v.D; ++i) v.dir32_host[i] = p.dir32_host[3 * d0 + i];
+  v.dir64 = p.dir64 + 3 * d0;
+  v.dir32 = p.dir32 + 3 * d0;
+  v.incoming = static_cast<char*>(p.incoming) + off * sizeof(float);
+  v.periodic = static_cast<char*>(p.periodic) + off * sizeof(float);
+  v.qe = p.qe + off;
+  v.counters = p.counters + off / 4;  // u8 counters, four to a word (Np is a multiple of 32)
+  v.order = p.order + (size_t)p.num_cells * d0;
+  v.lvl = p.space_lvl[s];
+  v.num_sched_levels = p.space_segments[s];
+  v.lvl_words = p.space_lvl_words[s];
+  constexpr size_t kFoldEntrySlots = 4;
+  if (p.fold_cnt) v.fold_cnt = p.fold_cnt + (size_t)d0 * p.n_periodic_cells;
+  if (p.fold_slots)
+    v.fold_slots = static_cast<char*>(p.fold_slots) + (size_t)d0 * p.n_periodic_cells * kFoldEntrySlots * 8;
+  v.num_spaces = 1;
+  return v;
+}
 
 extern const PrecisionOps kOpsFP64;
 extern const PrecisionOps kOpsMixed;

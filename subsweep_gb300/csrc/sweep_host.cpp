@@ -111,6 +111,7 @@ struct sw_handle {
   // fingerprint of the levelled schedule (direction groups and segment offsets): the pull
   // path's checkpointed words are indexed by schedule position
   uint64_t schedule_hash = 0;
+  int64_t device_bytes = 0;  // device memory held by the handle (its allocations)
   int64_t stats_upwind_slots = 0;
   int force_path = 0;  // 0 automatic, 1 always levelled, 2 always dependency-driven
   bool trace = false;  // SUBSWEEP_TRACE: one stderr line per level sweep
@@ -150,6 +151,7 @@ struct sw_handle {
     cudaError_t e = dalloc(ptr, count);
     if (e != cudaSuccess) return false;
     allocations.push_back((void*)*ptr);
+    device_bytes += (int64_t)(count * sizeof(T));
     return true;
   }
 
@@ -335,6 +337,15 @@ static std::vector<uint64_t> stable_level_order(const uint16_t* level, uint32_t 
   return per_level;
 }
 
+// Compact state (mixed path): task spaces hold fewer than kSpaceTasks tasks each.  The
+// fewest spaces of evenly split directions that do, 0 when kMaxSpaces are not enough.
+constexpr uint64_t kSpaceTasks = 1ull << 31;
+static int min_task_spaces(uint32_t Np, int D) {
+  for (int s = 1; s <= std::min(D, swh::kMaxSpaces); ++s)
+    if ((uint64_t)Np * (uint64_t)((D + s - 1) / s) < kSpaceTasks) return s;
+  return 0;
+}
+
 // Number of direction groups of the schedule: SUBSWEEP_DIR_GROUPS, else as many as keep
 // a group's levels about 40 K tasks wide on average (one per 40 K tasks of the average
 // level, rounded).  That is about the number of tasks the lockstep kernels hold in
@@ -351,103 +362,123 @@ static int schedule_dir_groups(int D, uint64_t tasks, size_t levels) {
 }
 
 // Levelled schedule (Kahn levels of all N*D tasks with every cell active), built once
-// per grid on the device.  A dependency cycle leaves tasks unscheduled; such a grid
-// keeps only the dependency-driven path, whose sweep then reports the stall as the
-// reference would deadlock.
+// per grid on the device, per task space (one space unless the compact state splits the
+// directions; task ids and positions are local to a space).  A dependency cycle leaves
+// tasks unscheduled; such a grid keeps only the dependency-driven path, whose sweep then
+// reports the stall as the reference would deadlock (the compact state, which has no
+// such path, refuses the grid).
 sw_status build_schedule(sw_handle* h) {
   swh::DevicePtrs& p = h->p;
-  const uint64_t total = (uint64_t)h->N * (uint64_t)h->D;
-  SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
   struct DeviceScratch {
     void* ptr = nullptr;
     ~DeviceScratch() {
       if (ptr) cudaFree(ptr);
     }
   } level_scratch;
-  SW_CUDA(h, cudaMalloc(&level_scratch.ptr, (size_t)h->Np * h->D * sizeof(uint16_t)), "schedule scratch");
+  int max_ds = 0;
+  for (int sp = 0; sp < p.num_spaces; ++sp) max_ds = std::max(max_ds, p.space_d0[sp + 1] - p.space_d0[sp]);
+  SW_CUDA(h, cudaMalloc(&level_scratch.ptr, (size_t)h->Np * max_ds * sizeof(uint16_t)), "schedule scratch");
   uint16_t* task_level = static_cast<uint16_t*>(level_scratch.ptr);
-  SW_CUDA(h, cudaMemsetAsync(task_level, 0, (size_t)h->Np * h->D * sizeof(uint16_t), h->stream), "schedule scratch");
-  SW_CUDA(h, h->ops->schedule_seed(p, h->stream), "schedule seed kernel");
-  std::vector<uint32_t> lvl = {0};
-  unsigned long long tail = 0;
-  SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
-  SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule seed");
-  uint32_t begin = 0;
-  uint32_t round = 0;
-  while (tail > begin) {
-    const uint32_t end = (uint32_t)tail;
-    lvl.push_back(end);
-    if (round + 1 >= 0xffffu) return h->fail(SW_ERR_UNSUPPORTED, "dependency graph deeper than 65534 levels");
-    SW_CUDA(h, h->ops->kahn_round(p, begin, end, task_level, round, h->stream), "schedule round kernel");
-    ++round;
-    SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
-    SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule round");
-    begin = end;
-  }
-  uint32_t err = 0;
-  SW_CUDA(h, cudaMemcpy(&err, &p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
-  if (tail != total || err != 0) {
-    // cyclic dependency graph: no schedule.  The push path falls back to the
-    // dependency-driven queue; the pull path visits tasks in id order and its waits run
-    // out, so either reports the stall at the first sweep, where the reference deadlocks.
-    p.num_sched_levels = 0;
-    if (h->ops->pull) {
-      std::vector<uint32_t> ids;
-      ids.reserve(total);
-      for (uint32_t d = 0; d < (uint32_t)h->D; ++d)
-        for (uint32_t c = 0; c < (uint32_t)h->N; ++c) ids.push_back(d * h->Np + c);
-      SW_CUDA(h, cudaMemcpy(p.order, ids.data(), ids.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "order");
-    }
-    SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
-    return SW_OK;
-  }
-  // The positions: the directions are cut into `groups` contiguous groups, each group's
-  // tasks listed after the previous group's, by Kahn level, in task-id order within a
-  // level.  Directions never depend on one another, so this is a topological order, and
-  // its segments (one per non-empty (group, level)) are levels of a valid levelled
-  // schedule.  Fewer directions per level keep the words a level reads (written one or a
-  // few levels before) in L2 on large grids.  The order is a stable counting sort on
-  // the host, so every handle on the same grid gets the same schedule: the pull path's
-  // words are indexed by schedule position, and checkpoints hold them in that order.
-  const size_t L = lvl.size() - 1;
-  const int groups = schedule_dir_groups(h->D, total, L);
-  std::vector<uint32_t> seg = {0};
-  {
-    std::vector<uint16_t> tl((size_t)h->Np * h->D);
-    SW_CUDA(h, cudaMemcpy(tl.data(), task_level, tl.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost),
-            "read task levels");
-    std::vector<uint32_t> order(total);
-    uint64_t base = 0;
-    for (int g = 0; g < groups; ++g) {
-      const uint64_t d0 = (uint64_t)h->D * g / groups, d1 = (uint64_t)h->D * (g + 1) / groups;
-      const std::vector<uint64_t> n =
-          stable_level_order(tl.data(), h->Np, (uint32_t)h->N, d0 * h->Np, d1 * h->Np, L, base, order.data());
-      for (size_t l = 0; l < L; ++l)
-        if (n[l]) {
-          base += n[l];
-          seg.push_back((uint32_t)base);
-        }
-    }
-    if (base != total) return h->fail(SW_ERR_CUDA, "schedule order incomplete");
-    SW_CUDA(h, cudaMemcpy(p.order, order.data(), order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
-            "upload order");
-  }
-  uint32_t* d_lvl;
-  // padded to a multiple of four entries: the staged wavefront kernel copies them whole
-  const size_t lvl_words = (seg.size() + 3) & ~(size_t)3;
-  if (!h->alloc(&d_lvl, lvl_words)) return h->fail(SW_ERR_OOM, "device allocation of the schedule failed");
-  SW_CUDA(h, cudaMemset(d_lvl, 0, lvl_words * sizeof(uint32_t)), "schedule");
-  SW_CUDA(h, cudaMemcpy(d_lvl, seg.data(), seg.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload schedule");
-  p.lvl_words = (uint32_t)lvl_words;
-  p.lvl = d_lvl;
-  p.num_sched_levels = (uint32_t)(seg.size() - 1);
-  h->stats_schedule_levels = (uint32_t)L;  // the dependency depth
-  uint64_t hash = 0xcbf29ce484222325ull;  // FNV-1a over the group count and the offsets
+  uint64_t hash = 0xcbf29ce484222325ull;  // FNV-1a over the state kind, spaces, groups and offsets
   auto mix = [&](uint32_t v) {
     for (int k = 0; k < 4; ++k) hash = (hash ^ ((v >> (8 * k)) & 0xffu)) * 0x100000001b3ull;
   };
-  mix((uint32_t)groups);
-  for (uint32_t o : seg) mix(o);
+  mix((uint32_t)p.geo_mode);
+  mix((uint32_t)p.num_spaces);
+  uint32_t depth = 0;
+  for (int sp = 0; sp < p.num_spaces; ++sp) {
+    const swh::DevicePtrs q = swh::space_view(p, sp);
+    const uint64_t total = (uint64_t)h->N * (uint64_t)q.D;
+    SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
+    SW_CUDA(h, cudaMemsetAsync(task_level, 0, (size_t)h->Np * q.D * sizeof(uint16_t), h->stream), "schedule scratch");
+    SW_CUDA(h, h->ops->schedule_seed(q, h->stream), "schedule seed kernel");
+    std::vector<uint32_t> lvl = {0};
+    unsigned long long tail = 0;
+    SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
+    SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule seed");
+    uint32_t begin = 0;
+    uint32_t round = 0;
+    while (tail > begin) {
+      const uint32_t end = (uint32_t)tail;
+      lvl.push_back(end);
+      if (round + 1 >= 0xffffu) return h->fail(SW_ERR_UNSUPPORTED, "dependency graph deeper than 65534 levels");
+      SW_CUDA(h, h->ops->kahn_round(q, begin, end, task_level, round, h->stream), "schedule round kernel");
+      ++round;
+      SW_CUDA(h, cudaMemcpyAsync(&tail, &p.ctl->tail, sizeof(tail), cudaMemcpyDeviceToHost, h->stream), "read tail");
+      SW_CUDA(h, cudaStreamSynchronize(h->stream), "schedule round");
+      begin = end;
+    }
+    uint32_t err = 0;
+    SW_CUDA(h, cudaMemcpy(&err, &p.ctl->error, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
+    if (tail != total || err != 0) {
+      if (p.geo_mode) return h->fail(SW_ERR_STALLED, "the dependency graph has a cycle (compact state)");
+      // cyclic dependency graph: no schedule.  The push path falls back to the
+      // dependency-driven queue; the pull path visits tasks in id order and its waits run
+      // out, so either reports the stall at the first sweep, where the reference deadlocks.
+      p.num_sched_levels = 0;
+      if (h->ops->pull) {
+        std::vector<uint32_t> ids;
+        ids.reserve(total);
+        for (uint32_t d = 0; d < (uint32_t)h->D; ++d)
+          for (uint32_t c = 0; c < (uint32_t)h->N; ++c) ids.push_back(d * h->Np + c);
+        SW_CUDA(h, cudaMemcpy(p.order, ids.data(), ids.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "order");
+      }
+      SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
+      return SW_OK;
+    }
+    // The positions: the space's directions are cut into `groups` contiguous groups,
+    // each group's tasks listed after the previous group's, by Kahn level, in task-id
+    // order within a level.  Directions never depend on one another, so this is a
+    // topological order, and its segments (one per non-empty (group, level)) are levels
+    // of a valid levelled schedule.  Fewer directions per level keep the words a level
+    // reads (written one or a few levels before) in L2 on large grids; the compact
+    // state's geometry kernel pays a grid barrier per segment and keeps one group.  The
+    // order is a stable counting sort on the host, so every handle on the same grid
+    // gets the same schedule: the pull path's words are indexed by schedule position,
+    // and checkpoints hold them in that order.
+    const size_t L = lvl.size() - 1;
+    depth = std::max(depth, (uint32_t)L);
+    int groups = schedule_dir_groups(q.D, total, L);
+    if (p.geo_mode && !std::getenv("SUBSWEEP_DIR_GROUPS")) groups = 1;
+    std::vector<uint32_t> seg = {0};
+    {
+      std::vector<uint16_t> tl((size_t)h->Np * q.D);
+      SW_CUDA(h, cudaMemcpy(tl.data(), task_level, tl.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost),
+              "read task levels");
+      std::vector<uint32_t> order(total);
+      uint64_t base = 0;
+      for (int g = 0; g < groups; ++g) {
+        const uint64_t d0 = (uint64_t)q.D * g / groups, d1 = (uint64_t)q.D * (g + 1) / groups;
+        const std::vector<uint64_t> n =
+            stable_level_order(tl.data(), h->Np, (uint32_t)h->N, d0 * h->Np, d1 * h->Np, L, base, order.data());
+        for (size_t l = 0; l < L; ++l)
+          if (n[l]) {
+            base += n[l];
+            seg.push_back((uint32_t)base);
+          }
+      }
+      if (base != total) return h->fail(SW_ERR_CUDA, "schedule order incomplete");
+      SW_CUDA(h, cudaMemcpy(q.order, order.data(), order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+              "upload order");
+    }
+    uint32_t* d_lvl;
+    // padded to a multiple of four entries: the staged wavefront kernel copies them whole
+    const size_t lvl_words = (seg.size() + 3) & ~(size_t)3;
+    if (!h->alloc(&d_lvl, lvl_words)) return h->fail(SW_ERR_OOM, "device allocation of the schedule failed");
+    SW_CUDA(h, cudaMemset(d_lvl, 0, lvl_words * sizeof(uint32_t)), "schedule");
+    SW_CUDA(h, cudaMemcpy(d_lvl, seg.data(), seg.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+            "upload schedule");
+    p.space_lvl[sp] = d_lvl;
+    p.space_segments[sp] = (uint32_t)(seg.size() - 1);
+    p.space_lvl_words[sp] = (uint32_t)lvl_words;
+    mix((uint32_t)groups);
+    for (uint32_t o : seg) mix(o);
+  }
+  SW_CUDA(h, cudaMemsetAsync(p.ctl, 0, offsetof(swk::SweepCtl, tasks), h->stream), "reset control");
+  p.lvl = p.space_lvl[0];
+  p.num_sched_levels = p.space_segments[0];
+  p.lvl_words = p.space_lvl_words[0];
+  h->stats_schedule_levels = depth;  // the dependency depth
   h->schedule_hash = hash;
   return SW_OK;
 }
@@ -524,6 +555,11 @@ sw_status build_push_records(sw_handle* h) {
 sw_status build_records(sw_handle* h) {
   if (!h->ops->records) return SW_OK;
   swh::DevicePtrs& p = h->p;
+  if (p.geo_mode) {  // compact state: only the periodic fold's entries
+    SW_CUDA(h, h->ops->records(p, 1, nullptr, h->stream), "periodic fold entries");
+    SW_CUDA(h, cudaStreamSynchronize(h->stream), "periodic fold entries");
+    return SW_OK;
+  }
   const size_t nc = (size_t)((h->N * (int64_t)h->D + swk::kCompactChunk - 1) / swk::kCompactChunk);
   struct DeviceScratch {
     void* ptr = nullptr;
@@ -648,8 +684,14 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
   const int64_t N = grid->num_cells;
   if (N < 1 || N >= (int64_t)1 << 30) return create_fail(SW_ERR_INVALID_ARG, "num_cells must be in 1..2^30-1");
   const uint32_t Np = (uint32_t)((N + 31) / 32 * 32);
-  if ((uint64_t)Np * (uint64_t)D >= 0xffffffffull)
-    return create_fail(SW_ERR_UNSUPPORTED, "num_cells * directions must stay below 2^32 task ids");
+  // The FP64 path keeps 32-bit task ids; the mixed path splits larger grids into task
+  // spaces of fewer than 2^31 tasks each (compact state).
+  const uint64_t task_ids = (uint64_t)Np * (uint64_t)D;
+  if (P.precision == SW_PRECISION_FP64 && task_ids >= 0xffffffffull)
+    return create_fail(SW_ERR_UNSUPPORTED, "num_cells * directions must stay below 2^32 task ids (FP64 path)");
+  if (min_task_spaces(Np, D) == 0)
+    return create_fail(SW_ERR_UNSUPPORTED, "num_cells * directions needs more than %d task spaces of 2^31 tasks",
+                       swh::kMaxSpaces);
   if (!grid->row_ptr || !grid->nbr || !grid->kind || !grid->area || !grid->normal || !grid->volume || !grid->size)
     return create_fail(SW_ERR_INVALID_ARG, "grid array is NULL");
   if (!init->density || !init->ionized_hydrogen_fraction || !init->temperature || !init->source)
@@ -975,6 +1017,34 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     p.src_dir = d_src_dir;
   }
   // per-(cell, direction) state, [dir][cell]
+  // Compact state of the mixed path (no task records, upwind slots or inverse order;
+  // words by task; the geometry kernel): for grids of 2^31 tasks or more, for grids whose
+  // full state would not fit in the free device memory (records, slots, schedule, words,
+  // rates and the active lists of the levels: ~44 + 4 * faces per cell + 4 * (levels - 1)
+  // bytes per task), and on request (SUBSWEEP_COMPACT_STATE=1; SUBSWEEP_TASK_SPACES asks
+  // for more task spaces than the grid needs).
+  p.num_spaces = 1;
+  p.space_d0[0] = 0;
+  p.space_d0[1] = D;
+  if (h->ops->pull) {
+    const uint64_t tasks = (uint64_t)Np * (uint64_t)D;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) (void)cudaGetLastError();
+    const double full = (44.0 + 4.0 * (double)E / (double)N + 4.0 * (h->L - 1)) * (double)tasks;
+    bool geo = tasks >= kSpaceTasks || (free_b > 0 && full > 0.92 * (double)free_b);
+    if (const char* env = std::getenv("SUBSWEEP_COMPACT_STATE")) geo = geo || std::atoi(env) != 0;
+    if (geo) {
+      int spaces = min_task_spaces(Np, D);
+      if (const char* env = std::getenv("SUBSWEEP_TASK_SPACES"))
+        spaces = std::max(spaces, std::min(std::atoi(env), std::min(D, swh::kMaxSpaces)));
+      p.geo_mode = 1;
+      p.num_spaces = spaces;
+      for (int sp = 0; sp <= spaces; ++sp) p.space_d0[sp] = D * sp / spaces;
+      p.compact_mode = 2;  // every sweep visits every position
+      p.pull_variant = 0;
+      h->autotune = false;
+    }
+  }
   {
     const size_t nd = (size_t)Np * D;
     const size_t rb = (size_t)h->ops->rate_bytes;
@@ -995,7 +1065,10 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     float* per_pos = nullptr;
     const size_t chunks = (nd + swk::kCompactChunk - 1) / swk::kCompactChunk + 1;
     if (ok) ok = h->alloc(&chunk, chunks);
-    if (ok && pull)
+    if (ok && pull && p.geo_mode)  // compact state: words by task, no records or inverse order
+      ok = h->alloc(&qe, nd) && h->alloc(&act_counts, 32) && h->alloc(&cell_sweep, (size_t)h->Np) &&
+           h->alloc(&cellpack, (size_t)h->Np);
+    else if (ok && pull)
       ok = h->alloc(&qe, nd) && h->alloc(&rec, nd) && h->alloc(&act_counts, 32) && h->alloc(&pos_of_task, nd) &&
            h->alloc(&act_bits, (nd + 31) / 32) && h->alloc(&cell_sweep, (size_t)h->Np) &&
            h->alloc(&cellpack, (size_t)h->Np) &&
@@ -1004,7 +1077,7 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (ok && !pull) ok = h->alloc(&outg, nd * rb) && h->alloc(&pend, nd * rb) && h->alloc(&queue, nd);
     if (!ok) {
       h->fail(SW_ERR_OOM, "device allocation of the transport state (%zu MB) failed",
-              (pull ? 2 * rb + 41 : 4 * rb + 9) * nd >> 20);
+              (pull ? (p.geo_mode ? 2 * rb + 13 : 2 * rb + 41) : 4 * rb + 9) * nd >> 20);
       return bail(SW_ERR_OOM);
     }
     cudaMemset(inc, 0, nd * rb);
@@ -1522,11 +1595,28 @@ sw_status sw_get_dependency_counts(sw_handle* h, int32_t level, uint8_t* counts)
   uint8_t* d_counts = nullptr;
   size_t nb = (size_t)h->N * h->D;
   SW_CUDA(h, cudaMalloc(&d_counts, nb), "alloc");
-  // inactive cells' entries are not written by the counting kernel: start from zero
-  cudaError_t e = cudaMemsetAsync(d_counts, 0, nb, h->stream);
-  if (e == cudaSuccess) e = h->ops->init_counts(h->p, level, d_counts, false, h->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_counts, nb, cudaMemcpyDeviceToHost, h->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaError_t e = cudaSuccess;
+  if (h->p.num_spaces <= 1) {
+    // inactive cells' entries are not written by the counting kernel: start from zero
+    e = cudaMemsetAsync(d_counts, 0, nb, h->stream);
+    if (e == cudaSuccess) e = h->ops->init_counts(h->p, level, d_counts, false, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d_counts, nb, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  } else {  // task spaces: each space's [cell][its directions] block, interleaved on the host
+    std::vector<uint8_t> part;
+    for (int sp = 0; sp < h->p.num_spaces && e == cudaSuccess; ++sp) {
+      const swh::DevicePtrs v = swh::space_view(h->p, sp);
+      const size_t ns = (size_t)h->N * v.D;
+      part.resize(ns);
+      e = cudaMemsetAsync(d_counts, 0, ns, h->stream);
+      if (e == cudaSuccess) e = h->ops->init_counts(v, level, d_counts, false, h->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), d_counts, ns, cudaMemcpyDeviceToHost, h->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+      const int d0 = h->p.space_d0[sp];
+      for (int64_t c = 0; c < h->N && e == cudaSuccess; ++c)
+        std::memcpy(counts + (size_t)c * h->D + d0, part.data() + (size_t)c * v.D, v.D);
+    }
+  }
   cudaFree(d_counts);
   if (e != cudaSuccess) return h->cuda_fail(e, "dependency counts");
   return SW_OK;
@@ -1752,7 +1842,10 @@ sw_status sw_get_stats(sw_handle* h, sw_stats* out) {
   if (!h || !out) return SW_ERR_INVALID_ARG;
   h->stats.schedule_levels = h->stats_schedule_levels;
   h->stats.upwind_slots = h->stats_upwind_slots;
-  h->stats.pull_variant = h->ops->pull ? (h->p.pull_variant > 0 ? h->p.pull_variant : swh::kDefaultPullVariant) : 0;
+  h->stats.pull_variant =
+      h->ops->pull && !h->p.geo_mode ? (h->p.pull_variant > 0 ? h->p.pull_variant : swh::kDefaultPullVariant) : 0;
+  h->stats.task_spaces = h->p.geo_mode ? h->p.num_spaces : 0;
+  h->stats.device_bytes = h->device_bytes;
   *out = h->stats;
   return SW_OK;
 }

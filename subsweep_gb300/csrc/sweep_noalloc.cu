@@ -60,6 +60,10 @@ extern "C" sw_status sw_get_dependency_counts_noalloc(sw_handle* h, int32_t leve
   }
   if (v.device < 0 || v.device >= kMaxDevices)
     return swh::handle_fail(h, SW_ERR_UNSUPPORTED, "device ordinal above the scratch table");
+  if (v.p->num_spaces > 1)
+    return swh::handle_fail(h, SW_ERR_UNSUPPORTED,
+                            "sw_get_dependency_counts_noalloc: a handle split into task spaces (use "
+                            "sw_get_dependency_counts)");
   // the handle's device is current during the call; the caller's device afterwards
   swh::DeviceScope device_scope(v.device);
   if (device_scope.status != cudaSuccess) return cuda_failure(h, device_scope.status, "select device");

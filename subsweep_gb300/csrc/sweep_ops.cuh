@@ -13,6 +13,7 @@
 #include "sweep_pull_setup.cuh"
 #include "sweep_pull_lockstep.cuh"
 #include "sweep_pull_wavefront.cuh"
+#include "sweep_pull_geometry.cuh"
 #include "sweep_pull_fold.cuh"
 #else
 #include "sweep_push_records.cuh"
@@ -245,6 +246,7 @@ swk::PullArgs pull_args(const DevicePtrs& p, int level) {
   a.cellpack = static_cast<const uint2*>(p.cellpack);
   a.per_pos = p.per_pos;
   a.pos_of_task = p.pos_of_task;
+  a.order = p.order;
   return a;
 }
 
@@ -253,6 +255,15 @@ uint32_t num_chunks(const DevicePtrs& p) {
 }
 
 cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_off, cudaStream_t s) {
+  if (p.geo_mode) {  // compact state: no records or slots; the fold's periodic entries, space by space
+    if (phase != 1 || p.n_periodic_cells == 0) return cudaSuccess;
+    for (int sp = 0; sp < p.num_spaces; ++sp) {
+      const DevicePtrs v = space_view(p, sp);
+      swk::k_fold_build<<<grid_for((int64_t)v.n_periodic_cells * v.D, 256), 256, 0, s>>>(
+          pull_args(v, 0), v.periodic_cells, v.n_periodic_cells, v.fold_cnt, static_cast<uint2*>(v.fold_slots));
+    }
+    return cudaGetLastError();
+  }
   swk::PullArgs a = pull_args(p, 0);
   uint4* rec = static_cast<uint4*>(p.pull_rec);
   const uint32_t nc = num_chunks(p);
@@ -373,7 +384,27 @@ cudaError_t staged_layout(const DevicePtrs& p, uint32_t* cap, size_t* smem) {
   return cudaSuccess;
 }
 
+// compact state: the geometry kernel over every position, one task space after another
+cudaError_t sweep_pull_geo(const DevicePtrs& p, int level, cudaStream_t s) {
+  const void* fn = (const void*)swk::k_sweep_pull_geo<4>;
+  int grid = 0;
+  cudaError_t e = coop_grid(p, fn, &grid);
+  if (e != cudaSuccess) return e;
+  for (int sp = 0; sp < p.num_spaces; ++sp) {
+    const DevicePtrs v = space_view(p, sp);
+    if (v.num_sched_levels == 0) continue;
+    swk::PullArgs a = pull_args(v, level);
+    e = cudaMemsetAsync(&p.ctl->head, 0, sizeof(p.ctl->head), s);  // barrier arrivals
+    if (e != cudaSuccess) return e;
+    void* args[] = {&a};
+    e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(swk::kGeoThreads), args, 0, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {
+  if (p.geo_mode) return sweep_pull_geo(p, level, s);
   swk::PullArgs a = pull_args(p, level);
   const int variant = pull_variant(&p);
   if (p.sparse_sweep) {
@@ -432,6 +463,17 @@ cudaError_t fold_pull(const DevicePtrs& p, cudaStream_t s) {
     changed = p.fold_changed;
     swk::k_fold_mark<<<grid_for(p.n_periodic_cells, 256), 256, 0, s>>>(a, p.periodic_cells, p.n_periodic_cells,
                                                                         changed);
+  }
+  if (p.geo_mode) {  // compact state: the entries of each task space
+    for (int sp = 0; sp < p.num_spaces; ++sp) {
+      const DevicePtrs v = space_view(p, sp);
+      swk::PullArgs av = pull_args(v, 0);
+      av.per_pos = nullptr;
+      swk::k_fold_pull<<<dim3(grid.x, v.D), 256, 0, s>>>(av, static_cast<float*>(v.periodic), v.periodic_cells,
+                                                         v.n_periodic_cells, v.fold_cnt,
+                                                         static_cast<const uint2*>(v.fold_slots), changed);
+    }
+    return cudaGetLastError();
   }
   swk::k_fold_pull<<<grid, 256, 0, s>>>(a, static_cast<float*>(p.periodic), p.periodic_cells, p.n_periodic_cells,
                                         p.fold_cnt, static_cast<const uint2*>(p.fold_slots), changed);

@@ -70,7 +70,10 @@ struct PullArgs {
   // staged wavefront kernel
   const uint2* cellpack;      // per cell: {(float) attenuation bits or kInactiveCell, source / D bits}
   float* per_pos;             // periodic source of every position (written by the fold)
+  // schedule position of every task, or null in the compact state, whose words are
+  // indexed by task
   const uint32_t* pos_of_task;
+  const uint32_t* order;      // compact state: the task at every schedule position
 };
 
 // cellpack.x of a cell that is not active in the sweep (no attenuation is computed)
@@ -159,6 +162,11 @@ __device__ __forceinline__ unsigned long long rec_offset(const uint4& r) {
 __device__ __forceinline__ uint32_t rec_count(const uint4& r) { return r.w & 0x7fu; }
 __device__ __forceinline__ uint32_t rec_dir(const uint4& r) { return (r.w >> 7) & 0x7fu; }
 __device__ __forceinline__ bool rec_periodic(const uint4& r) { return (r.w & kRecPeriodic) != 0u; }
+
+// index of task t's word: its schedule position, or t in the compact state
+__device__ __forceinline__ size_t word_of_task(const PullArgs& a, size_t t) {
+  return a.pos_of_task ? (size_t)a.pos_of_task[t] : t;
+}
 
 // commit of the task with record r at position p
 __device__ __forceinline__ void commit_slot(const PullArgs& a, size_t p, const uint4& r, unsigned long long word,

@@ -19,7 +19,7 @@ __device__ __forceinline__ float gather_in(const PullArgs& a, uint32_t c, uint32
     if ((g.w >> kKindShift) != want) continue;
     const float s = face_eff(g, fx, fy, fz, a.geo64 + f, dx, dy, dz);
     if (s < 0.f)
-      in = fmaf(-s, __uint_as_float((uint32_t)*word_ptr(a.qe, a.pos_of_task[(size_t)d * a.Np + (g.w & kNbrMask)])),
+      in = fmaf(-s, __uint_as_float((uint32_t)*word_ptr(a.qe, word_of_task(a, (size_t)d * a.Np + (g.w & kNbrMask)))),
                 in);
   }
   return in;
@@ -29,7 +29,7 @@ __device__ __forceinline__ float gather_in(const PullArgs& a, uint32_t c, uint32
 // faces and every direction, the flux arriving through its LOCAL_PERIODIC upwind faces.
 // Entry e = d * n_cells + (index of the cell in `cells`).  The upwind periodic faces of
 // an entry are precomputed once per grid (k_fold_build: up to kFoldSlots of them, in
-// face order, as {upwind task's schedule position, |area n . d|}); an entry with more is
+// face order, as {upwind task's word index, |area n . d|}); an entry with more is
 // gathered from the geometry.  Both sum in face order with the same roundings.
 constexpr int kFoldSlots = 4;
 constexpr uint8_t kFoldOverflow = 0xffu;
@@ -48,7 +48,8 @@ __global__ void k_fold_build(PullArgs a, const uint32_t* cells, uint32_t n_cells
       const float sf = face_eff(g, fx, fy, fz, a.geo64 + f, dx, dy, dz);
       if (!(sf < 0.f)) continue;
       if (n < (uint32_t)kFoldSlots)
-        slots[e * kFoldSlots + n] = make_uint2(a.pos_of_task[d * a.Np + (g.w & kNbrMask)], __float_as_uint(-sf));
+        slots[e * kFoldSlots + n] =
+            make_uint2((uint32_t)word_of_task(a, (size_t)d * a.Np + (g.w & kNbrMask)), __float_as_uint(-sf));
       ++n;
     }
     cnt[e] = n > (uint32_t)kFoldSlots ? kFoldOverflow : (uint8_t)n;
@@ -114,7 +115,7 @@ __device__ __forceinline__ float current_incoming(const PullArgs& a, uint32_t c,
                                                   bool cell_is_current) {
   const size_t t = (size_t)d * a.Np + c;
   if (cell_is_current) return a.inc[t];
-  if ((uint32_t)(*word_ptr(a.qe, a.pos_of_task[t]) >> 32) == (last_epoch << 1)) return a.inc[t];  // solved
+  if ((uint32_t)(*word_ptr(a.qe, word_of_task(a, t)) >> 32) == (last_epoch << 1)) return a.inc[t];  // solved
   return gather_in(a, c, d, false);
 }
 
@@ -160,7 +161,7 @@ __global__ void k_export_pull(PullArgs a, uint32_t last_epoch, int which, double
         const float s = face_eff(a.geo16[f], fx, fy, fz, a.geo64 + f, dx, dy, dz);
         if (s > 0.f) area_down += s;
       }
-      v = __uint_as_float((uint32_t)*word_ptr(a.qe, a.pos_of_task[t])) * area_down;
+      v = __uint_as_float((uint32_t)*word_ptr(a.qe, word_of_task(a, t))) * area_down;
     }
     out[i] = (double)v * rate_scale;
   }

@@ -1,0 +1,111 @@
+// The geometry pull sweep kernel of the compact state (pull path).
+// Part of the pull-form transport of the mixed path; the shared definitions
+// (PullArgs, words, records) are in sweep_pull.cuh, the grid barrier in
+// sweep_pull_wavefront.cuh.
+#pragma once
+
+#include "sweep_pull.cuh"
+#include "sweep_pull_wavefront.cuh"
+
+namespace swk {
+
+// ---------------------------------------------------------------------------------------
+// Compact state: grids whose per-position records and upwind slots (~78 bytes per task)
+// do not fit next to the rest of the state, or whose tasks exceed 32-bit ids, keep only
+// the words (by task), the incoming and periodic rates and the schedule.  The sweep
+// then classifies each task's faces itself, as the record and slot kernels do once per
+// grid: one thread per task, segment by segment of one task space's levelled schedule,
+// with a grid barrier between segments (cooperative launch), so every upwind word is
+// final when it is read and no readiness test is needed.  Every position of the space
+// is visited; a task whose cell is inactive in the sweep keeps its word (its flux
+// persists, as in the reference), and nothing in this state tests sweep numbers inside
+// a sweep.
+//
+// A task walks its cell's faces in face order: the FP32 effective area s of each face
+// (exact sign as everywhere), s > 0 summed into the total downwind area, each upwind
+// LOCAL face k adding |s| q(n, d) into partial k mod 8 by FMA, an upwind LOCAL_PERIODIC
+// face flagging the periodic source.  The faces are taken eight upwind faces at a time,
+// so eight upwind words are in flight per thread.  Partial sums, their combination
+// ((p0 + p1) + (p2 + p3)) + ((p4 + p5) + (p6 + p7)), 1 / A_down and the commit are those
+// of the record kernels, so both states give the same bits.
+constexpr int kGeoThreads = 256;
+
+__device__ __forceinline__ void geo_solve(const PullArgs& a, uint32_t t, uint32_t sweep, unsigned long long& solved) {
+  const uint32_t d = t / a.Np, c = t - d * a.Np;
+  const uint2 cp = __ldg(a.cellpack + c);  // {(float) attenuation or inactive mark, source / D}
+  if (cp.x == kInactiveCell) return;
+  const float fx = a.dir32[3 * d], fy = a.dir32[3 * d + 1], fz = a.dir32[3 * d + 2];
+  const double dx = a.dir64[3 * d], dy = a.dir64[3 * d + 1], dz = a.dir64[3 * d + 2];
+  const size_t dnp = (size_t)d * a.Np;
+  const uint32_t end = a.off[c + 1];
+  uint32_t f = a.off[c];
+  float part[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) part[j] = 0.f;
+  float area_down = 0.f;
+  bool periodic_up = false;
+  bool more = true;
+  while (more) {  // one round: the next eight upwind LOCAL faces
+    float w[8], q[8];
+    bool have[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      have[j] = false;
+      w[j] = 0.f;
+      q[j] = 0.f;
+      while (f < end) {
+        const uint4 g = __ldg(a.geo16 + f);
+        const float s = face_eff(g, fx, fy, fz, a.geo64 + f, dx, dy, dz);
+        ++f;
+        if (s > 0.f) {
+          area_down += s;
+        } else if (s < 0.f) {
+          const uint32_t kind = g.w >> kKindShift;
+          if (kind == kKindLocal) {
+            w[j] = -s;
+            q[j] = __uint_as_float((uint32_t)ld_relaxed_u64(word_ptr(a.qe, dnp + (g.w & kNbrMask))));
+            have[j] = true;
+            break;
+          }
+          if (kind == kKindPeriodic) periodic_up = true;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (have[j]) part[j] = fmaf(w[j], q[j], part[j]);
+    more = have[7] && f < end;
+  }
+  const float in = ((part[0] + part[1]) + (part[2] + part[3])) + ((part[4] + part[5]) + (part[6] + part[7]));
+  const float inv = area_down > 0.f ? 1.0f / area_down : 0.f;
+  const float per = periodic_up ? __ldcg(a.periodic + t) : 0.f;
+  const float rt = (in + __uint_as_float(cp.y)) + per;                  // Site::get_rate, site.rs:53-56
+  const float out = (rt < a.threshold) ? 0.f : rt * __uint_as_float(cp.x);  // get_outgoing_rate
+  a.inc[t] = in;
+  st_relaxed_u64(word_ptr(a.qe, t), pack_qe(out * inv, sweep));
+  ++solved;
+}
+
+// grid: every block resident (cooperative); ctl->head zeroed before the launch
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kGeoThreads, kMinBlocks) k_sweep_pull_geo(PullArgs a) {
+  __shared__ int flag;
+  const uint32_t T = gridDim.x * kGeoThreads;
+  const uint32_t j = blockIdx.x * kGeoThreads + threadIdx.x;
+  const uint32_t L = a.num_sched;
+  const uint32_t sweep = sweep_number(a);
+  unsigned long long solved = 0;
+  for (uint32_t k = 0; k < L; ++k) {
+    const uint32_t lo = __ldg(a.lvl + k), hi = __ldg(a.lvl + k + 1);
+    for (uint32_t i = lo + j; i < hi; i += T) geo_solve(a, __ldg(a.order + i), sweep, solved);
+    if (k + 1 < L && !wave_barrier(a, (unsigned long long)(k + 1) * gridDim.x, &flag)) break;
+  }
+  const uint32_t lane = threadIdx.x & 31;
+  for (int o = 16; o > 0; o >>= 1) solved += __shfl_xor_sync(0xffffffffu, solved, o);
+  if (lane == 0 && solved) {
+    atomicAdd(&a.ctl->tasks, solved);
+    atomicAdd(&a.ctl->attempts, solved);
+  }
+}
+
+}  // namespace swk

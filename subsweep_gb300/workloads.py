@@ -27,6 +27,8 @@ and the field ends at the source cells.  `thick=True` keeps that
   C4  256^3 cells of 750 pc, n_H = exp(GRF), P(k) ~ k^-2, ln-sigma 1.5, mean 2e-4
       (median tau 0.3), 1000 sources at the densest cells with rates proportional
       to density (1e52 total), 84 directions, 4 levels, threshold 1e-5 photons/s
+  C5  384^3 cells of 750 pc, C4's field with ln-sigma 2.0, 4000 sources (4e52
+      total), 84 directions, 6 levels, threshold 1e-5 photons/s, 20 steps of 1 Myr
 Any configuration can be scaled down (`n_per_side`) for tests.
 """
 from __future__ import annotations
@@ -114,6 +116,10 @@ def label(name: str, n_per_side: int | None = None, num_directions: int | None =
     if name == "c4":
         n, d, lv = n_per_side or 256, num_directions or 84, num_levels or 4
         return f"C4 periodic jittered-lattice Voronoi {n}^3 GRF{_cells(thick, C4_CELL)}, {d} dirs, {lv} levels"
+    if name == "c5":
+        n, d, lv = n_per_side or 384, num_directions or 84, num_levels or 6
+        return (f"C5 periodic jittered-lattice Voronoi {n}^3 GRF ln-sigma 2.0{_cells(thick, C4_CELL)}, {d} dirs, "
+                f"{lv} levels")
     raise ValueError(f"unknown workload {name}")
 
 
@@ -210,7 +216,8 @@ def gaussian_random_field(m: int, ln_sigma: float, seed: int) -> np.ndarray:
 
 def c4_grf(n_per_side: int = 256, seed: int = 4, ln_sigma: float = 1.5, num_sources: int = 1000,
            num_directions: int = 84, num_levels: int = 4, nthreads: int = 0, grid_device: str = "host",
-           thick: bool = False, voronoi=None) -> Workload:
+           thick: bool = False, voronoi=None, total_rate: float = 1e52, steps: int = 4,
+           name: str = "c4") -> Workload:
     box = _cell(thick, C4_CELL) * n_per_side
     pts = gridmod.jittered_lattice(n_per_side, box, 0.25, seed)
     g = _voronoi(pts, box, nthreads, grid_device, voronoi)
@@ -222,12 +229,25 @@ def c4_grf(n_per_side: int = 256, seed: int = 4, ln_sigma: float = 1.5, num_sour
     n_h *= 2e-4 / n_h.mean()
     peaks = np.argsort(n_h)[-num_sources:]
     src = np.zeros(n)
-    src[peaks] = n_h[peaks] / n_h[peaks].sum() * 1e52
+    src[peaks] = n_h[peaks] / n_h[peaks].sum() * total_rate
     params = SweepParameters(directions=num_directions, num_timestep_levels=num_levels, periodic=True,
                              max_timestep=1.0 * MEGAYEAR, significant_rate_threshold=THRESHOLD)
-    return Workload(label("c4", n_per_side, num_directions, num_levels, thick), params, g,
+    return Workload(label(name, n_per_side, num_directions, num_levels, thick), params, g,
                     mass_density_from_number_density(n_h), np.full(n, 1e-10),
-                    np.full(n, 1e4), src, steps=4)
+                    np.full(n, 1e4), src, steps=steps)
+
+
+def c5_grf(n_per_side: int = 384, seed: int = 5, num_directions: int = 84, num_levels: int = 6,
+           nthreads: int = 0, grid_device: str = "host", thick: bool = False, voronoi=None) -> Workload:
+    """C5, the stress configuration: C4's generator (750 pc cells, exp of a Gaussian random
+    field with P(k) ~ k^-2, mean n_H 2e-4 cm^-3, sources at the density peaks with rates
+    proportional to the local density) at 384^3 with ln-sigma 2.0, 4000 sources (their
+    total scaled with the count from C4's 1e52 photons/s for 1000), 84 directions, 6
+    levels, threshold 1e-5 photons/s, 20 steps of 1 Myr (final time 20 Myr).  Its 4.76 G
+    tasks exceed 32-bit task ids: the mixed path runs it in the compact state."""
+    return c4_grf(n_per_side=n_per_side, seed=seed, ln_sigma=2.0, num_sources=4000, num_directions=num_directions,
+                  num_levels=num_levels, nthreads=nthreads, grid_device=grid_device, thick=thick, voronoi=voronoi,
+                  total_rate=4e52, steps=20, name="c5")
 
 
 def cartesian_column(n: int, cell_size: float, n_h: float, source_rate: float, num_levels: int = 1,

@@ -145,27 +145,38 @@ def test_stats_fields_used_by_smoke_and_bench():
     names = {n for n, _ in _native.SwStats._fields_}
     for k in ("tasks", "chem_cells", "level_sweeps", "step_ms", "transport_kernel_ms", "transport_launches",
               "kernel_launches", "levelled_sweeps", "schedule_levels", "transport_attempts", "chem_attempts",
-              "sweep_ms", "chem_ms", "level_ms", "pull_variant", "graph_launches"):
+              "sweep_ms", "chem_ms", "level_ms", "pull_variant", "graph_launches", "task_spaces"):
         assert k in names, k
 
 
-def test_c5_size_rejected_before_any_allocation():
-    """The C5 stress configuration (384^3 cells x 84 directions = 4.76 G tasks) exceeds the
-    32-bit task ids: sw_create rejects it from the sizes alone, before reading an array
-    or touching the device."""
+def _create_sized(num_cells, directions, precision):
     lib = _native.load_gpu()
     p = _native.SwParams()
     assert lib.sw_default_params(ctypes.byref(p)) == 0
-    p.num_directions = 84
-    p.precision = _native.SW_PRECISION_MIXED
+    p.num_directions = directions
+    p.precision = precision
     g = _native.SwGridCsr()
-    g.num_cells = 384 ** 3  # arrays left NULL: never read
+    g.num_cells = num_cells  # arrays left NULL: never read
     init = _native.SwCellInit()
     h = ctypes.c_void_p()
     st = lib.sw_create(ctypes.byref(p), ctypes.byref(g), ctypes.byref(init), ctypes.byref(h))
-    assert st == _native.SW_ERR_UNSUPPORTED
     assert not h.value
-    assert b"2^32" in lib.sw_last_error(None)
+    return st, lib.sw_last_error(None)
+
+
+def test_task_id_limits_checked_before_any_allocation():
+    """The C5 stress configuration (384^3 cells x 84 directions = 4.76 G tasks) exceeds
+    32-bit task ids.  The FP64 path rejects it from the sizes alone; the mixed path
+    accepts the sizes (its compact state splits the directions into task spaces) and
+    stops at the NULL arrays, before reading one or touching the device; a grid that
+    would need more than eight task spaces is rejected."""
+    directions = 84
+    st, msg = _create_sized(384 ** 3, directions, _native.SW_PRECISION_FP64)
+    assert st == _native.SW_ERR_UNSUPPORTED and b"2^32" in msg
+    st, msg = _create_sized(384 ** 3, directions, _native.SW_PRECISION_MIXED)
+    assert st == _native.SW_ERR_INVALID_ARG and b"NULL" in msg
+    st, msg = _create_sized((1 << 30) - 1, directions, _native.SW_PRECISION_MIXED)
+    assert st == _native.SW_ERR_UNSUPPORTED and b"task spaces" in msg
 
 
 def test_no_device_fails_loudly():
