@@ -340,9 +340,9 @@ constexpr int kTuneVariants[] = {122, 143, 344};
 
 // cooperative grid of a kernel: its occupancy limit (capped by
 // SUBSWEEP_LEVEL_BLOCKS_PER_SM) on every SM
-cudaError_t coop_grid(const DevicePtrs& p, const void* fn, int* grid) {
+cudaError_t coop_grid(const DevicePtrs& p, const void* fn, int* grid, int threads = swk::kPullThreads) {
   int bps = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, swk::kPullThreads, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, threads, 0);
   if (e != cudaSuccess) return e;
   if (bps < 1) return cudaErrorInvalidConfiguration;
   if (p.level_bps_cap >= 1 && p.level_bps_cap < bps) bps = p.level_bps_cap;
@@ -384,23 +384,36 @@ cudaError_t staged_layout(const DevicePtrs& p, uint32_t* cap, size_t* smem) {
   return cudaSuccess;
 }
 
-// compact state: the geometry kernel over every position, one task space after another
+// compact state: the geometry kernel over every position of every task space, one
+// launch (segment k of all spaces between two grid barriers)
 cudaError_t sweep_pull_geo(const DevicePtrs& p, int level, cudaStream_t s) {
-  const void* fn = (const void*)swk::k_sweep_pull_geo<4>;
+  static_assert(swk::kGeoMaxSpaces >= kMaxSpaces, "a task space per entry");
+  const void* fn = (const void*)swk::k_sweep_pull_geo<1>;
   int grid = 0;
-  cudaError_t e = coop_grid(p, fn, &grid);
+  cudaError_t e = coop_grid(p, fn, &grid, swk::kGeoThreads);
   if (e != cudaSuccess) return e;
+  swk::GeoArgs g{};
+  g.a = pull_args(p, level);
+  g.num_spaces = p.num_spaces;
+  g.max_levels = 0;
   for (int sp = 0; sp < p.num_spaces; ++sp) {
     const DevicePtrs v = space_view(p, sp);
-    if (v.num_sched_levels == 0) continue;
-    swk::PullArgs a = pull_args(v, level);
-    e = cudaMemsetAsync(&p.ctl->head, 0, sizeof(p.ctl->head), s);  // barrier arrivals
-    if (e != cudaSuccess) return e;
-    void* args[] = {&a};
-    e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(swk::kGeoThreads), args, 0, s);
-    if (e != cudaSuccess) return e;
+    swk::GeoSpace& x = g.sp[sp];
+    x.order = v.order;
+    x.lvl = v.lvl;
+    x.num_levels = v.num_sched_levels;
+    x.qe = v.qe;
+    x.inc = static_cast<float*>(v.incoming);
+    x.periodic = static_cast<const float*>(v.periodic);
+    x.dir32 = v.dir32;
+    x.dir64 = v.dir64;
+    g.max_levels = std::max(g.max_levels, x.num_levels);
   }
-  return cudaSuccess;
+  if (g.max_levels == 0) return cudaSuccess;
+  e = cudaMemsetAsync(&p.ctl->head, 0, sizeof(p.ctl->head), s);  // barrier arrivals
+  if (e != cudaSuccess) return e;
+  void* args[] = {&g};
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(swk::kGeoThreads), args, 0, s);
 }
 
 cudaError_t sweep_pull(const DevicePtrs& p, int level, cudaStream_t s) {

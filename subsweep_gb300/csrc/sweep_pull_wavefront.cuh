@@ -34,14 +34,20 @@ __device__ __forceinline__ bool wave_barrier(const PullArgs& a, unsigned long lo
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
     atomicAdd(&a.ctl->head, 1ull);
     unsigned long long w0 = 0;
+    uint32_t spins = 0;
+    // the pollers share the arrivals' cache line: poll it alone, with a short sleep,
+    // and look at the clock and the error flag every 16th poll
     while (ld_relaxed64(&a.ctl->head) < target) {
-      const unsigned long long now = globaltimer_ns();
-      if (w0 == 0) w0 = now;
-      if (now - w0 > a.timeout_ns || *(volatile uint32_t*)&a.ctl->error != 0) {
-        atomicOr(&a.ctl->error, kErrStall);
-        ok = 0;
-        break;
+      if ((++spins & 15u) == 0) {
+        const unsigned long long now = globaltimer_ns();
+        if (w0 == 0) w0 = now;
+        if (now - w0 > a.timeout_ns || *(volatile uint32_t*)&a.ctl->error != 0) {
+          atomicOr(&a.ctl->error, kErrStall);
+          ok = 0;
+          break;
+        }
       }
+      __nanosleep(20);
     }
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
     *flag = ok;
