@@ -122,9 +122,24 @@ struct ChemSolver {
   bool has_floor;
   double floor_t, floor_x;
   bool clamp_invalid;
+  // Mixed path: the per-cell factors of the update, formed once per cell instead of once
+  // per attempt (prepare(); the FP64 path keeps the reference's expressions)
+  double nh_cell, k_cell, rate_per_volume, compton_cell, xx_cell;
+
+  __device__ void prepare() {
+    if (!kCarryNeutral) return;
+    nh_cell = density / Units::kProtonMass;
+    k_cell = (Units::kGamma - 1.0) * Units::kProtonMass / (density * Units::kBoltzmann);
+    rate_per_volume = rate / volume;
+    xx_cell = 2.727 / scale_factor;
+    const double x2 = xx_cell * xx_cell;
+    compton_cell = (1.017e-37 * (x2 * x2)) * Units::kErgsPerS;
+  }
 
   __device__ __forceinline__ double neutral() const { return kCarryNeutral ? y : (1.0 - x); }
-  __device__ __forceinline__ double nh() const { return density / Units::kProtonMass; }
+  __device__ __forceinline__ double nh() const {
+    return kCarryNeutral ? nh_cell : density / Units::kProtonMass;
+  }
   __device__ __forceinline__ double n_ionized() const { return nh() * x; }
   __device__ __forceinline__ double n_neutral() const { return nh() * neutral(); }
   __device__ __forceinline__ double mu() const { return 1.0 / (x + 1.0); }
@@ -152,10 +167,8 @@ struct ChemSolver {
     const double nhi = n_ionized();
     const Fits32 f = fits32((float)t);
     const double u = Units::kErgsCentimetersCubedPerS;
-    const double xx = 2.727 / scale_factor;
-    const double x2 = xx * xx;
-    const double compton = (1.017e-37 * (x2 * x2) * (t - xx)) * Units::kErgsPerS;
-    const double dcompton = (1.017e-37 * (x2 * x2)) * Units::kErgsPerS;
+    const double compton = compton_cell * (t - xx_cell);
+    const double dcompton = compton_cell;
     const double coll = ((double)f.exc + 1.27e-21 * (double)f.fit) * u * ne * nhn;
     const double dcoll = ((double)f.dexc + 1.27e-21 * (double)f.fitd) * u * ne * nhn;
     lambda_c = coll + ((double)f.recc + (double)f.brems) * u * ne * nhi + compton * ne;
@@ -217,25 +230,25 @@ struct ChemSolver {
     return 1.0 - exp(-n_neutral() * Units::kSigma * length);
   }
 
-  // 304-310 (+ photoheating_rate 321-325)
-  __device__ double temperature_change(double timestep, double absorbed) const {
-    double k = (Units::kGamma - 1.0) * Units::kProtonMass / (density * Units::kBoltzmann);
-    double heating, lc, dlc;
+  // 304-310 (+ photoheating_rate 321-325); m = mu() of the attempt
+  __device__ double temperature_change(double timestep, double absorbed, double m) const {
+    double k, heating, lc, dlc;
     if (kCarryNeutral) {
-      heating = ((rate * absorbed) / volume) * (Units::kPhotonAverageEnergy - Units::kRydberg);
+      k = k_cell;
+      heating = (rate_per_volume * absorbed) * (Units::kPhotonAverageEnergy - Units::kRydberg);
       cooling32(lc, dlc);
     } else {
+      k = (Units::kGamma - 1.0) * Units::kProtonMass / (density * Units::kBoltzmann);
       heating = ((timestep * rate * absorbed) / volume) * (Units::kPhotonAverageEnergy - Units::kRydberg) / timestep;
       cooling(lc, dlc);
     }
     double lambda = heating - lc;
     double dlambdadt = -dlc;
-    double m = mu();
     return k * m * lambda * timestep / (1.0 - k * m * dlambdadt * timestep);
   }
   // 334-354 (+ photoionization_rate 327-332), case B rate 175-194 at the current
   // (already updated) temperature
-  __device__ double ionized_fraction_change(double timestep, double absorbed) const {
+  __device__ double ionized_fraction_change(double timestep, double absorbed, double m) const {
     const double t = temperature;
     double n_h = nh();
     double ne = n_ionized();
@@ -247,7 +260,7 @@ struct ChemSolver {
       dalpha = (double)f.dalpha * Units::kCentimetersCubedPerS;
       fit = (double)f.fit;
       fitd = (double)f.fitd;
-      photo = (rate * absorbed) / (n_neutral() * volume);
+      photo = (rate_per_volume * absorbed) / n_neutral();
     } else {
       const double lambda = 315614.0 / t;
       const double dlambda_dt = -315614.0 / (t * t);
@@ -265,7 +278,6 @@ struct ChemSolver {
     double beta = (5.85e-11 * fit) * Units::kCentimetersCubedPerS;
     double dbeta = (5.85e-11 * fitd) * Units::kCentimetersCubedPerS;
     double c = beta * ne + photo;
-    double m = mu();
     double d = alpha * ne;
     double xhii = x;
     double rhsc = ne * t * m * 1.0 * dbeta;
@@ -303,11 +315,12 @@ struct ChemSolver {
   // try_timestep_update 371-392
   __device__ bool try_update(double timestep, double safety, Timescale& out) {
     const double absorbed = absorbed_fraction();
-    double tc = temperature_change(timestep, absorbed);
+    const double m = mu();  // both updates use the x of the attempt's start
+    double tc = temperature_change(timestep, absorbed, m);
     double rec_t;
     if (!accept(temperature, tc, safety, timestep, rec_t)) return false;
     temperature += tc;
-    double xc = ionized_fraction_change(timestep, absorbed);
+    double xc = ionized_fraction_change(timestep, absorbed, m);
     double rec_x;
     if (!accept(x, xc, safety, timestep, rec_x)) return false;
     x += xc;

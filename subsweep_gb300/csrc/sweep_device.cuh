@@ -741,6 +741,7 @@ __global__ void k_chemistry(ChemArgs<R> a) {
     s.floor_t = s.temperature;
     s.floor_x = s.x;
     s.clamp_invalid = false;
+    s.prepare();
     bool failed = false;
     const Timescale chem_ts = s.perform_timestep(timestep, a.safety, failed, attempts);
     failures += failed ? 1u : 0u;
