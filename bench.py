@@ -158,9 +158,9 @@ TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a level-0
 
 # FP64 work of one try_timestep_update attempt of the chemistry kernel (mixed path: rate
 # fits in FP32, the update in FP64), counted by ncu on the second chemistry launch of
-# the C4 generator at 64^3 (84.97 M attempts): 62.1 DFMA, 43.0 DMUL and 9.0 DADD thread
-# instructions per attempt, i.e. 2 * 62 + 43 + 9 FP64 flops.
-CHEM_FP64_FLOPS_PER_ATTEMPT = 2 * 62 + 43 + 9
+# the C4 generator at 64^3 (60.18 M attempts by the sweep trace): 55.2 DFMA, 41.1 DMUL
+# and 9.0 DADD thread instructions per attempt, i.e. 2 * 55 + 41 + 9 FP64 flops.
+CHEM_FP64_FLOPS_PER_ATTEMPT = 2 * 55 + 41 + 9
 
 
 def chemistry_figures(d: dict, res: dict) -> dict:
