@@ -55,8 +55,10 @@ struct GeoArgs {
 __device__ __forceinline__ void geo_solve(const PullArgs& a, const GeoSpace& sp, uint32_t t, uint32_t sweep,
                                           unsigned long long& solved) {
   const uint32_t d = t / a.Np, c = t - d * a.Np;
-  const uint2 cp = __ldg(a.cellpack + c);  // {(float) attenuation or inactive mark, source / D}
-  if (cp.x == kInactiveCell) return;
+  // inactive in this sweep: the level (1 byte per cell, L2-resident) decides before the
+  // cell pack (8 bytes per cell) is read; attenuation marks exactly these cells inactive
+  if (a.level[c] < (uint32_t)a.current_level) return;
+  const uint2 cp = __ldg(a.cellpack + c);  // {(float) attenuation, source / D}
   const float fx = sp.dir32[3 * d], fy = sp.dir32[3 * d + 1], fz = sp.dir32[3 * d + 2];
   const double dx = sp.dir64[3 * d], dy = sp.dir64[3 * d + 1], dz = sp.dir64[3 * d + 2];
   const size_t dnp = (size_t)d * a.Np;
