@@ -284,9 +284,9 @@ cudaError_t records(const DevicePtrs& p, int phase, unsigned long long* chunk_of
 
 // Variants of the pull kernel: the warp-lockstep kernel with its shape as parameters
 // (100 * prefetch depth (3: the next slots into L1 only) + 10 * lanes per task (2, 4, 8,
-// or 6 for 16) + blocks per SM, + 1000 with streaming loads of records and slots; 83 and
-// 84 name 183 and 184) and the level-synchronous wavefronts (72: registers, 78:
-// TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
+// or 6 for 16) + blocks per SM, + 1000 with streaming loads of records and slots, + 2000
+// with the next block's words loaded one block ahead (prefetch depth 2); 83 and 84 name
+// 183 and 184) and the level-synchronous wavefronts (72: registers, 78: TMA-staged).  SUBSWEEP_PULL_VARIANT picks one.
 
 const void* pull_kernel(int variant) {
   switch (variant) {
@@ -311,6 +311,8 @@ const void* pull_kernel(int variant) {
     case 1143: return (const void*)swk::k_sweep_pull_lockg<3, 4, 1, true>;
     case 1242: return (const void*)swk::k_sweep_pull_lockg<2, 4, 2, true>;
     case 1344: return (const void*)swk::k_sweep_pull_lockg<4, 4, 3, true>;
+    case 2242: return (const void*)swk::k_sweep_pull_lockg<2, 4, 2, false, true>;
+    case 2283: return (const void*)swk::k_sweep_pull_lockg<3, 8, 2, false, true>;
     case 72: return (const void*)swk::k_sweep_pull_wave<2>;
     case 78: return (const void*)swk::k_sweep_pull_staged;
     default: return nullptr;

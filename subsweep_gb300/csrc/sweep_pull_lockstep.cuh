@@ -34,19 +34,23 @@ __device__ __forceinline__ uint32_t cell_at(const PullArgs& a, uint32_t p) {
 // autotuner: G lanes per task (2, 4, 8 or 16: 16, 8, 4 or 2 tasks per warp block) and the
 // prefetch depth PF of the slots and cell data (1: the next block's, 2: also the one
 // after; 3: the next block's cell data, its slots only into L1) and CS, whether the
-// records and slots are loaded with the streaming (evict-first) cache hint.  Whatever
-// the shape, the incoming rate is summed in one fixed order, so every shape gives the
-// same bits: eight partial sums, partial j over the slots j, j + 8 (and
+// records and slots are loaded with the streaming (evict-first) cache hint, and SP
+// (with PF = 2), whether the next block's upwind words are loaded one block ahead, as
+// soon as its slots are in registers: a block whose words were already current then
+// commits without a round trip of its own, and a word that was not is loaded again.
+// Whatever the shape, the incoming rate is summed in one fixed order, so every shape
+// gives the same bits: eight partial sums, partial j over the slots j, j + 8 (and
 // j + 16, j + 24, ... for tasks with more than 16 upwind faces) by fused multiply-adds
 // in slot order, then combined pairwise as an eight-lane butterfly (xor 1, 2, 4).  With
 // G = 4 a lane holds partials j and j + 4 (xor 4 within the lane); with G = 2 lane j
 // holds partials j, j + 2, j + 4, j + 6 (xor 2 and 4 within the lane); with G = 16
 // lanes 8..15 hand their slot's weight and word to lanes 0..7.
-template <int kMinBlocks, int G, int PF, bool CS = false>
+template <int kMinBlocks, int G, int PF, bool CS = false, bool SP = false>
 __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(PullArgs a) {
   static_assert(G == 2 || G == 4 || G == 8 || G == 16, "2, 4, 8 or 16 lanes per task");
   static_assert(PF == 1 || PF == 2 || PF == 3, "prefetch depth 1 or 2, or 3: next slots into L1 only");
   static_assert(kPullGroup == 8 && kPullRounds == 2, "eight partial sums of two register slots");
+  static_assert(!SP || PF == 2, "words one block ahead need the slots two blocks ahead");
   constexpr uint32_t kGroups = 32 / G;
   constexpr int V = G <= 8 ? 8 / G : 1;  // partial sums per lane
   constexpr int S = G <= 8 ? 2 * V : 1;  // slots per lane in registers
@@ -113,6 +117,11 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
       if (cell_lane) load_cell(n1, cp1, per1);
     }
   }
+  // SP: the upwind words of the next block (slots s1), loaded during this block
+  unsigned long long xp[S], xq[S];
+#pragma unroll
+  for (int k = 0; k < S; ++k) xp[k] = xq[k] = 0ull;
+  bool pre = false;
   uint32_t solved = 0, attempts = 0;
   bool stop = false;
   while (!stop && b * kGroups < count) {
@@ -129,6 +138,14 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
       }
       if (idx(b + 3 * W) < count) nn = ld_rec(p3);
       if (idx(b + 4 * W) < count) pn = pull_pos(a, idx(b + 4 * W));
+      if constexpr (SP) {
+        if (idx(b + W) < count) {
+          const uint32_t n1_up = rec_count(n1);
+#pragma unroll
+          for (int k = 0; k < S; ++k)
+            if (slot_of(k) < n1_up) xq[k] = ld_relaxed_u64(word_ptr(a.qe, s1[k].x));
+        }
+      }
     } else {
       if (idx(b + W) < count) {
         if constexpr (PF == 3)
@@ -168,10 +185,18 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
     const bool big = n_up > 16u;
     unsigned long long w0 = 0;
     uint32_t wait_ns = 32;
+    bool first = true;
     while (true) {
+      if (SP && first && pre) {  // the words loaded during the previous block
 #pragma unroll
-      for (int k = 0; k < S; ++k)
-        if (need[k]) x[k] = ld_relaxed_u64(word_ptr(a.qe, s[k].x));
+        for (int k = 0; k < S; ++k)
+          if (need[k]) x[k] = xp[k];
+      } else {
+#pragma unroll
+        for (int k = 0; k < S; ++k)
+          if (need[k]) x[k] = ld_relaxed_u64(word_ptr(a.qe, s[k].x));
+      }
+      first = false;
       bool bad = false;
 #pragma unroll
       for (int k = 0; k < S; ++k) {
@@ -268,6 +293,11 @@ __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(P
       for (int k = 0; k < S; ++k) {
         s[k] = s1[k];
         s1[k] = sn[k];
+      }
+      if constexpr (SP) {
+#pragma unroll
+        for (int k = 0; k < S; ++k) xp[k] = xq[k];
+        pre = true;
       }
       cp = cp1;
       per = per1;

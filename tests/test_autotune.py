@@ -52,12 +52,14 @@ def _poisson_boxes():
                                 num_directions=32, num_levels=3)
 
 
-@pytest.mark.parametrize("variant", [83, 72, 78, 122, 322, 323, 143, 144, 164, 242, 264, 283, 343, 344, 384, 1084, 1143, 1242, 1344])
+@pytest.mark.parametrize("variant", [83, 72, 78, 122, 322, 323, 143, 144, 164, 242, 264, 283, 343, 344, 384, 1084, 1143, 1242, 1344,
+                                     2242, 2283])
 @pytest.mark.parametrize("grid", ["lattice", "poisson"])
 def test_variant_equals_default(variant, grid, monkeypatch):
     """Each transport variant (the lockstep kernel at 2, 4, 8 and 16 lanes per task,
     prefetch depths 1 to 3, 2 to 4 target blocks per SM, with and without streaming
-    loads; the level-synchronous wavefront and its fully TMA-staged form) against the
+    loads, with and without the next block's words loaded one block ahead; the
+    level-synchronous wavefront and its fully TMA-staged form) against the
     lockstep kernel with 8 lanes per task at 4 blocks per SM, bit for bit over steps
     with dense and sparse sweeps above level 0."""
     monkeypatch.delenv("SUBSWEEP_AUTOTUNE", raising=False)
