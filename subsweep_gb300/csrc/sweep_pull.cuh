@@ -92,11 +92,6 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   return WordRef(*const_cast<unsigned long long*>(p)).load(cuda::memory_order_relaxed);
 }
 
-// predicated form: returns 0 without touching memory when pred is false
-__device__ __forceinline__ unsigned long long ld_relaxed_u64_if(bool pred, const unsigned long long* p) {
-  return pred ? ld_relaxed_u64(p) : 0ull;
-}
-
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
   WordRef(*p).store(v, cuda::memory_order_relaxed);
 }
@@ -138,8 +133,8 @@ __device__ __forceinline__ float face_eff(const uint4& g, float fx, float fy, fl
 }
 
 constexpr int kPullThreads = 256;
-constexpr int kPullGroup = 8;   // lanes per task
-constexpr int kPullRounds = 2;  // slots per lane held in registers (tasks with <= 16 upwind faces)
+constexpr int kPullPartials = 8;   // partial sums of a task's incoming rate (slot j into partial j mod 8)
+constexpr int kPullRegSlots = 16;  // upwind slots a task holds in registers (more are read from memory)
 
 // t = d * Np + c  ->  (c, d) without a runtime integer division: FP32 estimate of the
 // quotient (t / Np <= 128, so it is off by at most one), then an exact correction.

@@ -10,9 +10,9 @@ namespace swk {
 // ---------------------------------------------------------------------------------------
 // Scheduled pull sweep (cooperative launch; every block resident).
 //
-// Groups of kPullGroup lanes visit the active positions in schedule order.  For its
-// current task a group gathers the upwind tasks' words through the task's slots (lane
-// l: slots l, l + 8, ...) and commits
+// Groups of G lanes (a shape parameter below) visit the active positions in schedule
+// order.  For its current task a group gathers the upwind tasks' words through the
+// task's slots and commits
 //   in = sum_slots |area n . d| q(n, d),   out = (in + source/D + periodic) * attenuation
 // (zero below the threshold), q = out / A_down, once every word carries the current
 // sweep number; otherwise it retries.  The next positions' records, slots and cell data
@@ -49,7 +49,7 @@ template <int kMinBlocks, int G, int PF, bool CS = false, bool SP = false>
 __global__ void __launch_bounds__(kPullThreads, kMinBlocks) k_sweep_pull_lockg(PullArgs a) {
   static_assert(G == 2 || G == 4 || G == 8 || G == 16, "2, 4, 8 or 16 lanes per task");
   static_assert(PF == 1 || PF == 2 || PF == 3, "prefetch depth 1 or 2, or 3: next slots into L1 only");
-  static_assert(kPullGroup == 8 && kPullRounds == 2, "eight partial sums of two register slots");
+  static_assert(kPullPartials == 8 && kPullRegSlots == 16, "eight partial sums over sixteen register slots");
   static_assert(!SP || PF == 2, "words one block ahead need the slots two blocks ahead");
   constexpr uint32_t kGroups = 32 / G;
   constexpr int V = G <= 8 ? 8 / G : 1;  // partial sums per lane
