@@ -27,6 +27,24 @@ int32_t sw_host_lowest_allowed(int32_t num_levels, int32_t advances);
  * range. */
 int32_t sw_host_check_checkpoint(const void* buffer, size_t bytes);
 
+/* The schedule positions sw_create lays out for one task space from the tasks' Kahn
+ * levels (task_level[t] for t = dir * np + cell, levels 0..levels-1; cells >= n are
+ * padding): the d directions cut into `groups` contiguous groups, each group's tasks
+ * after the previous group's, by level, in task-id order within a level.  Writes
+ * order[n * d] and the segment offsets seg[0..segments] (at most seg_cap entries);
+ * returns the number of segments, -1 on an invalid argument. */
+int64_t sw_host_schedule_order(const uint16_t* task_level, uint32_t np, uint32_t n, uint32_t d, int32_t levels,
+                               int32_t groups, uint32_t* order, uint32_t* seg, int64_t seg_cap);
+
+/* Task spaces of fewer than 2^31 tasks that sw_create splits the mixed path's
+ * directions into at the least (0: more than eight would be needed); -1 on an invalid
+ * argument. */
+int32_t sw_host_task_spaces(uint32_t np, int32_t d);
+
+/* Direction groups of the schedule for d directions, `tasks` tasks and `levels` Kahn
+ * levels (SUBSWEEP_DIR_GROUPS overrides); -1 on an invalid argument. */
+int32_t sw_host_dir_groups(int32_t d, uint64_t tasks, int64_t levels);
+
 #ifdef __cplusplus
 }
 #endif

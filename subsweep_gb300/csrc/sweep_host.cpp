@@ -337,6 +337,26 @@ static std::vector<uint64_t> stable_level_order(const uint16_t* level, uint32_t 
   return per_level;
 }
 
+// The positions of one task space: its D directions cut into `groups` contiguous
+// groups, each group's tasks after the previous group's, by Kahn level (`level`, L
+// levels), in task-id order within a level.  Writes order[N * D] and appends the end of
+// every non-empty (group, level) segment to seg (which starts with 0); returns the
+// number of positions written.
+static uint64_t grouped_level_order(const uint16_t* level, uint32_t Np, uint32_t N, uint32_t D, size_t L,
+                                    int groups, uint32_t* order, std::vector<uint32_t>& seg) {
+  uint64_t base = 0;
+  for (int g = 0; g < groups; ++g) {
+    const uint64_t d0 = (uint64_t)D * g / groups, d1 = (uint64_t)D * (g + 1) / groups;
+    const std::vector<uint64_t> n = stable_level_order(level, Np, N, d0 * Np, d1 * Np, L, base, order);
+    for (size_t l = 0; l < L; ++l)
+      if (n[l]) {
+        base += n[l];
+        seg.push_back((uint32_t)base);
+      }
+  }
+  return base;
+}
+
 // Compact state (mixed path): task spaces hold fewer than kSpaceTasks tasks each.  The
 // fewest spaces of evenly split directions that do, 0 when kMaxSpaces are not enough.
 constexpr uint64_t kSpaceTasks = 1ull << 31;
@@ -446,17 +466,8 @@ sw_status build_schedule(sw_handle* h) {
       SW_CUDA(h, cudaMemcpy(tl.data(), task_level, tl.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost),
               "read task levels");
       std::vector<uint32_t> order(total);
-      uint64_t base = 0;
-      for (int g = 0; g < groups; ++g) {
-        const uint64_t d0 = (uint64_t)q.D * g / groups, d1 = (uint64_t)q.D * (g + 1) / groups;
-        const std::vector<uint64_t> n =
-            stable_level_order(tl.data(), h->Np, (uint32_t)h->N, d0 * h->Np, d1 * h->Np, L, base, order.data());
-        for (size_t l = 0; l < L; ++l)
-          if (n[l]) {
-            base += n[l];
-            seg.push_back((uint32_t)base);
-          }
-      }
+      const uint64_t base =
+          grouped_level_order(tl.data(), h->Np, (uint32_t)h->N, (uint32_t)q.D, L, groups, order.data(), seg);
       if (base != total) return h->fail(SW_ERR_CUDA, "schedule order incomplete");
       SW_CUDA(h, cudaMemcpy(q.order, order.data(), order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
               "upload order");
@@ -1724,6 +1735,29 @@ static int32_t check_checkpoint(const void* buffer, size_t bytes, CheckpointHead
   for (int64_t c = 0; c < hd.num_cells; ++c)
     if (level[c] >= hd.num_levels) return 3;
   return 0;
+}
+
+int64_t sw_host_schedule_order(const uint16_t* task_level, uint32_t np, uint32_t n, uint32_t d, int32_t levels,
+                                int32_t groups, uint32_t* order, uint32_t* seg, int64_t seg_cap) {
+  if (!task_level || !order || !seg || n == 0 || np < n || d == 0 || levels < 1 || groups < 1 ||
+      groups > (int32_t)d || (uint64_t)np * d >= (1ull << 32))
+    return -1;
+  for (uint64_t t = 0; t < (uint64_t)np * d; ++t)
+    if (t % np < n && task_level[t] >= levels) return -1;
+  std::vector<uint32_t> s = {0};
+  grouped_level_order(task_level, np, n, d, (size_t)levels, groups, order, s);
+  for (size_t i = 0; i < s.size() && (int64_t)i < seg_cap; ++i) seg[i] = s[i];
+  return (int64_t)s.size() - 1;
+}
+
+int32_t sw_host_task_spaces(uint32_t np, int32_t d) {
+  if (np == 0 || d < 1) return -1;
+  return min_task_spaces(np, d);
+}
+
+int32_t sw_host_dir_groups(int32_t d, uint64_t tasks, int64_t levels) {
+  if (d < 1 || levels < 1) return -1;
+  return schedule_dir_groups(d, tasks, (size_t)levels);
 }
 
 int32_t sw_host_check_checkpoint(const void* buffer, size_t bytes) {

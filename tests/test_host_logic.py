@@ -100,3 +100,68 @@ def test_checkpoint_validation_rejects_bad_level_before_upload(lib):
     assert lib.sw_host_check_checkpoint(bytes(buf), len(buf)) == 1
     buf, _ = _checkpoint(num_cells=40, np_=32)
     assert lib.sw_host_check_checkpoint(bytes(buf), len(buf)) == 1
+
+
+def _schedule(lib, level, np_, n, d, levels, groups):
+    lib.sw_host_schedule_order.restype = ctypes.c_int64
+    lib.sw_host_schedule_order.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_int64]
+    order = np.zeros(n * d, np.uint32)
+    seg = np.zeros(groups * levels + 1, np.uint32)
+    k = lib.sw_host_schedule_order(level.ctypes.data, np_, n, d, levels, groups, order.ctypes.data,
+                                   seg.ctypes.data, seg.size)
+    return k, order, seg[:k + 1] if k >= 0 else seg
+
+
+@pytest.mark.parametrize("groups", [1, 2, 3, 5])
+def test_schedule_order_layout(lib, groups):
+    """The positions sw_create lays out: every task (padding cells excluded) once; the
+    direction groups one after another, each by level, in task-id order inside a
+    segment; every segment one (group, level); the layout is deterministic."""
+    rng = np.random.default_rng(groups)
+    n, np_, d, levels = 45, 64, 7, 9
+    level = rng.integers(0, levels, size=np_ * d).astype(np.uint16)
+    k, order, seg = _schedule(lib, level, np_, n, d, levels, groups)
+    tasks = np.array([t for t in range(np_ * d) if t % np_ < n], np.uint32)
+    assert k >= 1 and seg[0] == 0 and seg[-1] == n * d
+    np.testing.assert_array_equal(np.sort(order), tasks)
+    bounds = [d * g // groups for g in range(groups + 1)]  # direction groups: [d*g/G, d*(g+1)/G)
+    group_of = lambda t: next(g for g in range(groups) if bounds[g] <= t // np_ < bounds[g + 1])
+    keys = []
+    for s in range(k):
+        part = order[seg[s]:seg[s + 1]]
+        assert len(part) > 0 and np.all(np.diff(part.astype(np.int64)) > 0)  # task-id order
+        gs, ls = {group_of(int(t)) for t in part}, {int(level[t]) for t in part}
+        assert len(gs) == 1 and len(ls) == 1  # one (group, level) per segment
+        keys.append((gs.pop(), ls.pop()))
+    assert keys == sorted(keys) and len(set(keys)) == len(keys)
+    k2, order2, seg2 = _schedule(lib, level, np_, n, d, levels, groups)
+    assert k2 == k and np.array_equal(order2, order) and np.array_equal(seg2, seg)
+
+
+def test_schedule_order_rejects_bad_input(lib):
+    level = np.zeros(64 * 4, np.uint16)
+    assert _schedule(lib, level, 64, 40, 4, 3, 5)[0] == -1  # more groups than directions
+    level[3] = 7
+    assert _schedule(lib, level, 64, 40, 4, 3, 1)[0] == -1  # a level beyond the count
+
+
+def test_task_spaces_and_direction_groups(lib, monkeypatch):
+    """The compact state's task spaces (fewer than 2^31 tasks each) and the schedule's
+    direction groups (one per 40 K tasks of the average Kahn level) at the benchmark
+    configurations' sizes."""
+    lib.sw_host_task_spaces.restype = ctypes.c_int32
+    lib.sw_host_task_spaces.argtypes = [ctypes.c_uint32, ctypes.c_int32]
+    lib.sw_host_dir_groups.restype = ctypes.c_int32
+    lib.sw_host_dir_groups.argtypes = [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int64]
+    np_ = lambda n: (n + 31) // 32 * 32
+    assert lib.sw_host_task_spaces(np_(256 ** 3), 84) == 1  # C4: 1.41 G tasks
+    assert lib.sw_host_task_spaces(np_(384 ** 3), 84) == 3  # C5: 4.76 G tasks, 28 directions a space
+    assert lib.sw_host_task_spaces(np_((1 << 30) - 1), 84) == 0  # beyond eight spaces
+    assert lib.sw_host_task_spaces(0, 84) == -1
+    monkeypatch.delenv("SUBSWEEP_DIR_GROUPS", raising=False)
+    assert lib.sw_host_dir_groups(84, 256 ** 3 * 84, 4927) == 7  # C4 256^3: 286 K tasks per level
+    assert lib.sw_host_dir_groups(84, 64 ** 3 * 84, 1200) == 1  # 64^3: 18 K tasks per level
+    assert lib.sw_host_dir_groups(84, 10, 5) == 1
+    assert lib.sw_host_dir_groups(0, 10, 5) == -1
