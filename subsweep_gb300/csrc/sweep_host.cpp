@@ -1137,32 +1137,6 @@ sw_status sw_create(const sw_params* params, const sw_grid_csr* grid, const sw_c
     if (st == SW_OK) st = build_push_records(h);
     if (st != SW_OK) return bail(st);
   }
-  // SUBSWEEP_L2_PERSIST=1 (mixed path): keep the per-cell packs the transport gathers at
-  // random (8 B per cell) in the persisting part of L2, through an access-policy window
-  // on the handle's stream.  It sets the context's persisting-L2 limit, which the
-  // calling process shares, so it stays opt-in.
-  if (p.cellpack) {
-    const char* env = std::getenv("SUBSWEEP_L2_PERSIST");
-    int max_persist = 0, max_window = 0;
-    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, h->device);
-    cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, h->device);
-    if (env && env[0] == '1' && max_persist > 0 && max_window > 0) {
-      const size_t bytes = std::min((size_t)h->Np * sizeof(uint2), (size_t)max_window);
-      const size_t keep = std::min(bytes, (size_t)max_persist);
-      cudaStreamAttrValue v{};
-      v.accessPolicyWindow.base_ptr = p.cellpack;
-      v.accessPolicyWindow.num_bytes = bytes;
-      v.accessPolicyWindow.hitRatio = (float)((double)keep / (double)bytes);
-      v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-      v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-      if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, keep) != cudaSuccess ||
-          cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess)
-        (void)cudaGetLastError();  // a hint: run without it
-      if (h->trace)
-        std::fprintf(stderr, "subsweep L2 persisting window %zu of %zu bytes (limit %d, window %d)\n", keep, bytes,
-                     max_persist, max_window);
-    }
-  }
   *out = h;
   return SW_OK;
 }
