@@ -30,14 +30,19 @@ Arepo's face normals are not the exact bisector normals of the generators, so th
 upwind graph of a direction can contain cycles; `dependency_cycles` counts the tasks
 that no topological order reaches (`Sweep` would report SW_ERR_STALLED on them).
 
-Reading the HDF5 files needs h5py, which is not installed on these machines;
-`read_grid_file` raises ImportError then, and `from_connections` works on the arrays.
+`read_grid_file` reads the grid file and the snapshot with the package's own HDF5
+reader (subsweep_gb300.hdf5; no libhdf5 needed), converting Arepo's units to SI as the
+reference does; `read_initial_conditions` reads the gas state the sweep starts from.
 """
 from __future__ import annotations
 
+from typing import Optional
+
 import numpy as np
 
+from . import hdf5
 from .grid import Grid
+from .sweep import PROTON_MASS
 
 FACE_LOCAL, FACE_LOCAL_PERIODIC, FACE_BOUNDARY = 0, 1, 2
 
@@ -119,21 +124,76 @@ def from_connections(unique_ids, volume, id1, id2, connection_type, area, normal
                 periodic=bool(periodic))
 
 
-def read_grid_file(grid_path, snapshot_path, periodic: bool, density=None) -> Grid:
-    """Grid of an Arepo grid file (Id1, Id2, ConnectionType, Area, Normal) and the gas
-    cells of a snapshot (PartType0/ParticleIDs, Masses, and Density unless given).
-    Lengths, areas and volumes are returned as stored (code units); areas and normals
-    only enter the sweep through ratios, volumes through the cell size."""
-    import h5py  # not installed on these machines: ImportError
+def read_grid_file(grid_path, snapshot_paths, periodic: bool, cosmology: Optional[hdf5.Cosmology] = None) -> Grid:
+    """Grid of an Arepo grid file and the gas cells of a snapshot, in SI units.
 
-    with h5py.File(snapshot_path, "r") as f:
-        gas = f["PartType0"]
-        ids = gas["ParticleIDs"][...]
-        mass = gas["Masses"][...]
-        rho = gas["Density"][...] if density is None else np.asarray(density)
-    with h5py.File(grid_path, "r") as f:
-        return from_connections(ids, mass / rho, f["Id1"][...], f["Id2"][...], f["ConnectionType"][...],
-                                f["Area"][...], f["Normal"][...], periodic)
+    Follows `ReadSweepGridPlugin` and `read_grid_system`
+    (src/arepo_postprocess/read_grid/mod.rs:165-195, 213-256, 402-437): the snapshot's
+    PartType0/ParticleIDs (no units), PartType0/Masses and PartType0/Density (Arepo's
+    units) give each cell's id and volume = mass / density; the grid file's Id1, Id2,
+    ConnectionType (no units), Area and Normal (Arepo's units) give the connections.
+    `snapshot_paths`: a file, a directory of `*.hdf5` files, or a list of them (read in
+    order, as one set of cells).  `cosmology` converts datasets with a or h exponents
+    (a file that has them and no cosmology is an error, as in the reference)."""
+    units = hdf5.ArepoUnits(cosmology)
+    ids = hdf5.read_dataset(snapshot_paths, "PartType0/ParticleIDs", hdf5.NONE, hdf5.IdUnits())
+    mass = hdf5.read_dataset(snapshot_paths, "PartType0/Masses", hdf5.MASS, units)
+    density = hdf5.read_dataset(snapshot_paths, "PartType0/Density", hdf5.DENSITY, units)
+    if not (ids.shape[0] == mass.shape[0] == density.shape[0]):
+        raise hdf5.H5Error(f"Different lengths of datasets: PartType0/ParticleIDs ({ids.shape[0]}), "
+                           f"PartType0/Masses ({mass.shape[0]}), PartType0/Density ({density.shape[0]})")
+    id1 = hdf5.read_dataset(grid_path, "Id1", hdf5.NONE, hdf5.IdUnits())
+    id2 = hdf5.read_dataset(grid_path, "Id2", hdf5.NONE, hdf5.IdUnits())
+    ctype = hdf5.read_dataset(grid_path, "ConnectionType", hdf5.NONE, hdf5.IdUnits())
+    area = hdf5.read_dataset(grid_path, "Area", hdf5.AREA, units)
+    normal = hdf5.read_dataset(grid_path, "Normal", hdf5.NONE, units)
+    return from_connections(ids, mass / density, id1, id2, ctype, area, normal.reshape(-1, 3), periodic)
+
+
+# src/units/mod.rs:101-104
+BOLTZMANN_CONSTANT = 1.380649e-23  # J/K
+GAMMA = 5.0 / 3.0
+HYDROGEN_MASS_FRACTION = 0.76  # src/main.rs:214, the assumed X_H
+
+
+def temperature_from_internal_energy(internal_energy, ionized_hydrogen_fraction, density):
+    """Temperature::from_internal_energy_density_hydrogen_only
+    (src/units/specific_impls.rs:46-60) of the energy density u * rho, as
+    src/main.rs:159-166 forms it: ((u * rho) / rho) * mu * (gamma - 1) * m_p / k_B with
+    mu = 1 / (x_HII + 1), evaluated left to right as there."""
+    rho = np.asarray(density, np.float64)
+    per_mass = (np.asarray(internal_energy, np.float64) * rho) / rho
+    mu = 1.0 / (np.asarray(ionized_hydrogen_fraction, np.float64) + 1.0)
+    return per_mass * mu * (GAMMA - 1.0) * PROTON_MASS / BOLTZMANN_CONSTANT
+
+
+def read_initial_conditions(snapshot_paths, initial_fraction_ionized_hydrogen: Optional[float] = None,
+                            cosmology: Optional[hdf5.Cosmology] = None) -> dict:
+    """The gas state of an Arepo snapshot as the sweep takes it, in SI units (src/main.rs:71-235):
+
+    * density: PartType0/Density;
+    * ionized_hydrogen_fraction: `initial_fraction_ionized_hydrogen` for every cell if
+      given, else 0.76 * PartType0/ElectronAbundance clamped to [1e-10, 1 - 1e-10]
+      (`set_initial_ionized_fraction_from_electron_abundance_system`);
+    * temperature: from PartType0/InternalEnergy and that fraction
+      (`insert_missing_components_system`, `temperature_from_internal_energy`);
+    * position: PartType0/Coordinates [N, 3], m.
+    """
+    units = hdf5.ArepoUnits(cosmology)
+    density = hdf5.read_dataset(snapshot_paths, "PartType0/Density", hdf5.DENSITY, units)
+    energy = hdf5.read_dataset(snapshot_paths, "PartType0/InternalEnergy", hdf5.ENERGY_PER_MASS, units)
+    position = hdf5.read_dataset(snapshot_paths, "PartType0/Coordinates", hdf5.LENGTH, units).reshape(-1, 3)
+    if initial_fraction_ionized_hydrogen is None:
+        xe = hdf5.read_dataset(snapshot_paths, "PartType0/ElectronAbundance", hdf5.NONE, units)
+        x = np.clip(HYDROGEN_MASS_FRACTION * xe, 1e-10, 1.0 - 1e-10)
+    else:
+        x = np.full(density.shape[0], float(initial_fraction_ionized_hydrogen))
+    n = density.shape[0]
+    if not (energy.shape[0] == position.shape[0] == x.shape[0] == n):
+        raise hdf5.H5Error("Different lengths of datasets: PartType0/Density, InternalEnergy, Coordinates, "
+                           "ElectronAbundance")
+    return {"density": density, "ionized_hydrogen_fraction": x,
+            "temperature": temperature_from_internal_energy(energy, x, density), "position": position}
 
 
 def dependency_cycles(grid: Grid, directions: np.ndarray) -> int:

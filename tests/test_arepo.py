@@ -3,8 +3,10 @@
 The conversion restates the reference's single-rank grid read-in
 (src/arepo_postprocess/read_grid/mod.rs).  CPU: the ConnectionType rules, face order
 and kinds on hand-made lists; a Voronoi grid written out as a shuffled connection list
-with fresh particle ids comes back face for face; the dependency-cycle count; and the
-oracle driven by the converted grid evolves like the original.  GPU: the mixed sweep on
+with fresh particle ids comes back face for face, also through HDF5 grid and snapshot
+files in Arepo's comoving code units; the initial gas state of a snapshot; the
+dependency-cycle count; and the oracle driven by the converted grid evolves like the
+original.  GPU: the mixed sweep on
 the converted grid against the original grid.
 """
 import numpy as np
@@ -119,14 +121,109 @@ def test_dependency_cycles():
     assert arepo.dependency_cycles(g, directions_from_num(16)) == 0
 
 
-def test_read_grid_file_needs_h5py():
-    try:
-        import h5py  # noqa: F401
-    except ImportError:
-        with pytest.raises(ImportError):
-            arepo.read_grid_file("grid.hdf5", "snap.hdf5", periodic=True)
-    else:
-        pytest.skip("h5py present: the file reader is exercised by from_connections' tests")
+KPC = 3.085678e21      # cm
+MSUN10 = 1.989e43      # 1e10 solar masses in g
+
+
+def _arepo_attrs(to_cgs, length=0, mass=0, velocity=0, a=0, h=0):
+    return {"to_cgs": np.float64(to_cgs), "length_scaling": np.float64(length), "mass_scaling": np.float64(mass),
+            "velocity_scaling": np.float64(velocity), "a_scaling": np.float64(a), "h_scaling": np.float64(h)}
+
+
+def _arepo_factor(to_cgs, length=0, mass=0, a=0, h=0, cosmo=(0.5, 0.7)):
+    """SI factor of a dataset with these exponents (src/arepo_postprocess/unit_reader.rs:97-115)."""
+    ca, ch = cosmo
+    return (1.0 / (ca ** -a * ch ** -h)) * (0.01 ** length * 0.001 ** mass) * to_cgs
+
+
+def test_read_grid_file_from_hdf5(voronoi_pair, tmp_path):
+    """A snapshot (split over two files) and a grid file written in Arepo's comoving code
+    units read back as the grid from_connections builds from the SI arrays."""
+    from hdf5_writer import H5Writer
+    from subsweep_gb300 import hdf5
+
+    w, _ = voronoi_pair
+    g = w.grid
+    rng = np.random.default_rng(11)
+    uid = rng.choice(10 ** 12, size=g.num_cells, replace=False).astype(np.uint64)
+    id1, id2, ctype, area, normal = to_connections(g, uid.astype(np.int64), rng)
+    a_mass = dict(mass=1, h=-1)
+    a_rho = dict(length=-3, mass=1, a=-3, h=2)
+    a_area = dict(length=2, a=2, h=-2)
+    rho_code = rng.uniform(1e-3, 1e-1, g.num_cells)
+    mass_code = g.volume * (rho_code * _arepo_factor(6.77e-22, **a_rho)) / _arepo_factor(MSUN10, **a_mass)
+    area_code = area / _arepo_factor(KPC ** 2, **a_area)
+
+    snap = tmp_path / "snap"
+    snap.mkdir()
+    half = g.num_cells // 2
+    for i, sl in enumerate((slice(0, half), slice(half, None))):
+        s = H5Writer()
+        s.group("Header", {"Time": np.float64(0.5)})
+        s.dataset("PartType0/ParticleIDs", uid[sl])
+        s.dataset("PartType0/Masses", mass_code[sl].astype(np.float32), attrs=_arepo_attrs(MSUN10, **a_mass))
+        s.dataset("PartType0/Density", rho_code[sl].astype(np.float32), attrs=_arepo_attrs(6.77e-22, **a_rho))
+        s.write(snap / f"snap_010.{i}.hdf5")
+    gw = H5Writer()
+    gw.dataset("Id1", id1.astype(np.uint64), layout="chunked", chunks=(1000,), filters=("shuffle", "deflate"))
+    gw.dataset("Id2", id2.astype(np.uint64), layout="chunked", chunks=(1000,), filters=("shuffle", "deflate"))
+    gw.dataset("ConnectionType", ctype.astype(np.int32))
+    gw.dataset("Area", area_code, attrs=_arepo_attrs(KPC ** 2, **a_area))
+    gw.dataset("Normal", normal, attrs=_arepo_attrs(0.0))
+    gw.write(tmp_path / "grid.hdf5")
+
+    cosmo = hdf5.Cosmology(a=0.5, h=0.7)
+    got = arepo.read_grid_file(tmp_path / "grid.hdf5", snap, periodic=True, cosmology=cosmo)
+    mass_si = mass_code.astype(np.float32).astype(np.float64) * _arepo_factor(MSUN10, **a_mass)
+    rho_si = rho_code.astype(np.float32).astype(np.float64) * _arepo_factor(6.77e-22, **a_rho)
+    want = arepo.from_connections(uid.astype(np.int64), mass_si / rho_si, id1, id2, ctype,
+                                  area_code * _arepo_factor(KPC ** 2, **a_area), normal, periodic=True)
+    for field in ("row_ptr", "nbr", "kind", "area", "normal", "volume", "size"):
+        np.testing.assert_array_equal(getattr(got, field), getattr(want, field), err_msg=field)
+    # the geometry is the original grid's to the float32 rounding of the snapshot's fields
+    np.testing.assert_allclose(got.volume, g.volume, rtol=1e-6)
+    np.testing.assert_allclose(got.area, want.area, rtol=0)
+    for c in range(0, g.num_cells, 37):
+        assert [r[:2] for r in face_table(got, c)] == [r[:2] for r in face_table(g, c)]
+    with pytest.raises(hdf5.H5Error, match="no cosmology given"):
+        arepo.read_grid_file(tmp_path / "grid.hdf5", snap, periodic=True)
+
+
+def test_read_initial_conditions(tmp_path):
+    """Density, x_HII from the electron abundance (0.76 x_e clamped) or a fixed fraction,
+    and T from the internal energy, in SI (src/main.rs:159-219)."""
+    from hdf5_writer import H5Writer
+    from subsweep_gb300 import hdf5
+    from subsweep_gb300.sweep import PROTON_MASS
+
+    rng = np.random.default_rng(5)
+    n = 50
+    rho = rng.uniform(1e-4, 1e-2, n)
+    u = rng.uniform(10.0, 1e3, n)       # (km/s)^2
+    xe = np.concatenate([[0.0, 2.0], rng.uniform(0, 1.2, n - 2)])
+    pos = rng.uniform(0, 1e4, (n, 3))  # kpc
+    s = H5Writer()
+    s.dataset("PartType0/Density", rho, attrs=_arepo_attrs(6.77e-22, length=-3, mass=1))
+    s.dataset("PartType0/InternalEnergy", u, attrs=_arepo_attrs(1e10, velocity=2))
+    s.dataset("PartType0/ElectronAbundance", xe, attrs=_arepo_attrs(0.0))
+    s.dataset("PartType0/Coordinates", pos, attrs=_arepo_attrs(KPC, length=1))
+    s.write(tmp_path / "snap.hdf5")
+    ic = arepo.read_initial_conditions(tmp_path / "snap.hdf5")
+    rho_si = rho * (0.01 ** -3 * 0.001 * 6.77e-22)
+    u_si = u * (0.01 ** 2 * 1e10)
+    x = np.clip(0.76 * xe, 1e-10, 1 - 1e-10)
+    np.testing.assert_array_equal(ic["density"], rho_si)
+    np.testing.assert_array_equal(ic["ionized_hydrogen_fraction"], x)
+    assert ic["ionized_hydrogen_fraction"][0] == 1e-10 and ic["ionized_hydrogen_fraction"][1] == 1 - 1e-10
+    np.testing.assert_array_equal(ic["position"], pos * (0.01 * KPC))
+    want_t = (u_si * rho_si) / rho_si * (1.0 / (x + 1.0)) * (5.0 / 3.0 - 1.0) * PROTON_MASS / 1.380649e-23
+    np.testing.assert_array_equal(ic["temperature"], want_t)
+    # u of 10 to 1000 (km/s)^2 is some 10^2.5 to 10^5 K
+    assert 1e2 < ic["temperature"].min() and ic["temperature"].max() < 1e6
+    fixed = arepo.read_initial_conditions(tmp_path / "snap.hdf5", initial_fraction_ionized_hydrogen=0.5)
+    assert np.all(fixed["ionized_hydrogen_fraction"] == 0.5)
+    np.testing.assert_array_equal(fixed["temperature"],
+                                  (u_si * rho_si) / rho_si * (1.0 / 1.5) * (5.0 / 3.0 - 1.0) * PROTON_MASS / 1.380649e-23)
 
 
 def _with_grid(w, grid):
