@@ -188,7 +188,9 @@ class _Object:
 
     @property
     def attrs(self) -> dict:
-        """Attributes stored in the object header: name -> numpy scalar or array."""
+        """Attributes stored in the object header: name -> numpy scalar or array, or None
+        for an attribute whose datatype this reader does not decode (variable-length
+        strings, compounds, ...: Arepo's `Parameters` and `Config` groups may hold them)."""
         r = self.file._r
         out = {}
         if self._first(_MSG_ATTRIBUTE_INFO) is not None:
@@ -229,7 +231,10 @@ def _attribute(r: _Reader, m: _Message):
         p = spos + ssize
     else:
         raise H5Error(f"attribute message version {version}")
-    dtype = _datatype(r, tpos)
+    try:
+        dtype = _datatype(r, tpos)
+    except H5Error:
+        return name, None
     shape = _dataspace(r, spos)
     if shape is None:
         return name, None
@@ -593,11 +598,15 @@ class Cosmology:
         return float(self.a) ** (-d.a) * float(self.h) ** (-d.h)
 
 
+def _scalar_float(value, name: str, dataset: str) -> float:
+    if value is None or np.ndim(value) != 0 or np.asarray(value).dtype.kind not in "iuf":
+        raise H5Error(f"attribute '{name}' of dataset '{dataset}' is not a number")
+    return float(value)
+
+
 def _scalar_int(value, name: str, dataset: str) -> int:
     """An integer attribute read as the library converts it to i32 (truncation)."""
-    if value is None or np.ndim(value) != 0:
-        raise H5Error(f"attribute '{name}' of dataset '{dataset}' is not a scalar")
-    return int(value)
+    return int(_scalar_float(value, name, dataset))
 
 
 class DefaultUnits:
@@ -609,7 +618,7 @@ class DefaultUnits:
         attrs = ds.attrs
         if "scale_factor_si" not in attrs:
             raise H5Error("No scale factor in dataset")
-        return float(attrs["scale_factor_si"])
+        return _scalar_float(attrs["scale_factor_si"], "scale_factor_si", ds.name)
 
     def dimension(self, ds: Dataset) -> Dimension:
         attrs = ds.attrs
@@ -672,7 +681,7 @@ class ArepoUnits:
         attrs = ds.attrs
         if "to_cgs" not in attrs:
             raise H5Error("No scale factor in dataset")
-        cgs = float(attrs["to_cgs"])
+        cgs = _scalar_float(attrs["to_cgs"], "to_cgs", ds.name)
         if cgs == 0.0:
             if d != NONE:
                 raise H5Error(f"unit scale factor 0 in dataset '{ds.name}' of dimension {d}")

@@ -61,13 +61,28 @@ def _message(mtype: int, data: bytes, flags: int = 0) -> bytes:
     return struct.pack("<HHB3x", mtype, len(data), flags) + data
 
 
+class VlenString:
+    """An attribute holding one variable-length string (datatype class 9): written with
+    a null global-heap reference, enough for a reader that does not decode it."""
+
+    def __init__(self, text: str):
+        self.text = text
+
+
 def _attribute(name: str, value) -> bytes:
-    value = np.asarray(value)
     nm = name.encode() + b"\0"
-    dt = _datatype(value.dtype)
-    ds = _dataspace(value.shape)
+    if isinstance(value, VlenString):
+        # class 9 version 1, type 1 (string), null-terminated ASCII; base type: 1-byte char
+        dt = bytes([0x19, 0x01, 0, 0]) + struct.pack("<I", 16) + bytes([0x13, 0, 0, 0]) + struct.pack("<I", 1)
+        ds = _dataspace(())
+        data = struct.pack("<IQI", len(value.text), 0, 0)
+    else:
+        value = np.asarray(value)
+        dt = _datatype(value.dtype)
+        ds = _dataspace(value.shape)
+        data = value.tobytes()
     body = struct.pack("<BBHHH", 1, 0, len(nm), len(dt), len(ds)) + _pad8(nm) + _pad8(dt) + _pad8(ds)
-    return _message(0x0C, body + value.tobytes())
+    return _message(0x0C, body + data)
 
 
 def _shuffle(raw: bytes, width: int) -> bytes:

@@ -159,6 +159,21 @@ def test_other_layouts_and_dataspaces(tmp_path):
         np.testing.assert_array_equal(f["v1_layout"].read(3, 6), DATA["f8_rows"][3:6])
 
 
+def test_undecoded_attributes_read_as_none(tmp_path):
+    """An attribute of a type the reader does not decode (a variable-length string, as
+    Arepo's Parameters group may hold) reads as None beside the others; a unit
+    attribute of such a type is an error of the unit reader, not of the file."""
+    from hdf5_writer import VlenString
+    w, path = _write(tmp_path)
+    w.group("Parameters", {"InitCondFile": VlenString("ics"), "BoxSize": np.float64(25.0)})
+    w.dataset("x", np.arange(3.0), attrs={**_ref_attrs(2.0), "scale_factor_si": VlenString("2")})
+    w.write(path)
+    with hdf5.File(path) as f:
+        assert f["Parameters"].attrs == {"InitCondFile": None, "BoxSize": 25.0}
+    with pytest.raises(hdf5.H5Error, match="attribute 'scale_factor_si' of dataset '/x' is not a number"):
+        hdf5.read_dataset(path, "x", hdf5.NONE)
+
+
 def test_rejections(tmp_path):
     w, path = _write(tmp_path)
     w.dataset("x", np.arange(10.0))
