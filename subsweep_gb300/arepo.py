@@ -36,6 +36,8 @@ reference does; `read_initial_conditions` reads the gas state the sweep starts f
 """
 from __future__ import annotations
 
+import pathlib
+import re
 from typing import Optional
 
 import numpy as np
@@ -167,8 +169,65 @@ def temperature_from_internal_energy(internal_energy, ionized_hydrogen_fraction,
     return per_mass * mu * (GAMMA - 1.0) * PROTON_MASS / BOLTZMANN_CONSTANT
 
 
+def snapshot_folders(remap_from):
+    """(first, last) output folders of an earlier run: the subdirectories of `remap_from`
+    with the lowest and the highest number (`get_highest_or_lowest_snapshot_dir`,
+    src/arepo_postprocess/remap.rs:318-353).  Every subdirectory must be named by a
+    number."""
+    root = pathlib.Path(remap_from)
+    if not root.is_dir():
+        raise hdf5.H5Error(f"remap path {root} is not a directory")
+    folders = []
+    for sub in sorted(q for q in root.iterdir() if q.is_dir()):
+        if not re.fullmatch(r"\+?[0-9]+", sub.name):
+            raise hdf5.H5Error(f"Unexpected folder in snapshot dir: {sub}")
+        folders.append((int(sub.name), sub))
+    if not folders:
+        raise hdf5.H5Error("No snapshot folder exists. Failed to remap")
+    return min(folders, key=lambda f: f[0])[1], max(folders, key=lambda f: f[0])[1]
+
+
+def remap_abundances_and_temperatures(remap_from, position, ionized_hydrogen_fraction, temperature,
+                                      cosmology: Optional[hdf5.Cosmology]):
+    """The reference's `remap_from` (src/arepo_postprocess/remap.rs:82-125, 380-383) on one
+    rank: each cell takes the larger of its own x_HII and T and those of the nearest cell
+    of an earlier run.  The earlier run's positions come from its first output folder
+    (dataset `position`, with the root attributes `scale_factor` and `little_h`) and are
+    scaled by (a / a_first); its x_HII and T (`ionized_hydrogen_fraction`, `temperature`)
+    from its last.  The reference requires a cosmological run here (its non-cosmological
+    branch panics); so does this.  Nearest means least Euclidean distance; among equally
+    near cells the choice is the search tree's, as in the reference.  Returns the new
+    (x_HII, T)."""
+    from scipy.spatial import cKDTree
+
+    if cosmology is None:
+        raise hdf5.H5Error("remapping needs the cosmology of the run (the reference supports only cosmological runs)")
+    first, last = snapshot_folders(remap_from)
+    first_files, last_files = hdf5.input_files(first), hdf5.input_files(last)
+    if not first_files or not last_files:
+        raise hdf5.H5Error(f"no *.hdf5 files in {first if not first_files else last}")
+    old_pos = hdf5.read_dataset(first_files, "position", hdf5.LENGTH).reshape(-1, 3)
+    old_x = hdf5.read_dataset(last_files, "ionized_hydrogen_fraction", hdf5.NONE)
+    old_t = hdf5.read_dataset(last_files, "temperature", hdf5.TEMPERATURE)
+    if not (old_pos.shape[0] == old_x.shape[0] == old_t.shape[0]):
+        raise hdf5.H5Error(f"remap data of different lengths: position {old_pos.shape[0]}, "
+                           f"ionized_hydrogen_fraction {old_x.shape[0]}, temperature {old_t.shape[0]}")
+    with hdf5.File(first_files[0]) as f:
+        attrs = f.attrs
+        for key in ("scale_factor", "little_h"):
+            if attrs.get(key) is None:
+                raise hdf5.H5Error(f"no attribute '{key}' in {first_files[0]}")
+        a_first = float(attrs["scale_factor"])
+    old_pos = old_pos * (cosmology.a / a_first) ** hdf5.LENGTH.length  # get_scale_factor_difference
+    _, nearest = cKDTree(old_pos).query(np.asarray(position, np.float64).reshape(-1, 3), k=1)
+    # Temperature / IonizedHydrogenFraction max: f64::max, which ignores a NaN
+    x = np.fmax(np.asarray(ionized_hydrogen_fraction, np.float64), old_x[nearest])
+    t = np.fmax(np.asarray(temperature, np.float64), old_t[nearest])
+    return x, t
+
+
 def read_initial_conditions(snapshot_paths, initial_fraction_ionized_hydrogen: Optional[float] = None,
-                            cosmology: Optional[hdf5.Cosmology] = None) -> dict:
+                            cosmology: Optional[hdf5.Cosmology] = None, remap_from=None) -> dict:
     """The gas state of an Arepo snapshot as the sweep takes it, in SI units (src/main.rs:71-235):
 
     * density: PartType0/Density;
@@ -177,7 +236,9 @@ def read_initial_conditions(snapshot_paths, initial_fraction_ionized_hydrogen: O
       (`set_initial_ionized_fraction_from_electron_abundance_system`);
     * temperature: from PartType0/InternalEnergy and that fraction
       (`insert_missing_components_system`, `temperature_from_internal_energy`);
-    * position: PartType0/Coordinates [N, 3], m.
+    * position: PartType0/Coordinates [N, 3], m;
+    * with `remap_from` (an earlier run's output folder), x_HII and T raised to those of
+      the nearest cell of that run (`remap_abundances_and_temperatures`).
     """
     units = hdf5.ArepoUnits(cosmology)
     density = hdf5.read_dataset(snapshot_paths, "PartType0/Density", hdf5.DENSITY, units)
@@ -192,8 +253,10 @@ def read_initial_conditions(snapshot_paths, initial_fraction_ionized_hydrogen: O
     if not (energy.shape[0] == position.shape[0] == x.shape[0] == n):
         raise hdf5.H5Error("Different lengths of datasets: PartType0/Density, InternalEnergy, Coordinates, "
                            "ElectronAbundance")
-    return {"density": density, "ionized_hydrogen_fraction": x,
-            "temperature": temperature_from_internal_energy(energy, x, density), "position": position}
+    temperature = temperature_from_internal_energy(energy, x, density)
+    if remap_from is not None:
+        x, temperature = remap_abundances_and_temperatures(remap_from, position, x, temperature, cosmology)
+    return {"density": density, "ionized_hydrogen_fraction": x, "temperature": temperature, "position": position}
 
 
 def dependency_cycles(grid: Grid, directions: np.ndarray) -> int:

@@ -7,14 +7,16 @@ with the library's default, earliest-format properties) produce:
 * version 1 object headers, with continuation blocks;
 * groups stored as symbol tables (version 1 B-tree of type 0, symbol nodes, local heap);
 * dataspaces (versions 1 and 2: scalar, simple, null);
-* fixed-point and IEEE floating-point datatypes of either byte order, fixed-length strings;
+* fixed-point and IEEE floating-point datatypes of either byte order, fixed-length
+  strings, and compound and array types built from them;
 * data layouts of versions 1 to 3: compact, contiguous, and chunked (version 1 B-tree of
   type 1) with the deflate, shuffle and Fletcher-32 filters;
 * attribute messages of versions 1 to 3 (stored in the object header).
 
 Files that need the format's newer structures (superblock 2/3, version 2 object
 headers, link messages, fractal heaps, version 4 layouts, dense attribute storage,
-shared or committed datatypes) are rejected with `H5Error` naming the structure.
+shared or committed datatypes) are rejected with `H5Error` naming the structure;
+an attribute of a type the reader does not decode reads as None.
 
 On top of the reader, `read_dataset` restates the reference's dataset input
 (src/io/input/mod.rs:260-299 `read_region_chunked`, `get_dataset_and_conversion_factor_for_file`,
@@ -102,14 +104,19 @@ class _Message:
 
 def _datatype(r: _Reader, pos: int) -> np.dtype:
     """numpy dtype of a datatype message (specification IV.A.2.d)."""
+    return _datatype_at(r, pos)[0]
+
+
+def _datatype_at(r: _Reader, pos: int) -> Tuple[np.dtype, int]:
+    """(numpy dtype, encoded length in bytes) of the datatype description at pos."""
     cv = r.u(pos, 1)
-    cls, bits, size = cv & 0x0F, r.u(pos + 1, 3), r.u(pos + 4, 4)
+    cls, version, bits, size = cv & 0x0F, cv >> 4, r.u(pos + 1, 3), r.u(pos + 4, 4)
     if cls == 0:  # fixed-point: bit 0 byte order, bit 3 signed; offset, precision
         order = ">" if bits & 1 else "<"
         offset, precision = r.u(pos + 8, 2), r.u(pos + 10, 2)
         if size not in (1, 2, 4, 8) or offset != 0 or precision != 8 * size:
             raise H5Error(f"fixed-point type of {size} bytes with bit offset {offset}, precision {precision}")
-        return np.dtype(f"{order}{'i' if bits & 8 else 'u'}{size}")
+        return np.dtype(f"{order}{'i' if bits & 8 else 'u'}{size}"), 12
     if cls == 1:  # floating-point: bit 0 byte order (bit 6: VAX order)
         if bits & 0x40:
             raise H5Error("VAX-order floating-point type")
@@ -119,11 +126,49 @@ def _datatype(r: _Reader, pos: int) -> np.dtype:
                r.u(pos + 15, 1), r.u(pos + 16, 4))
         if layouts.get(size) != got:
             raise H5Error(f"floating-point type of {size} bytes that is not IEEE 754 binary{8 * size}")
-        return np.dtype(f"{'>' if bits & 1 else '<'}f{size}")
+        return np.dtype(f"{'>' if bits & 1 else '<'}f{size}"), 20
     if cls == 3:  # fixed-length string
-        return np.dtype(f"S{size}")
-    names = {2: "time", 4: "bitfield", 5: "opaque", 6: "compound", 7: "reference", 8: "enumerated",
-             9: "variable-length", 10: "array"}
+        return np.dtype(f"S{size}"), 8
+    if cls == 6:  # compound: members by name, byte offset and type
+        names, formats, offsets = [], [], []
+        p = pos + 8
+        offset_bytes = 1 if size < 1 << 8 else 2 if size < 1 << 16 else 3 if size < 1 << 24 else 4
+        for _ in range(bits & 0xFFFF):
+            end = r.buf.find(b"\0", p)
+            if end < 0:
+                raise H5Error(f"unterminated compound member name at {p}")
+            names.append(bytes(r.buf[p:end]).decode("utf-8"))
+            p = (p + ((end - p + 1 + 7) & ~7)) if version < 3 else end + 1
+            if version < 3:
+                offsets.append(r.u(p, 4))
+                p += 4
+            else:
+                offsets.append(r.u(p, offset_bytes))
+                p += offset_bytes
+            dims = ()
+            if version == 1:
+                rank = r.u(p, 1)
+                dims = tuple(r.u(p + 12 + 4 * i, 4) for i in range(rank))
+                p += 28
+            member, n = _datatype_at(r, p)
+            p += n
+            formats.append((member, dims) if dims else member)
+        if not names:
+            raise H5Error("compound datatype without members")
+        return np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": size}), p - pos
+    if cls == 10:  # array of a base type
+        rank = r.u(pos + 8, 1)
+        if version == 2:
+            dims = tuple(r.u(pos + 12 + 4 * i, 4) for i in range(rank))
+            p = pos + 12 + 8 * rank
+        elif version == 3:
+            dims = tuple(r.u(pos + 9 + 4 * i, 4) for i in range(rank))
+            p = pos + 9 + 4 * rank
+        else:
+            raise H5Error(f"array datatype version {version}")
+        base, n = _datatype_at(r, p)
+        return np.dtype((base, dims)), p + n - pos
+    names = {2: "time", 4: "bitfield", 5: "opaque", 7: "reference", 8: "enumerated", 9: "variable-length"}
     raise H5Error(f"{names.get(cls, f'class {cls}')} datatype")
 
 
@@ -240,7 +285,7 @@ def _attribute(r: _Reader, m: _Message):
         return name, None
     n = int(np.prod(shape, dtype=np.int64)) if shape else 1
     data = np.frombuffer(r.raw(p, n * dtype.itemsize), dtype=dtype, count=n)
-    value = data.reshape(shape) if shape else data[0]
+    value = data.reshape(tuple(shape) + dtype.shape) if shape else data[0]
     return name, value
 
 
@@ -395,12 +440,13 @@ class Dataset(_Object):
 
     def read(self, start: Optional[int] = None, stop: Optional[int] = None) -> np.ndarray:
         """Rows [start, stop) along the first axis (all of them by default), in native
-        byte order."""
+        byte order; an array element type adds its dimensions as trailing axes, a
+        compound one gives a structured array."""
         if self._null:
             return np.empty(0, self.dtype.newbyteorder("="))
         if not self.shape:
             out = self._read_rows(0, 1, scalar=True)
-            return out.reshape(())
+            return out.reshape(self.dtype.shape)
         n0 = self.shape[0]
         lo, hi, _ = slice(start, stop).indices(n0)
         hi = max(hi, lo)
@@ -419,10 +465,10 @@ class Dataset(_Object):
                 data = np.zeros(n, self.dtype)
             else:
                 data = r.array(addr + lo * row * self.dtype.itemsize, self.dtype, n)
-            out = data.reshape(out_shape)
+            out = data.reshape(out_shape + self.dtype.shape)  # an array type adds trailing axes
         else:
             out = self._read_chunked(r, lo, hi, shape, out_shape)
-        return np.ascontiguousarray(out.astype(self.dtype.newbyteorder("="), copy=True))
+        return np.ascontiguousarray(out.astype(self.dtype.base.newbyteorder("="), copy=True))
 
     def _read_chunked(self, r: _Reader, lo: int, hi: int, shape, out_shape) -> np.ndarray:
         _, btree, chunk, elem = self._layout
@@ -450,7 +496,7 @@ class Dataset(_Object):
             full = int(np.prod(chunk, dtype=np.int64))
             if len(raw) < full * elem:
                 raise H5Error(f"dataset '{self.name}': chunk at {addr} holds {len(raw)} bytes, needs {full * elem}")
-            block = np.frombuffer(raw, self.dtype, count=full).reshape(chunk)
+            block = np.frombuffer(raw, self.dtype, count=full).reshape(tuple(chunk) + self.dtype.shape)
             src, dst = [], []
             for axis, (o, c, s) in enumerate(zip(offsets, chunk, shape)):
                 a, b = (max(o, lo), min(o + c, hi)) if axis == 0 else (o, min(o + c, s))
@@ -582,6 +628,7 @@ NONE = Dimension()
 LENGTH = Dimension(length=1)
 AREA = Dimension(length=2)
 MASS = Dimension(mass=1)
+TEMPERATURE = Dimension(temperature=1)
 DENSITY = Dimension(length=-3, mass=1)
 ENERGY_PER_MASS = Dimension(length=2, time=-2)
 
@@ -735,6 +782,12 @@ def read_dataset(paths: Union[str, os.PathLike, Sequence], name: str, dimension:
             if units.dimension(ds) != dimension:
                 raise H5Error(f"Mismatch in dimension while reading dataset {name}.")
             data = ds.read()
+            if data.dtype.names:
+                # a vector stored as a compound of numbers ({x, y, z}): its fields on a
+                # trailing axis, like a vector stored as an array type
+                if any(data.dtype[n].kind not in "iuf" or data.dtype[n].shape for n in data.dtype.names):
+                    raise H5Error(f"dataset {name}: compound members are not all numbers")
+                data = np.stack([data[n] for n in data.dtype.names], axis=-1)
             factor = factor_written / 1.0  # factor_written / base_conversion_factor (SI: 1)
             if factor != 1.0 or data.dtype.kind == "f":
                 data = data.astype(np.float64) * factor

@@ -23,8 +23,37 @@ def _pad8(b: bytes) -> bytes:
     return b + b"\0" * (-len(b) % 8)
 
 
-def _datatype(dtype: np.dtype) -> bytes:
+def _datatype(dtype: np.dtype, version: int = 0) -> bytes:
+    """Datatype message of a numpy dtype; `version` picks the encoding of compound (1, 2
+    or 3; default 1) and array (2 or 3; default 2) types."""
     dtype = np.dtype(dtype)
+    if dtype.subdtype is not None:  # array class
+        base, dims = dtype.subdtype
+        v = version or 2
+        head = bytes([0x0A | (v << 4), 0, 0, 0]) + struct.pack("<I", dtype.itemsize) + bytes([len(dims)])
+        if v == 2:
+            head += b"\0" * 3 + b"".join(struct.pack("<I", d) for d in dims) + \
+                b"".join(struct.pack("<I", i) for i in range(len(dims)))
+        else:
+            head += b"".join(struct.pack("<I", d) for d in dims)
+        return head + _datatype(base, version)
+    if dtype.names:  # compound class
+        v = version or 1
+        size = dtype.itemsize
+        body = b""
+        for name in dtype.names:
+            member, offset = dtype.fields[name][:2]
+            nm = name.encode() + b"\0"
+            if v < 3:
+                body += _pad8(nm) + struct.pack("<I", offset)
+                if v == 1:
+                    body += bytes([0, 0, 0, 0]) + b"\0" * 4 + b"\0" * 4 + b"\0" * 16
+            else:
+                nbytes = 1 if size < 1 << 8 else 2 if size < 1 << 16 else 3 if size < 1 << 24 else 4
+                body += nm + offset.to_bytes(nbytes, "little")
+            body += _datatype(member, version if member.names or member.subdtype else 0)
+        n = len(dtype.names)
+        return bytes([0x06 | (v << 4), n & 0xFF, n >> 8, 0]) + struct.pack("<I", size) + body
     be = 1 if dtype.byteorder == ">" or (dtype.byteorder == "=" and np.little_endian is False) else 0
     size = dtype.itemsize
     if dtype.kind in "iu":
@@ -110,12 +139,15 @@ class H5Writer:
 
     def dataset(self, path: str, data, attrs=None, layout="contiguous", chunks=None,
                 filters=(), filter_mask_first_chunk=0, btree_fanout=None, dataspace_version=1,
-                layout_version=3, unallocated=False):
+                layout_version=3, unallocated=False, dtype=None, type_version=0):
+        """`dtype`: the element type when it is an array type (numpy folds a subarray
+        dtype into the data's shape, so it is given apart)."""
         parent, _, name = path.strip("/").rpartition("/")
         self._group(parent)["members"][name] = {
             "data": np.asarray(data), "attrs": dict(attrs or {}), "layout": layout, "chunks": chunks,
             "filters": tuple(filters), "mask0": filter_mask_first_chunk, "fanout": btree_fanout,
-            "dsv": dataspace_version, "lv": layout_version, "unallocated": unallocated}
+            "dsv": dataspace_version, "lv": layout_version, "unallocated": unallocated,
+            "dtype": None if dtype is None else np.dtype(dtype), "tv": type_version}
 
     # -- serialising
     def _append(self, b: bytes) -> int:
@@ -184,10 +216,11 @@ class H5Writer:
 
     def _write_dataset(self, d) -> int:
         data = d["data"]
-        shape = data.shape
+        etype = d["dtype"] if d["dtype"] is not None else data.dtype
+        shape = data.shape[:data.ndim - len(etype.shape)]
         raw = np.ascontiguousarray(data).tobytes()
-        elem = data.dtype.itemsize
-        msgs = [_message(0x01, _dataspace(shape, d["dsv"])), _message(0x03, _datatype(data.dtype))]
+        elem = etype.itemsize
+        msgs = [_message(0x01, _dataspace(shape, d["dsv"])), _message(0x03, _datatype(etype, d["tv"]))]
         if d["layout"] == "contiguous":
             addr = UNDEF if (d["unallocated"] or not raw) else self._append(raw)
             if d["lv"] == 3:
@@ -204,7 +237,7 @@ class H5Writer:
             grid = [range(0, s, c) for s, c in zip(shape, chunks)]
             for k, origin in enumerate(np.ndindex(*[len(g) for g in grid])):
                 offsets = [g[i] for g, i in zip(grid, origin)]
-                block = np.zeros(chunks, data.dtype)
+                block = np.zeros(tuple(chunks) + etype.shape, data.dtype)
                 src = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offsets, chunks, shape))
                 block[tuple(slice(0, x.stop - x.start) for x in src)] = data[src]
                 mask = d["mask0"] if k == 0 else 0

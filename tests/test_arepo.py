@@ -263,3 +263,102 @@ def test_gpu_sweep_on_converted_grid(voronoi_pair):
         s.close()
     for k in ("ionized_hydrogen_fraction", "temperature"):
         np.testing.assert_allclose(out[0][k], out[1][k], rtol=1e-5, err_msg=k)
+
+
+def _ref_attrs(factor, length=0, mass=0, time=0, temperature=0):
+    return {"scale_factor_si": np.float64(factor), "scaling_length": np.int32(length),
+            "scaling_mass": np.int32(mass), "scaling_time": np.int32(time),
+            "scaling_temperature": np.int32(temperature)}
+
+
+def _write_run(folder, rng, n_old, a_first, vector="array"):
+    """Output folders 0, 3 and 12 of an earlier run: positions in the first (as an
+    array-typed or compound-typed 1-D dataset), x_HII and T in every folder (the last
+    one's differ), the cosmology attributes on the root group."""
+    from hdf5_writer import H5Writer
+    pos = rng.uniform(0, 1e21, (n_old, 3))
+    fields = {}
+    for k in (0, 3, 12):
+        sub = folder / f"{k}"
+        sub.mkdir(parents=True)
+        x = rng.uniform(0, 1, n_old)
+        t = rng.uniform(1e3, 1e5, n_old)
+        fields[k] = (x, t)
+        w = H5Writer()
+        w.group("/", {"scale_factor": np.float64(a_first + 0.01 * k), "little_h": np.float64(0.7),
+                      "time": np.float64(k)})
+        if vector == "array":
+            w.dataset("position", pos, dtype=np.dtype(("<f8", (3,))), attrs=_ref_attrs(1.0, length=1))
+        else:
+            xyz = np.zeros(n_old, dtype=[("x", "<f8"), ("y", "<f8"), ("z", "<f8")])
+            xyz["x"], xyz["y"], xyz["z"] = pos.T
+            w.dataset("position", xyz, attrs=_ref_attrs(1.0, length=1))
+        w.dataset("ionized_hydrogen_fraction", x, attrs=_ref_attrs(1.0))
+        w.dataset("temperature", t, attrs=_ref_attrs(1.0, temperature=1))
+        w.write(sub / "snapshot.hdf5")
+    return pos, fields
+
+
+@pytest.mark.parametrize("vector", ["array", "compound"])
+def test_remap_from_earlier_run(tmp_path, vector):
+    """remap_from (src/arepo_postprocess/remap.rs): positions of the first folder scaled
+    by a / a_first, x_HII and T of the last folder (12, not 3: folders go by number),
+    each cell raised to its nearest old cell's values; a NaN is ignored as f64::max does."""
+    from subsweep_gb300 import hdf5
+    rng = np.random.default_rng(21)
+    pos_old, fields = _write_run(tmp_path / "run", rng, 400, a_first=0.25, vector=vector)
+    cosmo = hdf5.Cosmology(a=0.5, h=0.7)
+    assert [p.name for p in arepo.snapshot_folders(tmp_path / "run")] == ["0", "12"]
+    pos_new = rng.uniform(0, 2e21, (300, 3))
+    x0 = rng.uniform(0, 1, 300)
+    t0 = rng.uniform(1e3, 1e5, 300)
+    x0[5], t0[7] = np.nan, np.nan
+    x, t = arepo.remap_abundances_and_temperatures(tmp_path / "run", pos_new, x0, t0, cosmo)
+    scaled = pos_old * (0.5 / 0.25)
+    d2 = ((pos_new[:, None, :] - scaled[None, :, :]) ** 2).sum(-1)
+    nearest = d2.argmin(1)
+    old_x, old_t = fields[12]
+    np.testing.assert_array_equal(x, np.fmax(x0, old_x[nearest]))
+    np.testing.assert_array_equal(t, np.fmax(t0, old_t[nearest]))
+    assert x[5] == old_x[nearest[5]] and t[7] == old_t[nearest[7]]
+    assert np.all(x >= np.nan_to_num(x0)) and np.any(x > x0)
+
+
+def test_remap_errors(tmp_path):
+    from subsweep_gb300 import hdf5
+    rng = np.random.default_rng(2)
+    cosmo = hdf5.Cosmology(a=0.5, h=0.7)
+    pos = np.zeros((1, 3))
+    with pytest.raises(hdf5.H5Error, match="No snapshot folder exists"):
+        (tmp_path / "empty").mkdir()
+        arepo.remap_abundances_and_temperatures(tmp_path / "empty", pos, [0.1], [1e4], cosmo)
+    _write_run(tmp_path / "run", rng, 10, a_first=0.25)
+    with pytest.raises(hdf5.H5Error, match="needs the cosmology"):
+        arepo.remap_abundances_and_temperatures(tmp_path / "run", pos, [0.1], [1e4], None)
+    (tmp_path / "run" / "latest").mkdir()
+    with pytest.raises(hdf5.H5Error, match="Unexpected folder in snapshot dir"):
+        arepo.remap_abundances_and_temperatures(tmp_path / "run", pos, [0.1], [1e4], cosmo)
+
+
+def test_read_initial_conditions_with_remap(tmp_path):
+    """The snapshot's own x_HII and T, then the remap on top, as src/main.rs orders the
+    startup stages (derived components before the remap)."""
+    from hdf5_writer import H5Writer
+    from subsweep_gb300 import hdf5
+    rng = np.random.default_rng(4)
+    _write_run(tmp_path / "run", rng, 200, a_first=0.5)
+    n = 60
+    s = H5Writer()
+    s.dataset("PartType0/Density", rng.uniform(1e-4, 1e-2, n), attrs=_arepo_attrs(6.77e-22, length=-3, mass=1))
+    s.dataset("PartType0/InternalEnergy", rng.uniform(10.0, 1e3, n), attrs=_arepo_attrs(1e10, velocity=2))
+    s.dataset("PartType0/ElectronAbundance", rng.uniform(0, 1, n), attrs=_arepo_attrs(0.0))
+    s.dataset("PartType0/Coordinates", rng.uniform(0, 1e21 / (0.01 * KPC), (n, 3)), attrs=_arepo_attrs(KPC, length=1))
+    s.write(tmp_path / "snap.hdf5")
+    cosmo = hdf5.Cosmology(a=0.5, h=0.7)
+    plain = arepo.read_initial_conditions(tmp_path / "snap.hdf5", cosmology=cosmo)
+    remapped = arepo.read_initial_conditions(tmp_path / "snap.hdf5", cosmology=cosmo, remap_from=tmp_path / "run")
+    x, t = arepo.remap_abundances_and_temperatures(tmp_path / "run", plain["position"],
+                                                   plain["ionized_hydrogen_fraction"], plain["temperature"], cosmo)
+    np.testing.assert_array_equal(remapped["ionized_hydrogen_fraction"], x)
+    np.testing.assert_array_equal(remapped["temperature"], t)
+    np.testing.assert_array_equal(remapped["density"], plain["density"])

@@ -159,6 +159,41 @@ def test_other_layouts_and_dataspaces(tmp_path):
         np.testing.assert_array_equal(f["v1_layout"].read(3, 6), DATA["f8_rows"][3:6])
 
 
+@pytest.mark.parametrize("type_version", [0, 3])
+@pytest.mark.parametrize("layout", ["contiguous", "chunked"])
+def test_compound_and_array_types(tmp_path, type_version, layout):
+    """Vectors stored as one element each: an array type [f64; 3] (trailing axis) and a
+    compound {x, y, z} (structured array), as writers of 3-vectors lay them out; a
+    compound with an array member and mixed types."""
+    rng = np.random.default_rng(9)
+    vec = rng.random((50, 3))
+    xyz = np.zeros(50, dtype=[("x", "<f8"), ("y", "<f8"), ("z", "<f8")])
+    xyz["x"], xyz["y"], xyz["z"] = vec.T
+    mixed = np.zeros(20, dtype=[("id", "<u8"), ("pos", "<f4", (3,)), ("flag", "i1")])
+    mixed["id"] = np.arange(20) * 7
+    mixed["pos"] = rng.random((20, 3))
+    mixed["flag"] = np.arange(20) % 3 - 1
+    w, path = _write(tmp_path)
+    kw = dict(layout=layout, chunks=(16,)) if layout == "chunked" else {}
+    w.dataset("vec", vec, dtype=np.dtype(("<f8", (3,))), type_version=type_version, **kw)
+    w.dataset("xyz", xyz, type_version=type_version, **kw)
+    w.dataset("mixed", mixed, type_version=type_version or 2, **kw)
+    w.group("g", {"corner": np.array([1.0, 2.0, 3.0])})
+    w.write(path)
+    with hdf5.File(path) as f:
+        ds = f["vec"]
+        assert ds.shape == (50,) and ds.dtype.shape == (3,)
+        np.testing.assert_array_equal(ds.read(), vec)
+        np.testing.assert_array_equal(ds.read(10, 20), vec[10:20])
+        got = f["xyz"].read()
+        assert got.dtype.names == ("x", "y", "z")
+        np.testing.assert_array_equal(np.stack([got["x"], got["y"], got["z"]], 1), vec)
+        got = f["mixed"].read()
+        assert got.dtype.names == ("id", "pos", "flag")
+        for name in ("id", "pos", "flag"):
+            np.testing.assert_array_equal(got[name], mixed[name])
+
+
 def test_undecoded_attributes_read_as_none(tmp_path):
     """An attribute of a type the reader does not decode (a variable-length string, as
     Arepo's Parameters group may hold) reads as None beside the others; a unit
