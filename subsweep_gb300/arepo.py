@@ -42,7 +42,8 @@ from typing import Optional
 
 import numpy as np
 
-from . import hdf5
+from . import bpass_table, hdf5
+from .cosmology import YEAR
 from .grid import Grid
 from .sweep import PROTON_MASS
 
@@ -224,6 +225,70 @@ def remap_abundances_and_temperatures(remap_from, position, ionized_hydrogen_fra
     x = np.fmax(np.asarray(ionized_hydrogen_fraction, np.float64), old_x[nearest])
     t = np.fmax(np.asarray(temperature, np.float64), old_t[nearest])
     return x, t
+
+
+SOLAR_MASS = 1.988477e30  # kg, src/units/mod.rs:55
+
+
+def _linear_interpolate(x1, x2, y1, y2, x):
+    return y1 + (x - x1) / (x2 - x1) * (y2 - y1)
+
+
+def bpass_lookup(age, metallicity, mass):
+    """Ionizing photon rate (photons/s) of stars of the given age (s), metallicity and
+    mass (kg) from the BPASS table (`bpass_lookup`, src/arepo_postprocess/bpass.rs:11-55):
+    age (in years) and metallicity clamped into the table's range shrunk by 1.00001,
+    bilinear interpolation of the per-solar-mass output in age, then metallicity, times
+    the mass in solar masses.  Elementwise over arrays."""
+    ages = np.asarray(bpass_table.AGE_BINS)
+    mets = np.asarray(bpass_table.METALLICITY_BINS)
+    table = np.asarray(bpass_table.TABLE)
+    safety = 1.00001
+    age_yr = np.clip(np.asarray(age, np.float64) / YEAR, ages[0] * safety, ages[-1] / safety)
+    met = np.clip(np.asarray(metallicity, np.float64), mets[0] * safety, mets[-1] / safety)
+    # binary_search_by_key: an exact hit at i gives i + 1, a miss its insertion point
+    mi = np.searchsorted(mets, met, side="right")
+    ai = np.searchsorted(ages, age_yr, side="right")
+    l1 = _linear_interpolate(ages[ai - 1], ages[ai], table[ai - 1, mi - 1], table[ai, mi - 1], age_yr)
+    l2 = _linear_interpolate(ages[ai - 1], ages[ai], table[ai - 1, mi], table[ai, mi], age_yr)
+    per_mass = _linear_interpolate(mets[mi - 1], mets[mi], l1, l2, met)
+    return per_mass * (np.asarray(mass, np.float64) / SOLAR_MASS)
+
+
+def read_sources(snapshot_paths, cosmology: hdf5.Cosmology, escape_fraction: float):
+    """Star particles of a snapshot as point sources (`read_sources`,
+    src/arepo_postprocess/sources.rs:54-128): PartType4/Coordinates, GFM_Metallicity,
+    GFM_StellarFormationTime (the scale factor of formation) and Masses in Arepo's units;
+    particles with a formation scale factor that is not positive (wind particles) are
+    dropped; each star's rate is `bpass_lookup` of its age (the cosmic time from its
+    formation to the cosmology's scale factor) times the escape fraction.  Returns
+    (positions [n, 3] in m, rates in photons/s); `grid.place_sources` or
+    `source_rates` adds each to its nearest cell."""
+    units = hdf5.ArepoUnits(cosmology)
+    pos = hdf5.read_dataset(snapshot_paths, "PartType4/Coordinates", hdf5.LENGTH, units).reshape(-1, 3)
+    met = hdf5.read_dataset(snapshot_paths, "PartType4/GFM_Metallicity", hdf5.NONE, units)
+    a_form = hdf5.read_dataset(snapshot_paths, "PartType4/GFM_StellarFormationTime", hdf5.NONE, units)
+    mass = hdf5.read_dataset(snapshot_paths, "PartType4/Masses", hdf5.MASS, units)
+    if not (pos.shape[0] == met.shape[0] == a_form.shape[0] == mass.shape[0]):
+        raise hdf5.H5Error("Different lengths of datasets: PartType4/Coordinates, GFM_Metallicity, "
+                           "GFM_StellarFormationTime, Masses")
+    stars = a_form > 0.0
+    age = np.array([cosmology.time_difference_between_scalefactors(float(a), cosmology.a) for a in a_form[stars]])
+    rates = bpass_lookup(age, met[stars], mass[stars]) * float(escape_fraction)
+    return pos[stars], rates
+
+
+def source_rates(cell_positions, source_positions, rates) -> np.ndarray:
+    """Per-cell source rates: each source's rate added, in order, to the cell whose
+    position is nearest (`set_source_terms_system`, src/source_systems.rs:48-80)."""
+    from scipy.spatial import cKDTree
+
+    out = np.zeros(np.asarray(cell_positions).reshape(-1, 3).shape[0])
+    if len(rates):
+        _, idx = cKDTree(np.asarray(cell_positions, np.float64).reshape(-1, 3)).query(
+            np.asarray(source_positions, np.float64).reshape(-1, 3), k=1)
+        np.add.at(out, idx, np.asarray(rates, np.float64))
+    return out
 
 
 def read_initial_conditions(snapshot_paths, initial_fraction_ionized_hydrogen: Optional[float] = None,

@@ -35,6 +35,8 @@ from typing import Optional, Sequence, Tuple, Union
 
 import numpy as np
 
+from .cosmology import Cosmology  # noqa: F401  (the unit readers' cosmology)
+
 SIGNATURE = b"\x89HDF\r\n\x1a\n"
 
 
@@ -631,18 +633,6 @@ MASS = Dimension(mass=1)
 TEMPERATURE = Dimension(temperature=1)
 DENSITY = Dimension(length=-3, mass=1)
 ENERGY_PER_MASS = Dimension(length=2, time=-2)
-
-
-@dataclasses.dataclass(frozen=True)
-class Cosmology:
-    """The parts of Cosmology::Cosmological the input reads (src/cosmology.rs:56-61):
-    the scale factor a and the little Hubble parameter h."""
-    a: float
-    h: float
-
-    def factor(self, d: Dimension) -> float:
-        # a.powi(-dimension.a) * h.powi(-dimension.h)
-        return float(self.a) ** (-d.a) * float(self.h) ** (-d.h)
 
 
 def _scalar_float(value, name: str, dataset: str) -> float:

@@ -14,6 +14,10 @@ and writes tests/golden/reference_kats.json:
 * voronoi_kat:     points and expected geometry of right_volume_and_face_areas_three_d
                    (src/voronoi/mod.rs tests)
 * direction_tables: SHA-256 of each direction table as little-endian doubles
+* bpass:           the check_is_close cases and tolerance of the BPASS lookup test
+                   (src/arepo_postprocess/bpass.rs tests)
+* cosmology:       the parameters and bounds of time_difference_between_scalefactors and
+                   get_scalefactor_from_scalefactor_and_time_difference (src/cosmology.rs tests)
 
 Usage: python tests/golden/gen_reference_kats.py /path/to/subsweep
 """
@@ -94,6 +98,32 @@ def main():
         tables[num] = hashlib.sha256(struct.pack("<%dd" % len(vals), *vals)).hexdigest()
     tables["1"] = hashlib.sha256(struct.pack("<3d", 1.0, 0.0, 0.0)).hexdigest()
     out["direction_tables"] = tables
+
+    src = (ref / "src/arepo_postprocess/bpass.rs").read_text()
+    tests = src[src.index("#[cfg(test)]"):]
+    tol = re.search(r"\(\(x - y\) / \(x\.abs\(\) \+ y\.abs\(\)\)\)\.abs\(\) < ([0-9.eE+-]+)", tests)
+    out["bpass"] = {
+        "relative_tolerance": rust_float(tol.group(1)),
+        "cases": [{"age_years": rust_float(a), "metallicity": rust_float(m), "photons_per_s": rust_float(v)}
+                  for a, m, v in re.findall(r"check_is_close\(([0-9.eE+-]+),\s*([0-9.eE+-]+),\s*([0-9.eE+-]+)\)",
+                                            tests)]}
+    assert len(out["bpass"]["cases"]) == 3
+
+    src = (ref / "src/cosmology.rs").read_text()
+    tests = src[src.index("#[cfg(test)]"):]
+    ol = re.search(r"omega_lambda: ([0-9.]+)", tests).group(1)
+    o0 = re.search(r"omega_0: ([0-9.]+)", tests).group(1)
+    h = re.search(r"\(cosmology, ([0-9.]+)\.into\(\)\)", tests).group(1)
+    diff = re.search(r"diff\(([0-9.]+), ([0-9.]+)\) - Time::gigayears\(([0-9.]+)\)\)\.abs\(\) < Time::years\(([0-9.]+)\)",
+                     tests)
+    grid = re.search(r"for a0 in \[([0-9., ]+)\]", tests).group(1)
+    tol = re.search(r"assert!\(diff < ([0-9.eE+-]+)\)", tests).group(1)
+    out["cosmology"] = {
+        "omega_lambda": float(ol), "omega_0": float(o0), "h": float(h),
+        "time_difference": {"a0": float(diff.group(1)), "a1": float(diff.group(2)),
+                            "gigayears": float(diff.group(3)), "tolerance_years": float(diff.group(4))},
+        "round_trip_scale_factors": [float(v) for v in grid.split(",")],
+        "round_trip_tolerance": rust_float(tol)}
 
     dest = pathlib.Path(__file__).with_name("reference_kats.json")
     dest.write_text(json.dumps(out, indent=1) + "\n")
