@@ -12,7 +12,7 @@ import pathlib
 import numpy as np
 import pytest
 
-from subsweep_gb300 import arepo, bpass_table, hdf5
+from subsweep_gb300 import arepo, bpass_table
 from subsweep_gb300.cosmology import YEAR, Cosmology
 from hdf5_writer import H5Writer
 
