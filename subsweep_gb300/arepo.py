@@ -36,6 +36,7 @@ reference does; `read_initial_conditions` reads the gas state the sweep starts f
 """
 from __future__ import annotations
 
+import dataclasses
 import pathlib
 import re
 from typing import Optional
@@ -353,3 +354,30 @@ def dependency_cycles(grid: Grid, directions: np.ndarray) -> int:
             reached += frontier.size
         stuck += n - reached
     return int(stuck)
+
+
+def read_postprocess_inputs(grid_file, snapshot_paths, cosmology: Optional[hdf5.Cosmology], periodic: bool,
+                            escape_fraction: Optional[float] = None, sources=None,
+                            initial_fraction_ionized_hydrogen: Optional[float] = None, remap_from=None) -> dict:
+    """Everything `Sweep` takes for post-processing an Arepo run with a grid file, in the
+    snapshot's cell order, as the reference's post-processing startup assembles it
+    (src/main.rs:30-140): the grid (`read_grid_file`), the gas state
+    (`read_initial_conditions`, with `remap_from`), and the per-cell source rates, from
+    the star particles (`read_sources`, `escape_fraction` given) or from explicit
+    `sources` = (positions [n, 3] in m, rates in photons/s), each on its nearest cell.
+    Returns a dict with grid, density, ionized_hydrogen_fraction, temperature, source
+    and position."""
+    if (escape_fraction is None) == (sources is None):
+        raise ValueError("give either escape_fraction (sources from the star particles) or explicit sources")
+    grid = read_grid_file(grid_file, snapshot_paths, periodic, cosmology)
+    ic = read_initial_conditions(snapshot_paths, initial_fraction_ionized_hydrogen, cosmology, remap_from)
+    if ic["density"].shape[0] != grid.num_cells:
+        raise hdf5.H5Error(f"the snapshot has {ic['density'].shape[0]} gas cells, its grid {grid.num_cells}")
+    if sources is None:
+        src_pos, src_rates = read_sources(snapshot_paths, cosmology, escape_fraction)
+    else:
+        src_pos, src_rates = (np.asarray(a, np.float64) for a in sources)
+    grid = dataclasses.replace(grid, position=ic["position"])
+    return {"grid": grid, "density": ic["density"], "ionized_hydrogen_fraction": ic["ionized_hydrogen_fraction"],
+            "temperature": ic["temperature"], "source": source_rates(ic["position"], src_pos, src_rates),
+            "position": ic["position"]}

@@ -362,3 +362,69 @@ def test_read_initial_conditions_with_remap(tmp_path):
     np.testing.assert_array_equal(remapped["ionized_hydrogen_fraction"], x)
     np.testing.assert_array_equal(remapped["temperature"], t)
     np.testing.assert_array_equal(remapped["density"], plain["density"])
+
+
+def test_read_postprocess_inputs_runs_on_the_oracle(voronoi_pair, tmp_path):
+    """Grid file + snapshot (gas and stars) -> the inputs of a sweep, in the snapshot's
+    cell order; they equal the pieces read one by one, and the oracle steps them."""
+    from hdf5_writer import H5Writer
+    from subsweep_gb300 import hdf5
+    from subsweep_gb300.cosmology import Cosmology
+
+    w, _ = voronoi_pair
+    g = w.grid
+    rng = np.random.default_rng(31)
+    n = g.num_cells
+    uid = rng.choice(10 ** 9, size=n, replace=False).astype(np.uint64)
+    id1, id2, ctype, area, normal = to_connections(g, uid.astype(np.int64), rng)
+    cosmo = Cosmology(a=0.5, h=0.7, omega_0=0.3, omega_lambda=0.7)
+    one = dict(a=0, h=0)
+    rho = rng.uniform(0.5, 2.0, n) * w.density
+    s = H5Writer()
+    s.dataset("PartType0/ParticleIDs", uid)
+    s.dataset("PartType0/Masses", rho * g.volume * 1e3, attrs=_arepo_attrs(1.0, mass=1, **one))
+    s.dataset("PartType0/Density", rho * 1e-3, attrs=_arepo_attrs(1.0, length=-3, mass=1, **one))
+    s.dataset("PartType0/InternalEnergy", rng.uniform(1e11, 1e12, n), attrs=_arepo_attrs(1.0, velocity=2, **one))
+    s.dataset("PartType0/ElectronAbundance", rng.uniform(0, 1e-3, n), attrs=_arepo_attrs(0.0))
+    s.dataset("PartType0/Coordinates", g.position * 100.0, attrs=_arepo_attrs(1.0, length=1, **one))
+    stars = g.position[rng.choice(n, 5, replace=False)] * 100.0
+    s.dataset("PartType4/Coordinates", stars, attrs=_arepo_attrs(1.0, length=1, **one))
+    s.dataset("PartType4/GFM_Metallicity", np.full(5, 0.01), attrs=_arepo_attrs(0.0))
+    s.dataset("PartType4/GFM_StellarFormationTime", np.array([0.49, 0.495, 0.48, -1.0, 0.499]),
+              attrs=_arepo_attrs(0.0))
+    s.dataset("PartType4/Masses", np.full(5, 1e5 * 1.988477e33), attrs=_arepo_attrs(1.0, mass=1, **one))
+    s.write(tmp_path / "snap.hdf5")
+    gw = H5Writer()
+    for name, arr in (("Id1", id1.astype(np.uint64)), ("Id2", id2.astype(np.uint64)), ("ConnectionType", ctype)):
+        gw.dataset(name, arr)
+    gw.dataset("Area", area * 1e4, attrs=_arepo_attrs(1.0, length=2, **one))
+    gw.dataset("Normal", normal, attrs=_arepo_attrs(0.0))
+    gw.write(tmp_path / "grid.hdf5")
+
+    inp = arepo.read_postprocess_inputs(tmp_path / "grid.hdf5", tmp_path / "snap.hdf5", cosmo, periodic=True,
+                                        escape_fraction=0.1)
+    grid = arepo.read_grid_file(tmp_path / "grid.hdf5", tmp_path / "snap.hdf5", True, cosmo)
+    ic = arepo.read_initial_conditions(tmp_path / "snap.hdf5", cosmology=cosmo)
+    pos, rates = arepo.read_sources(tmp_path / "snap.hdf5", cosmo, 0.1)
+    assert pos.shape == (4, 3)  # the wind particle is dropped
+    for field in ("row_ptr", "nbr", "kind", "area", "normal", "volume"):
+        np.testing.assert_array_equal(getattr(inp["grid"], field), getattr(grid, field))
+    np.testing.assert_array_equal(inp["grid"].position, ic["position"])
+    for k in ("density", "ionized_hydrogen_fraction", "temperature"):
+        np.testing.assert_array_equal(inp[k], ic[k])
+    np.testing.assert_array_equal(inp["source"], arepo.source_rates(ic["position"], pos, rates))
+    assert np.count_nonzero(inp["source"]) == 4 and inp["source"].sum() == pytest.approx(rates.sum(), rel=1e-12)
+    np.testing.assert_allclose(inp["grid"].volume, g.volume, rtol=1e-12)
+    with pytest.raises(ValueError, match="either escape_fraction"):
+        arepo.read_postprocess_inputs(tmp_path / "grid.hdf5", tmp_path / "snap.hdf5", cosmo, True)
+
+    def run(source):
+        o = binding.OracleSweep(w.params, inp["grid"], inp["density"], inp["ionized_hydrogen_fraction"],
+                                inp["temperature"], source, oracle_dirs(w.params))
+        for _ in range(2):
+            o.run_sweeps()
+        return o.fields()["ionized_hydrogen_fraction"]
+
+    lit, dark = run(inp["source"]), run(np.zeros(n))
+    assert np.all(np.isfinite(lit)) and np.all(lit >= dark)
+    assert np.all(lit[inp["source"] > 0] > dark[inp["source"] > 0])
