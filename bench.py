@@ -389,6 +389,29 @@ def precision_errors(mixed: dict, fp64: dict, lv_mixed, lv_fp64, total_source: f
                               "level": int(lv_fp64[worst]), "photon_rate_rel": float(r_f[worst] / total_source)})
 
 
+def write_back_split(s, reps: int = 3) -> dict:
+    """The e2e write-back after the timed steps, split (median ms of `reps` calls on the
+    state of the last timed step, outside the timed region): sw_get_fields with the
+    photon rate, and without it (the three per-cell copies alone); the difference is the
+    photon-rate export.  Diagnostic only: an error is reported, never raised."""
+    try:
+        n = s.num_cells
+        out = {k: np.empty(n) for k in ("ionized_hydrogen_fraction", "temperature", "timestep", "photon_rate")}
+        s.fields(out)  # the buffers' pages touched once, as in the timed steps
+
+        def median_ms(photon_rate: bool) -> float:
+            times = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                s.fields(out, photon_rate=photon_rate)
+                times.append(1e3 * (time.perf_counter() - t0))
+            return float(np.median(times))
+
+        return {"fields_ms": median_ms(True), "fields_without_photon_rate_ms": median_ms(False), "calls": reps}
+    except Exception as e:  # noqa: BLE001
+        return {"error": repr(e)}
+
+
 def radiation_field(s, w) -> dict:
     """How far the radiation reaches: the fraction of (cell, direction) incoming rates
     above 1e-6 of the total source per direction, of cells whose photon rate is above
@@ -492,6 +515,7 @@ def run_ours(args, dist: Dist):
         (fm, lm), (ff, lf) = snaps["mixed"], snaps["fp64"]
         err = dict(precision_errors(fm, ff, lm, lf, total_source), after_timed_steps=k_common)
     field = radiation_field(s, w) if dist.rank == 0 else None
+    write_back = write_back_split(s) if dist.rank == 0 else None
     n = w.grid.num_cells
     e2e_max = dist.allreduce(results[head]["timing"]["wall_s"], "max")
     e2e_tasks = dist.allreduce(float(results[head]["d"]["tasks"]), "sum")
@@ -554,7 +578,7 @@ def run_ours(args, dist: Dist):
         "periodic_semantics_vs_reference_order": semantics,
         # the same timed steps, host wall time of sw_step + the field write-back
         "e2e": {"value": e2e_tasks / e2e_max, "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 4 * 8 * n},
+                "d2h_bytes_per_step": 4 * 8 * n, "write_back": write_back},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": (achieved_gbs / peaks["hbm_gbs"]) if achieved_gbs else None,
                      "traffic": traffic, "traffic_unit": "bytes per launch",

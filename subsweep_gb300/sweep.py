@@ -187,14 +187,17 @@ class Sweep:
         return te.value
 
     # -- fields ----------------------------------------------------------------
-    def fields(self, out: Optional[dict] = None) -> dict:
-        """x_HII, T, species timestep and PhotonRate per cell (run_sweep_system write-back)."""
+    def fields(self, out: Optional[dict] = None, photon_rate: bool = True) -> dict:
+        """x_HII, T, species timestep and PhotonRate per cell (run_sweep_system write-back);
+        with photon_rate=False the photon rate (a device reduction over the directions) is
+        neither formed nor copied."""
         n = self.num_cells
+        keys = ("ionized_hydrogen_fraction", "temperature", "timestep") + (("photon_rate",) if photon_rate else ())
         if out is None:
-            out = {k: np.empty(n) for k in ("ionized_hydrogen_fraction", "temperature", "timestep", "photon_rate")}
+            out = {k: np.empty(n) for k in keys}
         self._check(self._lib.sw_get_fields(
             self._h, out["ionized_hydrogen_fraction"].ctypes.data, out["temperature"].ctypes.data,
-            out["timestep"].ctypes.data, out["photon_rate"].ctypes.data))
+            out["timestep"].ctypes.data, out["photon_rate"].ctypes.data if photon_rate else None))
         return out
 
     def cell_state(self) -> dict:

@@ -52,3 +52,34 @@ def test_reference_arm_json_line():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     mapped = [l for l in out.stdout.splitlines() if l.startswith("MAPPED")][0]
     assert "liboracle.so" in mapped and "libsubsweep" not in mapped, mapped
+
+
+def test_write_back_split_reports_and_never_raises():
+    """The e2e write-back split of the GPU arm, on stand-ins for a handle: the median
+    times of fields() with and without the photon rate, and an error captured, not
+    raised."""
+    import time as _time
+
+    import bench
+
+    class Handle:
+        num_cells = 4
+
+        def __init__(self):
+            self.calls = []
+
+        def fields(self, out, photon_rate=True):
+            self.calls.append(photon_rate)
+            _time.sleep(0.004 if photon_rate else 0.001)
+            return out
+
+    h = Handle()
+    got = bench.write_back_split(h, reps=3)
+    assert got["calls"] == 3 and h.calls == [True] * 4 + [False] * 3
+    assert got["fields_ms"] > got["fields_without_photon_rate_ms"] > 0.5
+
+    class Broken(Handle):
+        def fields(self, out, photon_rate=True):
+            raise RuntimeError("no device")
+
+    assert "no device" in bench.write_back_split(Broken())["error"]
