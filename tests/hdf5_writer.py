@@ -265,13 +265,28 @@ class H5Writer:
             heap += _pad8(name.encode() + b"\0")
         heap_data = self._append(heap)
         heap_at = self._append(b"HEAP" + struct.pack("<B3xQQQ", 0, len(heap), UNDEF, heap_data))
-        snod = b"SNOD" + struct.pack("<BBH", 1, 0, len(names))
-        for name in names:
-            snod += struct.pack("<QQII16x", offsets[name], children[name], 0, 0)
-        snod_at = self._append(snod)
-        last = offsets[names[-1]] if names else 0
-        tree = self._append(b"TREE" + struct.pack("<BBHQQ", 0, 0, 1, UNDEF, UNDEF) +
-                            struct.pack("<QQQ", 0, snod_at, last))
+        # symbol nodes of at most 2 * leaf K = 8 entries, as the library splits them; a
+        # tree node holds at most 2 * internal K = 32 children, so larger groups get a
+        # second level
+        leaves = []  # (address, heap offset of the node's last name)
+        for i in range(0, max(len(names), 1), 8):
+            part = names[i:i + 8]
+            snod = b"SNOD" + struct.pack("<BBH", 1, 0, len(part))
+            for name in part:
+                snod += struct.pack("<QQII16x", offsets[name], children[name], 0, 0)
+            leaves.append((self._append(snod), offsets[part[-1]] if part else 0))
+
+        def node(level, kids):
+            body = b"TREE" + struct.pack("<BBHQQ", 0, level, len(kids), UNDEF, UNDEF) + struct.pack("<Q", 0)
+            for addr, last in kids:
+                body += struct.pack("<QQ", addr, last)
+            return self._append(body)
+
+        if len(leaves) <= 32:
+            tree = node(0, leaves)
+        else:
+            tree = node(1, [(node(0, leaves[i:i + 32]), leaves[min(i + 32, len(leaves)) - 1][1])
+                            for i in range(0, len(leaves), 32)])
         msgs = [_message(0x11, struct.pack("<QQ", tree, heap_at))]
         msgs += [_attribute(k, v) for k, v in g["attrs"].items()]
         return self._header(msgs)

@@ -127,6 +127,21 @@ def test_round_trip_chunked(tmp_path, filters, fanout):
             np.testing.assert_array_equal(f["rows"].read(lo, hi), rows[lo:hi])
 
 
+@pytest.mark.parametrize("members", [1, 40, 300])
+def test_groups_of_many_members(tmp_path, members):
+    """Groups whose members fill several symbol nodes (8 entries each, as the library
+    writes them: a snapshot's PartType0 holds tens of datasets) and, past 256 members,
+    a two-level group B-tree."""
+    w, path = _write(tmp_path)
+    for i in range(members):
+        w.dataset(f"PartType0/field_{i:03d}", np.full(3, float(i)))
+    w.write(path)
+    with hdf5.File(path) as f:
+        assert f["PartType0"].keys() == [f"field_{i:03d}" for i in range(members)]
+        for i in (0, members // 2, members - 1):
+            np.testing.assert_array_equal(f[f"PartType0/field_{i:03d}"].read(), np.full(3, float(i)))
+
+
 def test_chunk_filter_mask(tmp_path):
     """A chunk stored with a filter skipped (its bit set in the chunk's filter mask) is
     decoded without that filter."""
