@@ -393,7 +393,8 @@ def write_back_split(s, reps: int = 3) -> dict:
     """The e2e write-back after the timed steps, split (median ms of `reps` calls on the
     state of the last timed step, outside the timed region): sw_get_fields with the
     photon rate, and without it (the three per-cell copies alone); the difference is the
-    photon-rate export.  Diagnostic only: an error is reported, never raised."""
+    photon-rate export.  With it, the number of cells at each timestep level.  Diagnostic
+    only: an error is reported, never raised."""
     try:
         n = s.num_cells
         out = {k: np.empty(n) for k in ("ionized_hydrogen_fraction", "temperature", "timestep", "photon_rate")}
@@ -407,7 +408,10 @@ def write_back_split(s, reps: int = 3) -> dict:
                 times.append(1e3 * (time.perf_counter() - t0))
             return float(np.median(times))
 
-        return {"fields_ms": median_ms(True), "fields_without_photon_rate_ms": median_ms(False), "calls": reps}
+        split = {"fields_ms": median_ms(True), "fields_without_photon_rate_ms": median_ms(False), "calls": reps}
+        # the export's cost follows the cells left behind by later sweeps: the level mix
+        split["cells_per_level"] = np.bincount(s.cell_state()["level"]).tolist()
+        return split
     except Exception as e:  # noqa: BLE001
         return {"error": repr(e)}
 

@@ -73,10 +73,14 @@ def test_write_back_split_reports_and_never_raises():
             _time.sleep(0.004 if photon_rate else 0.001)
             return out
 
+        def cell_state(self):
+            return {"level": np.array([0, 3, 3, 1], np.uint8)}
+
     h = Handle()
     got = bench.write_back_split(h, reps=3)
     assert got["calls"] == 3 and h.calls == [True] * 4 + [False] * 3
     assert got["fields_ms"] > got["fields_without_photon_rate_ms"] > 0.5
+    assert got["cells_per_level"] == [1, 1, 0, 2]
 
     class Broken(Handle):
         def fields(self, out, photon_rate=True):
