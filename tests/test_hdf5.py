@@ -361,3 +361,35 @@ def test_deflate_bytes_are_zlib(tmp_path):
     raw = path.read_bytes()
     stream = zlib.compress(arr.tobytes(), 6)
     assert raw.find(stream) > 0
+
+
+def test_random_round_trips(tmp_path_factory):
+    """Random datasets through the writer and the reader: shapes of rank 1 to 3, integer
+    and float types of both byte orders, contiguous or chunked layouts with random
+    chunk shapes and filter pipelines, and random row ranges."""
+    hypothesis = pytest.importorskip("hypothesis")
+    st = hypothesis.strategies
+
+    dtypes = st.sampled_from(["<f8", ">f8", "<f4", ">f4", "<i4", ">i8", "<u2", "|u1", "<f2"])
+    filters = st.sampled_from([(), ("deflate",), ("shuffle", "deflate"), ("shuffle", "deflate", "fletcher32")])
+
+    @hypothesis.settings(max_examples=60, deadline=None)
+    @hypothesis.given(shape=st.lists(st.integers(0, 9), min_size=1, max_size=3), dtype=dtypes,
+                      chunked=st.booleans(), chunk_seed=st.integers(0, 2 ** 16), filt=filters,
+                      fanout=st.sampled_from([None, 2, 5]), rows=st.tuples(st.integers(-12, 12), st.integers(-12, 12)))
+    def check(shape, dtype, chunked, chunk_seed, filt, fanout, rows):
+        rng = np.random.default_rng(chunk_seed)
+        data = (rng.random(shape) * 200 - 100).astype(dtype)
+        path = tmp_path_factory.mktemp("rt") / "x.hdf5"
+        w = H5Writer()
+        if chunked and all(s > 0 for s in shape):
+            chunks = tuple(int(rng.integers(1, s + 1)) for s in shape)
+            w.dataset("d", data, layout="chunked", chunks=chunks, filters=filt, btree_fanout=fanout)
+        else:
+            w.dataset("d", data)
+        w.write(path)
+        with hdf5.File(path) as f:
+            np.testing.assert_array_equal(f["d"].read(), data)
+            np.testing.assert_array_equal(f["d"].read(*rows), data[rows[0]:rows[1]])
+
+    check()
