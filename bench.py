@@ -316,8 +316,10 @@ def time_precision(w, precision: str, device: int, warmup: int, steps: int, dist
     host arrays (the same steps).  The fields and levels after `snapshot_after` timed
     steps are kept (outside the timed region) for the comparison of precisions."""
     from subsweep_gb300 import Sweep
+    t_create = time.perf_counter()
     s = Sweep(w.params, w.grid, w.density, w.ionized_hydrogen_fraction, w.temperature, w.source,
               precision=precision, device=device, use_graphs=graphs and precision == "mixed")
+    create_s = time.perf_counter() - t_create
     for _ in range(warmup):
         s.run_sweeps()
     n = w.grid.num_cells
@@ -345,7 +347,7 @@ def time_precision(w, precision: str, device: int, warmup: int, steps: int, dist
     d = {k: st1[k] - st0[k] for k in st1}
     for k in ("task_spaces", "device_bytes", "pull_variant", "schedule_levels"):  # states, not counters
         d[k] = st1[k]
-    return s, d, clocks, {"per_step_ms": per_step, "wall_s": wall, "snapshot": snap}
+    return s, d, clocks, {"per_step_ms": per_step, "wall_s": wall, "snapshot": snap, "create_s": create_s}
 
 
 def precision_errors(mixed: dict, fp64: dict, lv_mixed, lv_fp64, total_source: float) -> dict:
@@ -564,7 +566,9 @@ def run_ours(args, dist: Dist):
         "dtype": "f32 transport + f64 chemistry" if head == "mixed" else "f64",
         "data": "synthetic",
         "config": dict(workload_config(w), precision=head, replicas=args.gpus, cuda_graph_steps=bool(args.graphs),
-                       grid_build_s=round(grid_s, 1), grid_builder="gpu"),
+                       grid_build_s=round(grid_s, 1), grid_builder="gpu",
+                       # sw_create: upload, schedule, records and slots (outside the timed steps)
+                       handle_create_s={p: round(r["timing"]["create_s"], 1) for p, r in results.items()}),
         "chem_cells_per_s": main["chem_cells_per_s"],
         "chemistry": chemistry_figures(d, main),
         "fp64": ({**{k: fp64[k] for k in ("cell_dir_updates_per_s", "chem_cells_per_s", "ms_per_step",
